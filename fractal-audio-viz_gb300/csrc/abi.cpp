@@ -1,0 +1,950 @@
+// The extern "C" boundary: renderer.h v10 hot subset plus GB300 extensions.
+//
+// Validation, error strings and the 0/1/NULL conventions follow the
+// reference's exported API (renderer.cpp:15870-20535, render entry points at
+// :19568-20013 and :20280-20474).  Every render and colour call runs on the
+// GPU; no C++ exception crosses the boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device.h"
+#include "fractal_gb300.h"
+#include "reference.h"
+#include "runtime.h"
+
+namespace fgb {
+
+thread_local std::string last_error;
+
+void set_error(const std::string& message) { last_error = message; }
+
+void check_cuda(cudaError_t status, const char* what) {
+    if (status != cudaSuccess) {
+        throw Failure{std::string(what) + ": " + cudaGetErrorString(status)};
+    }
+}
+
+int current_device() {
+    int device = -1;
+    check_cuda(cudaGetDevice(&device), "cudaGetDevice");
+    return device;
+}
+
+ThreadRuntime::~ThreadRuntime() {
+    for (void* p : scratch) cudaFree(p);
+    cudaFree(stats);
+    cudaFree(stamp);
+    if (start) cudaEventDestroy(start);
+    if (stop) cudaEventDestroy(stop);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+ThreadRuntime& thread_runtime() {
+    thread_local ThreadRuntime rt;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        throw Failure{"no CUDA device is available; this library renders on the GPU only"};
+    }
+    const int device = current_device();
+    if (rt.stream == nullptr || rt.device != device) {
+        rt.~ThreadRuntime();
+        new (&rt) ThreadRuntime();
+        rt.device = device;
+        check_cuda(cudaStreamCreateWithFlags(&rt.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaMalloc(&rt.stats, sizeof(unsigned long long) * kStatsSlots), "cudaMalloc (stats)");
+        check_cuda(cudaMalloc(&rt.stamp, sizeof(unsigned long long)), "cudaMalloc (stamp)");
+        check_cuda(cudaEventCreate(&rt.start), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&rt.stop), "cudaEventCreate");
+    }
+    return rt;
+}
+
+void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes) {
+    if (bytes == 0) bytes = 1;
+    if (rt.capacity[slot] < bytes) {
+        // The stream may still use the old buffer.
+        check_cuda(cudaStreamSynchronize(rt.stream), "cudaStreamSynchronize");
+        cudaFree(rt.scratch[slot]);
+        rt.scratch[slot] = nullptr;
+        rt.capacity[slot] = 0;
+        check_cuda(cudaMalloc(&rt.scratch[slot], bytes), "cudaMalloc (scratch)");
+        rt.capacity[slot] = bytes;
+    }
+    return rt.scratch[slot];
+}
+
+namespace {
+
+constexpr int kMaxIterations = 10'000'000;
+constexpr int kMaxThreads = 4096;
+constexpr long long kMaxPixels = 100'000'000;
+constexpr int kStatsFields = 16;
+
+// ----------------------------------------------------------------- stats
+std::atomic<bool> stats_enabled{false};
+std::mutex stats_mutex;
+std::array<unsigned long long, kStatsSlots> last_stats{};
+
+void publish_stats(const std::array<unsigned long long, kStatsSlots>& values) {
+    std::lock_guard<std::mutex> lock(stats_mutex);
+    last_stats = values;
+}
+
+// ------------------------------------------------------------ validation
+bool valid_dims(int width, int height) {
+    if (width <= 0 || height <= 0) return false;
+    return static_cast<unsigned long long>(width)
+        <= static_cast<unsigned long long>(kMaxPixels) / static_cast<unsigned long long>(height);
+}
+bool valid_iterations(int value) { return value > 0 && value <= kMaxIterations; }
+bool valid_threads(int value) { return value >= 0 && value <= kMaxThreads; }
+bool valid_precision(int value) { return value >= 128 && value <= 131072; }
+bool valid_series(int order, int block) { return order >= 1 && order <= 32 && block >= 2 && block <= 4096; }
+bool valid_formula(int formula) { return formula >= 0 && formula <= 3; }
+
+bool valid_planes(const FractalRenderPlanes* planes, int width, int height) {
+    if (!planes || !valid_dims(width, height)) return false;
+    return planes->struct_size >= sizeof(FractalRenderPlanes) && planes->version == 1
+        && planes->orbit_iteration && planes->phase && planes->de_x && planes->de_y && planes->test1
+        && planes->test2;
+}
+
+FractalRenderOptions default_options() {
+    FractalRenderOptions o{};
+    o.struct_size = sizeof(FractalRenderOptions);
+    o.version = FRACTAL_RENDER_OPTIONS_VERSION;
+    o.strict = 1;
+    o.allow_recovery = 0;
+    o.time_budget_ms = 0;
+    o.disable_bla = 0;
+    o.disable_cycle = 0;
+    o.strict_cycle = 0;
+    o.series_min_terms = 8;
+    o.series_max_terms = 32;
+    o.max_bla_length = kMaxSafeBlaLength;
+    o.max_linear_bla_length = kMaxSafeLinearBlaLength;
+    o.backend = 0;
+    o.escape_radius_mode = 0;
+    o.coordinate_mode = 0;
+    o.output_bias = 0.0;
+    return o;
+}
+
+// checked_render_options (renderer.cpp:4729-4765).
+FractalRenderOptions checked_options(const FractalRenderOptions* supplied) {
+    FractalRenderOptions o = default_options();
+    if (!supplied) return o;
+    if (supplied->struct_size < sizeof(FractalRenderOptions) || supplied->version != FRACTAL_RENDER_OPTIONS_VERSION) {
+        throw Failure{"unsupported FractalRenderOptions version or size"};
+    }
+    o = *supplied;
+    auto flag = [](std::int32_t value, const char* label) {
+        if (value != 0 && value != 1) throw Failure{std::string(label) + " must be 0 or 1"};
+    };
+    flag(o.strict, "strict render flag");
+    flag(o.allow_recovery, "recovery flag");
+    flag(o.disable_bla, "disable-BLA flag");
+    flag(o.disable_cycle, "disable-cycle flag");
+    flag(o.strict_cycle, "strict-cycle flag");
+    if (o.escape_radius_mode != 0 && o.escape_radius_mode != 1) throw Failure{"unknown escape-radius mode"};
+    if (o.coordinate_mode != 0 && o.coordinate_mode != 1) throw Failure{"unknown coordinate mode"};
+    o.series_min_terms = std::clamp(o.series_min_terms, 1, 32);
+    o.series_max_terms = std::clamp(o.series_max_terms, o.series_min_terms, 32);
+    o.max_bla_length = std::clamp(o.max_bla_length, 1, kMaxSafeBlaLength);
+    o.max_linear_bla_length = std::clamp(o.max_linear_bla_length, 1, kMaxSafeLinearBlaLength);
+    if (o.time_budget_ms < 0) throw Failure{"render time budget cannot be negative"};
+    if (!std::isfinite(o.output_bias) || o.output_bias < 0.0) {
+        throw Failure{"render output bias must be finite and non-negative"};
+    }
+    return o;
+}
+
+void check_backend(const FractalRenderOptions& o) {
+    if (o.backend == 0 || o.backend == FRACTAL_BACKEND_CUDA) return;
+    if (o.backend == 1) throw Failure{"AVX2 backend requested but this build has no AVX2 support"};
+    if (o.backend == 2) throw Failure{"OpenCL backend is not available in this build"};
+    throw Failure{"unknown native render backend"};
+}
+
+// ------------------------------------------------------------ render core
+
+long double fe_log10(const fx::Fe& v) {
+    const long double log_two = 0.693147180559945309417232121458176568L;
+    return (std::log(std::fabs(static_cast<long double>(v.m))) + static_cast<long double>(v.e) * log_two)
+        / std::log(10.0L);
+}
+
+// Per-render geometry shared by the deep kernels (renderer.cpp:12690-12762).
+struct DeepGeometry {
+    fx::Fe view_height;
+    fx::Fe view_width;
+    fx::Fe pixel_spacing;
+    fx::Fe current_input_radius;
+};
+
+DeepGeometry deep_geometry(const fx::Fe& zoom, int width, int height, int coordinate_mode) {
+    DeepGeometry g;
+    const fx::Fe inverse_zoom = fx::fe_div(fx::fe_from(1.0, 0), zoom);
+    const double factor = viewport_height_factor(coordinate_mode);
+    g.view_height = fx::fe_mul(inverse_zoom, factor);
+    g.view_width = fx::fe_mul(g.view_height, static_cast<double>(width) / static_cast<double>(height));
+    g.pixel_spacing = fx::fe_div(g.view_height, fx::fe_from(static_cast<double>(height), 0));
+    g.current_input_radius = fx::fe_mul(inverse_zoom, factor);
+    return g;
+}
+
+void launch_deep_mandelbrot(ReferenceContext& ctx, DeviceTables& dev, const Outputs& out, int width, int height,
+                            const fx::Fe& zoom, int max_iter, int series_order, int series_block,
+                            const FractalRenderOptions& o, bool collect_stats, ThreadRuntime& rt,
+                            cudaStream_t stream) {
+    const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+    const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
+    const bool disable_bla = !covers || o.disable_bla != 0;
+    const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
+    const bool use_deep = fx::fe_cmp(g.current_input_radius, ctx.deep_input_radius) <= 0;
+    const fx::Fe ultra = fx::fe_mul(ctx.input_radius, 1.0e-40);
+    const bool use_ultra = fx::fe_cmp(g.current_input_radius, ultra) <= 0;
+    PlainParams p{};
+    p.orbit = dev.orbit;
+    p.orbit_size = dev.orbit_size;
+    p.cubic = dev.cubic;
+    p.cubic_index = dev.cubic_index;
+    p.linear = use_deep ? dev.deep_linear : dev.linear;
+    p.linear_index = use_deep ? dev.deep_linear_index : dev.linear_index;
+    p.series = dev.series;
+    p.series_terms = dev.series_terms;
+    p.series_iteration = ctx.series.iteration;
+    p.series_on = ctx.series.enabled && ctx.series.order >= o.series_min_terms
+        && ctx.series.order <= o.series_max_terms
+        && fx::fe_cmp(g.current_input_radius, fx::fe_sqrt(ctx.series.r2)) <= 0
+        && ctx.series.iteration < max_iter && dev.series_terms > 1;
+    p.series_r2 = fx::nrm_make(ctx.series.r2.m, ctx.series.r2.e);
+    p.view_width = g.view_width;
+    p.view_height = g.view_height;
+    p.coordinate_mode = o.coordinate_mode;
+    p.width = width;
+    p.height = height;
+    p.max_iter = max_iter;
+    p.map_end = ctx.map_end;
+    p.disable_bla = disable_bla;
+    p.strict = o.strict;
+    p.allow_recovery = o.allow_recovery;
+    p.strict_cycle = o.strict_cycle;
+    p.cycle = cycle ? 1 : 0;
+    p.escape_mode = o.escape_radius_mode;
+    p.max_bla_len = std::clamp(std::min(series_block, static_cast<int>(o.max_bla_length)), 2, kMaxSafeBlaLength);
+    p.max_lin_len = std::clamp(std::min(series_block, static_cast<int>(o.max_linear_bla_length)), 2,
+                               use_ultra ? kMaxSafeLinearBlaLength
+                                         : (use_deep ? kMaxSafeDeepLinearBlaLength : kMaxSafeBlaLength));
+    p.approx_order = std::clamp(series_order, 1, 3);
+    p.output_bias = o.output_bias;
+    p.pixel_spacing = g.pixel_spacing;
+    p.out = out.field;
+    p.counts = out.counts;
+    p.p_iter = out.p_iter;
+    p.p_phase = out.p_phase;
+    p.p_dex = out.p_dex;
+    p.p_dey = out.p_dey;
+    p.p_t1 = out.p_t1;
+    p.p_t2 = out.p_t2;
+    if (o.time_budget_ms > 0) {
+        check_cuda(launch_stamp_time(rt.stamp, stream), "time stamp launch");
+        p.deadline_base = rt.stamp;
+        p.budget_ns = static_cast<unsigned long long>(o.time_budget_ms) * 1000000ull;
+    }
+    p.stats = collect_stats ? rt.stats : nullptr;
+    check_cuda(launch_plain_mandelbrot(p, out.p_iter != nullptr, collect_stats, stream),
+               "plain Mandelbrot kernel launch");
+}
+
+void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outputs& out, int width, int height,
+                           const fx::Fe& zoom, int max_iter, const FractalRenderOptions& o, bool collect_stats,
+                           ThreadRuntime& rt, cudaStream_t stream) {
+    const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+    AltParams p{};
+    p.orbit = dev.orbit;
+    p.orbit_size = dev.orbit_size;
+    p.alt = dev.alt;
+    p.alt_index = dev.alt_index;
+    p.alt_start = ctx.alt_start;
+    p.alt_input_radius2 = ctx.alt_input_radius2;
+    p.series = dev.series;
+    p.series_terms = dev.series_terms;
+    p.series_iteration = ctx.series.iteration;
+    p.series_r2 = fx::nrm_make(ctx.series.r2.m, ctx.series.r2.e);
+    p.view_width = g.view_width;
+    p.view_height = g.view_height;
+    p.coordinate_mode = o.coordinate_mode;
+    p.width = width;
+    p.height = height;
+    p.max_iter = max_iter;
+    p.map_end = ctx.map_end;
+    p.formula = ctx.formula;
+    p.strict = o.strict;
+    p.allow_recovery = o.allow_recovery;
+    p.escape_mode = o.escape_radius_mode;
+    p.output_bias = o.output_bias;
+    p.pixel_spacing = g.pixel_spacing;
+    p.parameter = ctx.parameter;
+    p.current_input_radius2 = fx::fe_sqr(g.current_input_radius);
+    p.out = out.field;
+    p.counts = out.counts;
+    p.p_iter = out.p_iter;
+    p.p_phase = out.p_phase;
+    p.p_dex = out.p_dex;
+    p.p_dey = out.p_dey;
+    p.p_t1 = out.p_t1;
+    p.p_t2 = out.p_t2;
+    // Alternate-formula policy (render_alternate_reference_impl,
+    // renderer.cpp:12064-12140) is completed on the host here.
+    const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
+    p.disable_bla = (!covers || o.disable_bla != 0) ? 1 : 0;
+    p.max_lin_len = std::clamp(static_cast<int>(o.max_linear_bla_length), 1, kMaxSafeLinearBlaLength);
+    p.series_on = ctx.formula == kFormulaJulia && ctx.series.enabled
+        && ctx.series.order >= o.series_min_terms && ctx.series.order <= o.series_max_terms
+        && fx::fe_cmp(g.current_input_radius, fx::fe_sqrt(ctx.series.r2)) <= 0
+        && ctx.series.iteration < max_iter && dev.series_terms > 1;
+    if (o.time_budget_ms > 0) {
+        check_cuda(launch_stamp_time(rt.stamp, stream), "time stamp launch");
+        p.deadline_base = rt.stamp;
+        p.budget_ns = static_cast<unsigned long long>(o.time_budget_ms) * 1000000ull;
+    }
+    p.stats = collect_stats ? rt.stats : nullptr;
+    check_cuda(launch_plain_alternate(p, out.p_iter != nullptr, collect_stats, stream),
+               "plain alternate-formula kernel launch");
+}
+
+void launch_direct_render(const Outputs& out, int width, int height, long double zoom, long double x_center,
+                          long double y_center, int max_iter, int formula, double julia_re, double julia_im,
+                          const FractalRenderOptions& o, cudaStream_t stream) {
+    const double zoom_value = static_cast<double>(zoom);
+    const double center_re = static_cast<double>(x_center);
+    const double center_im = static_cast<double>(y_center);
+    if (!std::isfinite(zoom_value) || zoom_value <= 0.0 || !std::isfinite(center_re) || !std::isfinite(center_im)) {
+        throw Failure{"direct native coordinates or zoom exceed double range"};
+    }
+    const double height_span = viewport_height_factor(o.coordinate_mode) / zoom_value;
+    const double width_span = height_span * static_cast<double>(width) / static_cast<double>(height);
+    if (!std::isfinite(height_span) || !std::isfinite(width_span)) {
+        throw Failure{"direct native viewport is outside double range"};
+    }
+    DirectParams p{};
+    p.center_re = center_re;
+    p.center_im = center_im;
+    p.width_span = width_span;
+    p.height_span = height_span;
+    p.coordinate_mode = o.coordinate_mode;
+    p.width = width;
+    p.height = height;
+    p.max_iter = max_iter;
+    p.formula = formula;
+    p.julia_re = julia_re;
+    p.julia_im = julia_im;
+    p.output_bias = o.output_bias;
+    p.escape_mode = o.escape_radius_mode;
+    p.out = out.field;
+    p.counts = out.counts;
+    p.p_iter = out.p_iter;
+    p.p_phase = out.p_phase;
+    p.p_dex = out.p_dex;
+    p.p_dey = out.p_dey;
+    p.p_t1 = out.p_t1;
+    p.p_t2 = out.p_t2;
+    const std::uint32_t hints = static_cast<std::uint32_t>(o.reserved[0]);
+    p.need_phase = (hints & FRACTAL_RENDER_HINT_SKIP_PHASE) == 0;
+    p.need_de = (hints & FRACTAL_RENDER_HINT_SKIP_ANALYTIC_DE) == 0;
+    p.pixel_spacing = height_span / static_cast<double>(height);
+    check_cuda(launch_direct(p, stream), "direct kernel launch");
+}
+
+// Dispatch of a reference render by zoom depth and formula
+// (renderer.cpp:19868-19950): >= 1e6 deep paths, else the direct path.
+void render_from_reference(ReferenceContext& ctx, const Outputs& out, int width, int height,
+                           const char* zoom_text, int max_iter, int series_order, int series_block,
+                           const FractalRenderOptions& o, bool collect_stats, ThreadRuntime& rt,
+                           cudaStream_t stream) {
+    const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx.precision_bits);
+    const long double zoom_log10 = fe_log10(zoom);
+    if (zoom_log10 >= 6.0L) {
+        std::shared_ptr<DeviceTables> dev = device_tables(ctx);
+        if (ctx.formula != kFormulaMandelbrot) {
+            launch_deep_alternate(ctx, *dev, out, width, height, zoom, max_iter, o, collect_stats, rt, stream);
+        } else {
+            launch_deep_mandelbrot(ctx, *dev, out, width, height, zoom, max_iter, series_order, series_block, o,
+                                   collect_stats, rt, stream);
+        }
+        return;
+    }
+    const long double zoom_direct = parse_zoom_direct(zoom_text);
+    launch_direct_render(out, width, height, zoom_direct, ctx.x_center, ctx.y_center, max_iter, ctx.formula,
+                         ctx.julia_re, ctx.julia_im, o, stream);
+}
+
+// Host-buffer wrapper: device scratch, kernel, copies back, stats.
+void render_to_host(float* output, FractalRenderPlanes* planes, int width, int height,
+                    const std::function<void(const Outputs&, bool, ThreadRuntime&, cudaStream_t)>& launch) {
+    ThreadRuntime& rt = thread_runtime();
+    const auto started = std::chrono::steady_clock::now();
+    const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
+    Outputs out;
+    out.field = static_cast<float*>(scratch(rt, kScratchField, pixels * sizeof(float)));
+    if (planes) {
+        out.p_iter = static_cast<std::int64_t*>(scratch(rt, kScratchPlaneIter, pixels * sizeof(std::int64_t)));
+        out.p_phase = static_cast<double*>(scratch(rt, kScratchPhase, pixels * sizeof(double)));
+        out.p_dex = static_cast<double*>(scratch(rt, kScratchDeX, pixels * sizeof(double)));
+        out.p_dey = static_cast<double*>(scratch(rt, kScratchDeY, pixels * sizeof(double)));
+        out.p_t1 = static_cast<double*>(scratch(rt, kScratchTest1, pixels * sizeof(double)));
+        out.p_t2 = static_cast<double*>(scratch(rt, kScratchTest2, pixels * sizeof(double)));
+    }
+    const bool collect = stats_enabled.load(std::memory_order_relaxed);
+    if (collect) check_cuda(cudaMemsetAsync(rt.stats, 0, sizeof(unsigned long long) * kStatsSlots, rt.stream), "stats reset");
+    check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+    launch(out, collect, rt, rt.stream);
+    check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+    check_cuda(cudaMemcpyAsync(output, out.field, pixels * sizeof(float), cudaMemcpyDeviceToHost, rt.stream),
+               "copy field to host");
+    if (planes) {
+        check_cuda(cudaMemcpyAsync(planes->orbit_iteration, out.p_iter, pixels * sizeof(std::int64_t),
+                                   cudaMemcpyDeviceToHost, rt.stream), "copy planes");
+        check_cuda(cudaMemcpyAsync(planes->phase, out.p_phase, pixels * sizeof(double), cudaMemcpyDeviceToHost,
+                                   rt.stream), "copy planes");
+        check_cuda(cudaMemcpyAsync(planes->de_x, out.p_dex, pixels * sizeof(double), cudaMemcpyDeviceToHost,
+                                   rt.stream), "copy planes");
+        check_cuda(cudaMemcpyAsync(planes->de_y, out.p_dey, pixels * sizeof(double), cudaMemcpyDeviceToHost,
+                                   rt.stream), "copy planes");
+        check_cuda(cudaMemcpyAsync(planes->test1, out.p_t1, pixels * sizeof(double), cudaMemcpyDeviceToHost,
+                                   rt.stream), "copy planes");
+        check_cuda(cudaMemcpyAsync(planes->test2, out.p_t2, pixels * sizeof(double), cudaMemcpyDeviceToHost,
+                                   rt.stream), "copy planes");
+    }
+    std::array<unsigned long long, kStatsSlots> stats{};
+    if (collect) {
+        check_cuda(cudaMemcpyAsync(stats.data(), rt.stats, sizeof(unsigned long long) * kStatsSlots,
+                                   cudaMemcpyDeviceToHost, rt.stream), "copy stats");
+    }
+    check_cuda(cudaStreamSynchronize(rt.stream), "render");
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    if (collect) {
+        stats[22] = static_cast<unsigned long long>(  // render_ns
+            std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - started).count());
+        publish_stats(stats);
+    }
+}
+
+std::string julia_text(double value) {
+    char buffer[64];
+    if (std::snprintf(buffer, sizeof buffer, "%.17g", value) < 0) throw Failure{"failed to format the Julia constant"};
+    return buffer;
+}
+
+template <typename F>
+int guarded(const char* unknown, F&& body) {
+    try {
+        body();
+        set_error("");
+        return 0;
+    } catch (const Failure& failure) {
+        set_error(failure.message);
+        return 1;
+    } catch (const std::exception& error) {
+        set_error(error.what());
+        return 1;
+    } catch (...) {
+        set_error(unknown);
+        return 1;
+    }
+}
+
+template <typename F>
+void* guarded_handle(const char* unknown, F&& body) {
+    try {
+        void* handle = body();
+        set_error("");
+        return handle;
+    } catch (const Failure& failure) {
+        set_error(failure.message);
+    } catch (const std::exception& error) {
+        set_error(error.what());
+    } catch (...) {
+        set_error(unknown);
+    }
+    return nullptr;
+}
+
+void* create_handle(const char* x, const char* y, const char* zoom, int max_iter, int precision_bits,
+                    int series_order, bool retain, int formula, const char* jr, const char* ji,
+                    const FractalRenderOptions* supplied, const char* invalid_message) {
+    if (!x || !y || !zoom || !jr || !ji || !valid_iterations(max_iter) || !valid_precision(precision_bits)
+        || !valid_series(series_order, 2) || !valid_formula(formula)) {
+        throw Failure{invalid_message};
+    }
+    const FractalRenderOptions o = checked_options(supplied);
+    auto context = create_reference_context(x, y, zoom, max_iter, precision_bits, series_order, retain, formula,
+                                            jr, ji, o.escape_radius_mode, o.coordinate_mode);
+    return register_reference(std::move(context));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------- aurora palette
+// aurora_palette_for / colour_basis_for (renderer.cpp:4788-4923), built on
+// the host exactly as the reference does and cached per thread.
+namespace {
+
+struct AuroraCache {
+    int max_iter = -1;
+    double phase = 0, vocal = 0, pitch = 0;
+    std::vector<std::uint8_t> rgb;
+    int device = -1;
+    std::uint8_t* device_lut = nullptr;
+    std::size_t device_capacity = 0;
+};
+
+std::uint8_t colour_byte(double value) { return static_cast<std::uint8_t>(std::clamp(value, 0.0, 255.0)); }
+
+void build_aurora(AuroraCache& cache, int max_iter, double phase, double vocal, double pitch) {
+    const int size = std::min(65536, std::max(4096, max_iter * 4));
+    std::vector<float> cosine(static_cast<std::size_t>(size)), sine(static_cast<std::size_t>(size));
+    const double denominator = std::max(1, size - 1);
+    for (int i = 0; i < size; ++i) {
+        const double angle = 0.15 * static_cast<double>(max_iter) * static_cast<double>(i) / denominator;
+        cosine[static_cast<std::size_t>(i)] = static_cast<float>(std::cos(angle));
+        sine[static_cast<std::size_t>(i)] = static_cast<float>(std::sin(angle));
+    }
+    const double mix = std::clamp(vocal, 0.0, 1.0);
+    const double split = 5.0 * mix * mix;
+    const double rc = std::cos(phase), rs = std::sin(phase);
+    const double gc = std::cos(phase + split * 0.4), gs = std::sin(phase + split * 0.4);
+    const double bc = std::cos(phase + split), bs = std::sin(phase + split);
+    const double two_pi = 6.283185307179586476925286766559005768;
+    const double signed_pitch = std::clamp(2.0 * (pitch - 0.5), -1.0, 1.0);
+    const double hue = signed_pitch * 0.16 * two_pi;
+    const bool rotate = std::abs(hue) > 1.0e-15;
+    const double hcos = rotate ? std::cos(hue) : 1.0;
+    const double hsin = rotate ? std::sin(hue) : 0.0;
+    cache.rgb.resize(static_cast<std::size_t>(size) * 3);
+    for (int i = 0; i < size; ++i) {
+        const double c = cosine[static_cast<std::size_t>(i)];
+        const double s = sine[static_cast<std::size_t>(i)];
+        double r = (0.5 - 0.5 * (c * rc + s * rs)) * 140.0;
+        double g = (0.5 - 0.5 * (c * gc + s * gs)) * 140.0;
+        double b = (0.5 - 0.5 * (c * bc + s * bs)) * 140.0;
+        if (rotate) {
+            // Chroma rotation in YIQ (renderer.cpp:4815-4833).
+            const double y = 0.299 * r + 0.587 * g + 0.114 * b;
+            const double ii = 0.596 * r - 0.275 * g - 0.321 * b;
+            const double q = 0.212 * r - 0.523 * g + 0.311 * b;
+            const double ri = ii * hcos - q * hsin;
+            const double rq = ii * hsin + q * hcos;
+            const double nr = y + 0.956 * ri + 0.621 * rq;
+            const double ng = y - 0.272 * ri - 0.647 * rq;
+            const double nb = y - 1.106 * ri + 1.703 * rq;
+            r = nr;
+            g = ng;
+            b = nb;
+        }
+        cache.rgb[3 * static_cast<std::size_t>(i)] = colour_byte(r);
+        cache.rgb[3 * static_cast<std::size_t>(i) + 1] = colour_byte(g);
+        cache.rgb[3 * static_cast<std::size_t>(i) + 2] = colour_byte(b);
+    }
+    cache.max_iter = max_iter;
+    cache.phase = phase;
+    cache.vocal = vocal;
+    cache.pitch = pitch;
+}
+
+// Returns the device LUT for the parameters; uploads when they change.
+const std::uint8_t* aurora_lut(ThreadRuntime& rt, int max_iter, double phase, double vocal, double pitch,
+                               int& size) {
+    thread_local AuroraCache cache;
+    const bool same = cache.max_iter == max_iter && cache.phase == phase && cache.vocal == vocal
+        && cache.pitch == pitch && !cache.rgb.empty();
+    if (!same) build_aurora(cache, max_iter, phase, vocal, pitch);
+    size = static_cast<int>(cache.rgb.size() / 3);
+    if (!same || cache.device != rt.device || cache.device_lut == nullptr) {
+        std::uint8_t* lut = static_cast<std::uint8_t*>(scratch(rt, kScratchLut, cache.rgb.size()));
+        check_cuda(cudaMemcpyAsync(lut, cache.rgb.data(), cache.rgb.size(), cudaMemcpyHostToDevice, rt.stream),
+                   "upload aurora LUT");
+        check_cuda(cudaStreamSynchronize(rt.stream), "upload aurora LUT");
+        cache.device_lut = lut;
+        cache.device = rt.device;
+    }
+    return cache.device_lut;
+}
+
+bool valid_colour_controls(double a, double b, double c, double d) {
+    return std::isfinite(a) && std::isfinite(b) && std::isfinite(c) && std::isfinite(d);
+}
+
+}  // namespace
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" {
+
+int fractal_abi_version(void) { return FRACTAL_ABI_VERSION; }
+int fractal_render_options_version(void) { return FRACTAL_RENDER_OPTIONS_VERSION; }
+void fractal_render_options_default(FractalRenderOptions* options) {
+    if (options) *options = default_options();
+}
+
+int fractal_backend_capabilities(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        set_error("no CUDA device is available");
+        return 0;
+    }
+    set_error("");
+    return FRACTAL_CAPABILITY_CUDA;
+}
+
+const char* fractal_last_error(void) { return last_error.c_str(); }
+
+void fractal_set_stats_enabled(int enabled) { stats_enabled.store(enabled != 0, std::memory_order_relaxed); }
+
+int fractal_get_last_stats(uint64_t* values, int capacity) {
+    if (!values || capacity < kStatsFields) return -1;
+    std::lock_guard<std::mutex> lock(stats_mutex);
+    for (int i = 0; i < kStatsFields; ++i) values[i] = last_stats[static_cast<std::size_t>(i)];
+    return kStatsFields;
+}
+
+int fractal_get_last_stats_ex(uint64_t* values, int capacity) {
+    if (!values || capacity < kStatsSlots) return -1;
+    std::lock_guard<std::mutex> lock(stats_mutex);
+    for (int i = 0; i < kStatsSlots; ++i) values[i] = last_stats[static_cast<std::size_t>(i)];
+    return kStatsSlots;
+}
+
+void* fractal_create_reference(const char* x, const char* y, const char* zoom, int max_iter, int precision_bits,
+                               int series_order) {
+    return guarded_handle("native reference creation failed with an unknown exception", [&] {
+        return create_handle(x, y, zoom, max_iter, precision_bits, series_order, false, kFormulaMandelbrot, "0", "0",
+                             nullptr, "invalid reference configuration");
+    });
+}
+
+void* fractal_create_reference_reusable(const char* x, const char* y, const char* zoom, int max_iter,
+                                        int precision_bits, int series_order) {
+    return guarded_handle("native reusable reference creation failed with an unknown exception", [&] {
+        return create_handle(x, y, zoom, max_iter, precision_bits, series_order, true, kFormulaMandelbrot, "0", "0",
+                             nullptr, "invalid reusable reference configuration");
+    });
+}
+
+void* fractal_create_reference_reusable_options(const char* x, const char* y, const char* zoom, int max_iter,
+                                                int precision_bits, int series_order,
+                                                const FractalRenderOptions* options) {
+    return guarded_handle("native reusable reference creation failed with an unknown exception", [&] {
+        return create_handle(x, y, zoom, max_iter, precision_bits, series_order, true, kFormulaMandelbrot, "0", "0",
+                             options, "invalid reusable reference configuration");
+    });
+}
+
+void* fractal_create_reference_ex(const char* x, const char* y, const char* zoom, int max_iter, int precision_bits,
+                                  int series_order, int formula, const char* jr, const char* ji) {
+    return guarded_handle("formula-aware reference creation failed with an unknown exception", [&] {
+        return create_handle(x, y, zoom, max_iter, precision_bits, series_order, formula != kFormulaMandelbrot,
+                             formula, jr, ji, nullptr, "invalid formula-aware reference configuration");
+    });
+}
+
+void* fractal_create_reference_ex_options(const char* x, const char* y, const char* zoom, int max_iter,
+                                          int precision_bits, int series_order, int formula, const char* jr,
+                                          const char* ji, const FractalRenderOptions* options) {
+    return guarded_handle("formula-aware reference creation failed with an unknown exception", [&] {
+        return create_handle(x, y, zoom, max_iter, precision_bits, series_order, formula != kFormulaMandelbrot,
+                             formula, jr, ji, options, "invalid formula-aware reference configuration");
+    });
+}
+
+void* fractal_clone_reference(void* source_handle, const char* zoom) {
+    return guarded_handle("native reference clone failed with an unknown exception", [&] {
+        if (!source_handle || !zoom) throw Failure{"invalid reference tier clone configuration"};
+        const auto source = acquire_reference(source_handle);
+        if (!source) throw Failure{"invalid or already-destroyed reference handle"};
+        return register_reference(clone_reference_context(*source, zoom));
+    });
+}
+
+void fractal_destroy_reference(void* handle) {
+    try {
+        if (!handle) {
+            set_error("");
+            return;
+        }
+        const auto context = remove_reference(handle);
+        if (!context) {
+            set_error("invalid or already-destroyed reference handle");
+            return;
+        }
+        set_error("");
+    } catch (...) {
+        set_error("native reference destruction failed with an unknown exception");
+    }
+}
+
+int fractal_get_reference_stats(void* handle, uint64_t* values, int capacity) {
+    try {
+        if (!values || capacity < 5) {
+            set_error("reference statistics buffer is too small or null");
+            return -1;
+        }
+        const auto ctx = acquire_reference(handle);
+        if (!ctx) {
+            set_error("invalid or already-destroyed reference handle");
+            return -1;
+        }
+        values[0] = ctx->reference_build_ns;
+        values[1] = ctx->series_build_ns;
+        values[2] = ctx->bla_build_ns;
+        values[3] = ctx->series.enabled ? static_cast<uint64_t>(ctx->series.iteration) : 0;
+        values[4] = ctx->series.enabled ? static_cast<uint64_t>(ctx->series.order) : 0;
+        set_error("");
+        return 5;
+    } catch (...) {
+        set_error("reference statistics lookup failed with an unknown exception");
+        return -1;
+    }
+}
+
+int fractal_render_reference_ex_planes(float* output, int width, int height, const char* zoom_text, void* handle,
+                                       int max_iter, int threads, int series_order, int series_block,
+                                       const FractalRenderOptions* supplied, FractalRenderPlanes* planes) {
+    return guarded("native reference render failed with an unknown exception", [&] {
+        if (!output || !zoom_text || !handle || !valid_dims(width, height) || !valid_iterations(max_iter)
+            || !valid_threads(threads) || !valid_series(series_order, series_block)
+            || (planes != nullptr && !valid_planes(planes, width, height))) {
+            throw Failure{"invalid native render dimensions or handle"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        const auto ctx = acquire_reference(handle);
+        if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
+        if (ctx->escape_mode != o.escape_radius_mode) {
+            throw Failure{"reference escape-radius mode does not match render options"};
+        }
+        if (max_iter > ctx->requested_max_iter) throw Failure{"render iteration count exceeds prepared reference"};
+        render_to_host(output, planes, width, height, [&](const Outputs& out, bool collect, ThreadRuntime& rt,
+                                                          cudaStream_t stream) {
+            render_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o,
+                                  collect, rt, stream);
+        });
+    });
+}
+
+int fractal_render_reference_ex(float* output, int width, int height, const char* zoom_text, void* handle,
+                                int max_iter, int threads, int series_order, int series_block,
+                                const FractalRenderOptions* options) {
+    return fractal_render_reference_ex_planes(output, width, height, zoom_text, handle, max_iter, threads,
+                                              series_order, series_block, options, nullptr);
+}
+
+int fractal_render_mandelbrot_reference_ex(float* output, int width, int height, const char* zoom_text,
+                                           void* handle, int max_iter, int threads, int series_order,
+                                           int series_block, const FractalRenderOptions* options) {
+    return fractal_render_reference_ex(output, width, height, zoom_text, handle, max_iter, threads, series_order,
+                                       series_block, options);
+}
+
+int render_mandelbrot_reference(float* output, int width, int height, const char* zoom_text, void* handle,
+                                int max_iter, int threads, int series_order, int series_block) {
+    return fractal_render_reference_ex(output, width, height, zoom_text, handle, max_iter, threads, series_order,
+                                       series_block, nullptr);
+}
+
+int render_fractal_ex_planes(float* output, int width, int height, const char* zoom_text, const char* x_center,
+                             const char* y_center, int max_iter, int precision_bits, int use_perturbation,
+                             int threads, int formula, double julia_real, double julia_imag,
+                             const FractalRenderOptions* supplied, FractalRenderPlanes* planes) {
+    return guarded("native render failed with an unknown exception", [&] {
+        if (!output || !zoom_text || !x_center || !y_center || !valid_dims(width, height)
+            || (planes != nullptr && !valid_planes(planes, width, height)) || !valid_iterations(max_iter)
+            || !valid_precision(precision_bits) || use_perturbation < 0 || use_perturbation > 1
+            || !valid_threads(threads) || !valid_formula(formula) || !std::isfinite(julia_real)
+            || !std::isfinite(julia_imag)) {
+            throw Failure{"invalid native render dimensions, formula, or argument"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        if (!use_perturbation) {
+            const long double zoom = parse_zoom_direct(zoom_text);
+            const long double cx = parse_coordinate(x_center, "real");
+            const long double cy = parse_coordinate(y_center, "imaginary");
+            render_to_host(output, planes, width, height, [&](const Outputs& out, bool, ThreadRuntime&,
+                                                              cudaStream_t stream) {
+                launch_direct_render(out, width, height, zoom, cx, cy, max_iter, formula, julia_real, julia_imag, o,
+                                     stream);
+            });
+            return;
+        }
+        // One-shot deep render: series order 8 and block 32 as the
+        // reference's render_fractal_ex does (renderer.cpp:20340-20354).
+        const std::string jr = julia_text(julia_real);
+        const std::string ji = julia_text(julia_imag);
+        void* handle = fractal_create_reference_ex_options(x_center, y_center, zoom_text, max_iter, precision_bits,
+                                                           8, formula, jr.c_str(), ji.c_str(), &o);
+        if (!handle) throw Failure{last_error};
+        const int status = fractal_render_reference_ex_planes(output, width, height, zoom_text, handle, max_iter,
+                                                              threads, 8, 32, &o, planes);
+        const std::string render_error = last_error;
+        fractal_destroy_reference(handle);
+        if (status != 0) throw Failure{render_error};
+    });
+}
+
+int render_fractal_ex(float* output, int width, int height, const char* zoom_text, const char* x_center,
+                      const char* y_center, int max_iter, int precision_bits, int use_perturbation, int threads,
+                      int formula, double julia_real, double julia_imag, const FractalRenderOptions* options) {
+    return render_fractal_ex_planes(output, width, height, zoom_text, x_center, y_center, max_iter, precision_bits,
+                                    use_perturbation, threads, formula, julia_real, julia_imag, options, nullptr);
+}
+
+int render_mandelbrot_ex(float* output, int width, int height, const char* zoom_text, const char* x_center,
+                         const char* y_center, int max_iter, int precision_bits, int use_perturbation, int threads,
+                         const FractalRenderOptions* options) {
+    return render_fractal_ex(output, width, height, zoom_text, x_center, y_center, max_iter, precision_bits,
+                             use_perturbation, threads, kFormulaMandelbrot, 0.0, 0.0, options);
+}
+
+int render_mandelbrot(float* output, int width, int height, const char* zoom_text, const char* x_center,
+                      const char* y_center, int max_iter, int precision_bits, int use_perturbation, int threads) {
+    return render_mandelbrot_ex(output, width, height, zoom_text, x_center, y_center, max_iter, precision_bits,
+                                use_perturbation, threads, nullptr);
+}
+
+int fractal_colourise(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
+                      double vocal, double instrumental, double pitch, int threads) {
+    return guarded("native colouriser failed with an unknown exception", [&] {
+        if (!field || !output || !valid_dims(width, height) || !valid_iterations(max_iter) || !valid_threads(threads)
+            || !valid_colour_controls(phase, vocal, instrumental, pitch)) {
+            throw Failure{"invalid native colour dimensions or palette"};
+        }
+        ThreadRuntime& rt = thread_runtime();
+        const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
+        int lut_size = 0;
+        const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size);
+        float* d_field = static_cast<float*>(scratch(rt, kScratchField, pixels * sizeof(float)));
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        check_cuda(cudaMemcpyAsync(d_field, field, pixels * sizeof(float), cudaMemcpyHostToDevice, rt.stream),
+                   "copy field to device");
+        const float scale = static_cast<float>(lut_size - 1) / static_cast<float>(max_iter);
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        check_cuda(launch_aurora(d_field, d_rgb, static_cast<long long>(pixels), lut, lut_size, scale, max_iter,
+                                 rt.stream), "aurora kernel launch");
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream), "copy RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "aurora colour");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+// ------------------------------------------------------------ extensions
+int fractal_gb300_device_count(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return count;
+}
+
+double fractal_gb300_last_kernel_ms(void) {
+    try {
+        return thread_runtime().last_kernel_ms;
+    } catch (...) {
+        return 0.0;
+    }
+}
+
+int fractal_gb300_render_reference_device(float* field, uint32_t* counts, int width, int height,
+                                          const char* zoom_text, void* handle, int max_iter, int series_order,
+                                          int series_block, const FractalRenderOptions* supplied, int form,
+                                          void* stream_handle) {
+    return guarded("device render failed with an unknown exception", [&] {
+        if (!field || !zoom_text || !handle || !valid_dims(width, height) || !valid_iterations(max_iter)
+            || !valid_series(series_order, series_block) || (form != 0 && form != 1)) {
+            throw Failure{"invalid native render dimensions or handle"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        const auto ctx = acquire_reference(handle);
+        if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
+        if (ctx->escape_mode != o.escape_radius_mode) {
+            throw Failure{"reference escape-radius mode does not match render options"};
+        }
+        if (max_iter > ctx->requested_max_iter) throw Failure{"render iteration count exceeds prepared reference"};
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        Outputs out;
+        out.field = field;
+        out.counts = counts;
+        if (form == 1) {
+            render_floatexp_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block,
+                                           o, rt, stream);
+        } else {
+            render_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, false,
+                                  rt, stream);
+        }
+    });
+}
+
+int fractal_gb300_render_direct_device(float* field, uint32_t* counts, int width, int height, const char* zoom_text,
+                                       const char* x_center, const char* y_center, int max_iter, int formula,
+                                       double julia_real, double julia_imag, const FractalRenderOptions* supplied,
+                                       void* stream_handle) {
+    return guarded("device direct render failed with an unknown exception", [&] {
+        if (!field || !zoom_text || !x_center || !y_center || !valid_dims(width, height)
+            || !valid_iterations(max_iter) || !valid_formula(formula) || !std::isfinite(julia_real)
+            || !std::isfinite(julia_imag)) {
+            throw Failure{"invalid native render dimensions, formula, or argument"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        Outputs out;
+        out.field = field;
+        out.counts = counts;
+        launch_direct_render(out, width, height, parse_zoom_direct(zoom_text), parse_coordinate(x_center, "real"),
+                             parse_coordinate(y_center, "imaginary"), max_iter, formula, julia_real, julia_imag, o,
+                             stream);
+    });
+}
+
+int fractal_gb300_colourise_device(const float* field, uint8_t* rgb, int width, int height, int max_iter,
+                                   double phase, double vocal, double instrumental, double pitch,
+                                   void* stream_handle) {
+    return guarded("device colour failed with an unknown exception", [&] {
+        if (!field || !rgb || !valid_dims(width, height) || !valid_iterations(max_iter)
+            || !valid_colour_controls(phase, vocal, instrumental, pitch)) {
+            throw Failure{"invalid native colour dimensions or palette"};
+        }
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        int lut_size = 0;
+        const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size);
+        const float scale = static_cast<float>(lut_size - 1) / static_cast<float>(max_iter);
+        check_cuda(launch_aurora(field, rgb, static_cast<long long>(width) * height, lut, lut_size, scale, max_iter,
+                                 stream), "aurora kernel launch");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,256 @@
+/*
+ * fractal_gb300.h - C ABI of the GB300 deep-zoom field renderer.
+ *
+ * Part 1 is the drop-in boundary: the hot subset of the reference's
+ * renderer.h ABI version 10, byte-compatible (same struct layouts, same
+ * prototypes, same 0/1 and NULL error convention with a thread-local
+ * fractal_last_error()).  Each declaration cites the renderer.h prototype it
+ * replaces.  A caller that loads the reference's mandelbrot.so through ctypes
+ * (visualizer.py:1512-2387) can load libfractal_gb300.so instead.
+ *
+ * Part 2 adds entry points the reference has no counterpart for: renders into
+ * caller-owned device memory on a caller-chosen CUDA stream, used by
+ * benchmarks and by callers that keep fields resident in HBM.
+ *
+ * Every render in this library runs on the GPU.  There is no CPU fallback:
+ * without a usable CUDA device the calls fail with a message.
+ */
+#ifndef FRACTAL_GB300_H
+#define FRACTAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FRACTAL_ABI_VERSION 10
+#define FRACTAL_RENDER_OPTIONS_VERSION 2
+#define FRACTAL_KFP_OPTIONS_VERSION 3
+#define FRACTAL_KFP_PLANES_VERSION 1
+#define FRACTAL_RENDER_PLANES_VERSION 1
+#define FRACTAL_KFP_MAX_MULTI_COLORS 256
+
+#define FRACTAL_FORMULA_MANDELBROT 0
+#define FRACTAL_FORMULA_JULIA 1
+#define FRACTAL_FORMULA_BURNING_SHIP 2
+#define FRACTAL_FORMULA_TRICORN 3
+
+#define FRACTAL_COORDINATE_MODE_PROJECT 0
+#define FRACTAL_COORDINATE_MODE_KALLES 1
+
+#define FRACTAL_RENDER_HINT_SKIP_PHASE (1u << 0)
+#define FRACTAL_RENDER_HINT_SKIP_ANALYTIC_DE (1u << 1)
+
+/* Backend id of this library.  The reference uses 0 scalar, 1 AVX2,
+ * 2 OpenCL and capability bits 1/2/4/8; its loader tests 1 << backend
+ * (visualizer.py:1286), so the CUDA backend takes id 4 and bit 16.
+ * Backend 0 (the struct default) also selects the CUDA path here. */
+#define FRACTAL_BACKEND_CUDA 4
+#define FRACTAL_CAPABILITY_CUDA (1 << FRACTAL_BACKEND_CUDA)
+
+/* renderer.h:43-67 */
+typedef struct FractalRenderOptions {
+    uint32_t struct_size;
+    uint32_t version;
+    int32_t strict;
+    int32_t allow_recovery;
+    int32_t time_budget_ms;
+    int32_t disable_bla;
+    int32_t disable_cycle;
+    int32_t strict_cycle;
+    int32_t series_min_terms;
+    int32_t series_max_terms;
+    int32_t max_bla_length;
+    int32_t max_linear_bla_length;
+    int32_t backend;
+    int32_t escape_radius_mode;
+    int32_t coordinate_mode;
+    int32_t reserved[1];
+    double output_bias;
+} FractalRenderOptions;
+
+/* renderer.h:75-119 */
+typedef struct FractalKfpOptions {
+    uint32_t struct_size;
+    uint32_t version;
+    double iter_div;
+    double color_offset;
+    double ratio;
+    int32_t color_method;
+    int32_t smooth_method;
+    int32_t smooth;
+    int32_t flat;
+    int32_t inverse_transition;
+    double phase_color_strength;
+    int32_t multi_color;
+    int32_t blend_multi_color;
+    uint32_t multi_color_count;
+    double multi_color_period[FRACTAL_KFP_MAX_MULTI_COLORS];
+    int32_t multi_color_start[FRACTAL_KFP_MAX_MULTI_COLORS];
+    int32_t multi_color_type[FRACTAL_KFP_MAX_MULTI_COLORS];
+    double power;
+    int32_t slopes;
+    double slope_power;
+    double slope_ratio;
+    double slope_angle;
+    int32_t differences;
+    int32_t interior_color[3];
+    double field_bias;
+    int32_t bailout_radius_preset;
+    double bailout_radius_custom;
+    int32_t bailout_norm_preset;
+    double bailout_norm_custom;
+    int32_t texture_enabled;
+    double texture_merge;
+    double texture_power;
+    double texture_ratio;
+    int32_t texture_resize;
+    int32_t use_opengl;
+    int32_t use_srgb;
+    int32_t show_glitches;
+} FractalKfpOptions;
+
+/* renderer.h:155-170 */
+typedef struct FractalRenderPlanes {
+    uint32_t struct_size;
+    uint32_t version;
+    int64_t *orbit_iteration;
+    double *phase;
+    double *de_x;
+    double *de_y;
+    double *test1;
+    double *test2;
+} FractalRenderPlanes;
+
+/* ---------------------------------------------------------------------
+ * Part 1: renderer.h v10 hot subset
+ * ------------------------------------------------------------------- */
+
+int fractal_abi_version(void);                                    /* renderer.h:172 */
+int fractal_render_options_version(void);                         /* renderer.h:173 */
+void fractal_render_options_default(FractalRenderOptions *options); /* renderer.h:174 */
+/* renderer.h:175-177; returns FRACTAL_CAPABILITY_CUDA when a device is usable. */
+int fractal_backend_capabilities(void);
+const char *fractal_last_error(void);                             /* renderer.h:178 */
+
+void fractal_set_stats_enabled(int enabled);                      /* renderer.h:180 */
+int fractal_get_last_stats(uint64_t *values, int capacity);       /* renderer.h:181 */
+int fractal_get_last_stats_ex(uint64_t *values, int capacity);    /* renderer.h:182 */
+
+/* renderer.h:184-191 */
+void *fractal_create_reference(const char *x_center, const char *y_center,
+                               const char *viewport_zoom, int max_iter,
+                               int precision_bits, int series_order);
+/* renderer.h:193-200 */
+void *fractal_create_reference_reusable(const char *x_center, const char *y_center,
+                                        const char *viewport_zoom, int max_iter,
+                                        int precision_bits, int series_order);
+/* renderer.h:203-211 */
+void *fractal_create_reference_reusable_options(const char *x_center, const char *y_center,
+                                                const char *viewport_zoom, int max_iter,
+                                                int precision_bits, int series_order,
+                                                const FractalRenderOptions *options);
+/* renderer.h:215-225 */
+void *fractal_create_reference_ex(const char *x_center, const char *y_center,
+                                  const char *viewport_zoom, int max_iter, int precision_bits,
+                                  int series_order, int formula, const char *julia_real,
+                                  const char *julia_imag);
+/* renderer.h:226-237 */
+void *fractal_create_reference_ex_options(const char *x_center, const char *y_center,
+                                          const char *viewport_zoom, int max_iter,
+                                          int precision_bits, int series_order, int formula,
+                                          const char *julia_real, const char *julia_imag,
+                                          const FractalRenderOptions *options);
+void *fractal_clone_reference(void *source_handle, const char *viewport_zoom); /* renderer.h:239 */
+void fractal_destroy_reference(void *handle);                                 /* renderer.h:240 */
+int fractal_get_reference_stats(void *handle, uint64_t *values, int capacity); /* renderer.h:241 */
+
+/* renderer.h:243-254 */
+int fractal_render_mandelbrot_reference_ex(float *output, int width, int height,
+                                           const char *zoom_text, void *handle, int max_iter,
+                                           int threads, int series_order, int series_block,
+                                           const FractalRenderOptions *options);
+/* renderer.h:257-268 */
+int fractal_render_reference_ex(float *output, int width, int height, const char *zoom_text,
+                                void *handle, int max_iter, int threads, int series_order,
+                                int series_block, const FractalRenderOptions *options);
+/* renderer.h:273-285 */
+int fractal_render_reference_ex_planes(float *output, int width, int height,
+                                       const char *zoom_text, void *handle, int max_iter,
+                                       int threads, int series_order, int series_block,
+                                       const FractalRenderOptions *options,
+                                       FractalRenderPlanes *planes);
+/* renderer.h:323-335 */
+int render_mandelbrot_ex(float *output, int width, int height, const char *zoom_text,
+                         const char *x_center, const char *y_center, int max_iter,
+                         int precision_bits, int use_perturbation, int threads,
+                         const FractalRenderOptions *options);
+/* renderer.h:338-353 */
+int render_fractal_ex(float *output, int width, int height, const char *zoom_text,
+                      const char *x_center, const char *y_center, int max_iter,
+                      int precision_bits, int use_perturbation, int threads, int formula,
+                      double julia_real, double julia_imag, const FractalRenderOptions *options);
+/* renderer.h:357-373 */
+int render_fractal_ex_planes(float *output, int width, int height, const char *zoom_text,
+                             const char *x_center, const char *y_center, int max_iter,
+                             int precision_bits, int use_perturbation, int threads, int formula,
+                             double julia_real, double julia_imag,
+                             const FractalRenderOptions *options, FractalRenderPlanes *planes);
+/* renderer.h:376-386 */
+int render_mandelbrot_reference(float *output, int width, int height, const char *zoom_text,
+                                void *handle, int max_iter, int threads, int series_order,
+                                int series_block);
+/* renderer.h:387-398 */
+int render_mandelbrot(float *output, int width, int height, const char *zoom_text,
+                      const char *x_center, const char *y_center, int max_iter,
+                      int precision_bits, int use_perturbation, int threads);
+
+/* renderer.h:400-411: aurora palette. */
+int fractal_colourise(const float *field, uint8_t *output, int width, int height, int max_iter,
+                      double phase, double vocal, double instrumental, double pitch,
+                      int threads);
+
+/* ---------------------------------------------------------------------
+ * Part 2: GB300 extensions (no counterpart in the reference)
+ *
+ * Device-pointer variants: every buffer argument is device memory on the
+ * current CUDA device; `stream` is a cudaStream_t (NULL = the calling
+ * thread's library stream).  The calls enqueue work and return without
+ * synchronising; results are ready when the stream reaches them.
+ * ------------------------------------------------------------------- */
+
+/* Number of usable CUDA devices (0 when none). */
+int fractal_gb300_device_count(void);
+/* Duration in ms of the last render/colour kernel issued by this thread,
+ * measured with CUDA events on its stream (after a synchronous call). */
+double fractal_gb300_last_kernel_ms(void);
+
+/* Deep or direct render of one field from a prepared reference into device
+ * buffers: `field` float[width*height], `counts` uint32[width*height] (escape
+ * index, max_iter for interior, 0 for an unresolved glitch; may be NULL).
+ * `form` selects the arithmetic: 0 = plain FP64 form (parity with the
+ * reference), 1 = FP32-mantissa floatexp form. */
+int fractal_gb300_render_reference_device(float *field, uint32_t *counts, int width, int height,
+                                          const char *zoom_text, void *handle, int max_iter,
+                                          int series_order, int series_block,
+                                          const FractalRenderOptions *options, int form,
+                                          void *stream);
+
+/* Direct (shallow) render into device buffers; same conventions as above. */
+int fractal_gb300_render_direct_device(float *field, uint32_t *counts, int width, int height,
+                                       const char *zoom_text, const char *x_center,
+                                       const char *y_center, int max_iter, int formula,
+                                       double julia_real, double julia_imag,
+                                       const FractalRenderOptions *options, void *stream);
+
+/* Aurora colour pass from a device field to device RGB8. */
+int fractal_gb300_colourise_device(const float *field, uint8_t *rgb, int width, int height,
+                                   int max_iter, double phase, double vocal, double instrumental,
+                                   double pitch, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,279 @@
+"""Generate the seeded deep-zoom centres used by the parity tests and bench.
+
+The reference bundles hand-picked centres only; the workloads here need
+seeded Misiurewicz points instead.  A Misiurewicz point M(k, p) is a
+parameter c whose critical orbit z_0 = 0, z_{n+1} = z_n^2 + c is strictly
+preperiodic with preperiod k and period p:  z_{k+p} = z_k, while
+z_{k-1+p} != z_{k-1} and z_{k+d} != z_k for every proper divisor d of p.
+It lies on the boundary of the Mandelbrot set, so a deep view centred on it
+keeps detail at every depth.
+
+Method (seeded, deterministic):
+  1. draw k ~ U{3..20}, p ~ U{1..8} and a start c0 in the upper half-plane;
+  2. Newton on g(c) = z_{k+p}(c) - z_k(c) in double precision, with
+     dz/dc carried alongside (d z_{n+1} = 2 z_n dz_n + 1);
+  3. polish the converged root with Newton at the requested binary precision
+     (mpmath, 400 or 1200 bits) and check the exact preperiod and period;
+  4. reject and redraw on any failure.
+The centres are printed as decimal strings of the requested length.
+
+Julia constants for the mixed-formula batch are boundary points of the
+Mandelbrot set found by bisection along a seeded ray (inside = critical
+orbit bounded for the test budget), with |c| < 0.8.
+
+Run:  python tests/golden/make_centres.py   (writes tests/golden/centres.json)
+"""
+
+from __future__ import annotations
+
+import json
+import math
+import os
+import sys
+
+import mpmath
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _orbit_with_derivative(c: complex, steps: int):
+    z = 0j
+    dz = 0j
+    zs = [z]
+    dzs = [dz]
+    for _ in range(steps):
+        dz = 2.0 * z * dz + 1.0
+        z = z * z + c
+        zs.append(z)
+        dzs.append(dz)
+        if abs(z) > 1e150:
+            return None, None
+    return zs, dzs
+
+
+def _newton_double(c: complex, k: int, p: int, iterations: int = 600):
+    for _ in range(iterations):
+        zs, dzs = _orbit_with_derivative(c, k + p)
+        if zs is None:
+            return None
+        g = zs[k + p] - zs[k]
+        dg = dzs[k + p] - dzs[k]
+        if dg == 0:
+            return None
+        step = g / dg
+        c = c - step
+        if not (abs(c) < 4.0):
+            return None
+        if abs(step) < 1e-15:
+            return c
+    return None
+
+
+def _mp_orbit(c, steps):
+    z = mpmath.mpc(0)
+    dz = mpmath.mpc(0)
+    zs = [z]
+    dzs = [dz]
+    for _ in range(steps):
+        dz = 2 * z * dz + 1
+        z = z * z + c
+        zs.append(z)
+        dzs.append(dz)
+    return zs, dzs
+
+
+def misiurewicz_centre(seed: int, bits: int, digits: int):
+    rng = np.random.default_rng(seed)
+    for attempt in range(10_000):
+        k = int(rng.integers(3, 21))
+        p = int(rng.integers(1, 9))
+        c0 = complex(rng.uniform(-2.0, 0.5), rng.uniform(0.02, 1.2))
+        root = _newton_double(c0, k, p)
+        if root is None or root.imag <= 1e-6:
+            continue
+        with mpmath.workprec(bits + 64):
+            c = mpmath.mpc(root.real, root.imag)
+            for _ in range(40):
+                zs, dzs = _mp_orbit(c, k + p)
+                g = zs[k + p] - zs[k]
+                dg = dzs[k + p] - dzs[k]
+                step = g / dg
+                c = c - step
+                if abs(step) < mpmath.mpf(2) ** (-(bits + 32)):
+                    break
+            zs, _ = _mp_orbit(c, k + p)
+            tiny = mpmath.mpf(2) ** (-(bits - 16))
+            loose = mpmath.mpf(10) ** -12
+            if abs(zs[k + p] - zs[k]) > tiny:
+                continue
+            if abs(zs[k - 1 + p] - zs[k - 1]) < loose:
+                continue  # smaller preperiod
+            if any(abs(zs[k + d] - zs[k]) < loose for d in range(1, p) if p % d == 0):
+                continue  # smaller period
+            if any(abs(z) < loose for z in zs[1:]):
+                continue  # a periodic centre, not a boundary point
+            if c.imag <= 0:
+                continue
+            re = mpmath.nstr(c.real, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            im = mpmath.nstr(c.imag, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            return {
+                "seed": seed,
+                "attempt": attempt,
+                "preperiod": k,
+                "period": p,
+                "bits": bits,
+                "digits": digits,
+                "re": re,
+                "im": im,
+            }
+    raise RuntimeError("no Misiurewicz point found")
+
+
+def nucleus_centre(seed: int, period: int, bits: int, digits: int):
+    """Centre of a period-p hyperbolic component (z_p(c) = 0), found by
+    Newton from a seeded start; its minibrot fills deep views with interior
+    pixels, which exercises BLA, rebasing and long exact tails."""
+    rng = np.random.default_rng(seed)
+    for attempt in range(10_000):
+        c0 = complex(rng.uniform(-1.9, 0.4), rng.uniform(0.02, 1.1))
+        c = c0
+        ok = False
+        for _ in range(400):
+            z, dz = 0j, 0j
+            for _ in range(period):
+                dz = 2.0 * z * dz + 1.0
+                z = z * z + c
+            if dz == 0 or abs(z) > 1e100:
+                break
+            step = z / dz
+            c -= step
+            if abs(c) > 2.5:
+                break
+            if abs(step) < 1e-15:
+                ok = True
+                break
+        if not ok or c.imag <= 1e-4:
+            continue
+        with mpmath.workprec(bits + 64):
+            cm = mpmath.mpc(c.real, c.imag)
+            for _ in range(60):
+                z, dz = mpmath.mpc(0), mpmath.mpc(0)
+                for _ in range(period):
+                    dz = 2 * z * dz + 1
+                    z = z * z + cm
+                step = z / dz
+                cm = cm - step
+                if abs(step) < mpmath.mpf(2) ** (-(bits + 32)):
+                    break
+            # exact period: no earlier return to zero
+            z = mpmath.mpc(0)
+            exact = True
+            for k in range(1, period):
+                z = z * z + cm
+                if abs(z) < mpmath.mpf(10) ** -20:
+                    exact = False
+                    break
+            if not exact:
+                continue
+            z, dz = mpmath.mpc(0), mpmath.mpc(0)
+            for _ in range(period):
+                dz = 2 * z * dz + 1
+                z = z * z + cm
+            size = float(1.0 / abs(dz) ** 2) if abs(dz) > 0 else 0.0
+            re = mpmath.nstr(cm.real, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            im = mpmath.nstr(cm.imag, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            return {"seed": seed, "attempt": attempt, "period": period, "bits": bits, "digits": digits,
+                    "size_estimate": size, "re": re, "im": im}
+    raise RuntimeError("no nucleus found")
+
+
+def nucleus_near(centre: dict, period: int, offset_log10: float, bits: int, digits: int):
+    """Nucleus of a period-p minibrot on the spiral of a Misiurewicz point:
+    Newton from the point shifted by 10^offset (1 + i).  Such minibrots sit
+    at depth ~1e30 with long interior orbits, the regime where the BLA
+    hierarchy, rebasing and replay do most of the work."""
+    with mpmath.workprec(bits + 64):
+        m = mpmath.mpc(mpmath.mpf(centre["re"]), mpmath.mpf(centre["im"]))
+        cm = m + mpmath.mpf(10) ** offset_log10 * mpmath.mpc(1, 1)
+        for _ in range(200):
+            z, dz = mpmath.mpc(0), mpmath.mpc(0)
+            for _ in range(period):
+                dz = 2 * z * dz + 1
+                z = z * z + cm
+            step = z / dz
+            cm = cm - step
+            if abs(step) < mpmath.mpf(2) ** (-(bits + 16)):
+                break
+        else:
+            raise RuntimeError("nucleus Newton did not converge")
+        z, dz = mpmath.mpc(0), mpmath.mpc(0)
+        for _ in range(period):
+            dz = 2 * z * dz + 1
+            z = z * z + cm
+        re = mpmath.nstr(cm.real, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+        im = mpmath.nstr(cm.imag, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+        return {"period": period, "bits": bits, "digits": digits, "size_estimate": float(1 / abs(dz) ** 2),
+                "distance_to_misiurewicz": float(abs(cm - m)), "re": re, "im": im}
+
+
+def _bounded(c: complex, budget: int = 4000) -> bool:
+    z = 0j
+    for _ in range(budget):
+        z = z * z + c
+        if (z.real * z.real + z.imag * z.imag) > 4.0:
+            return False
+    return True
+
+
+def julia_boundary_constant(seed: int):
+    """A Mandelbrot-boundary parameter with |c| < 0.8 along a seeded ray."""
+    rng = np.random.default_rng(seed)
+    for _ in range(1000):
+        angle = rng.uniform(0.0, 2.0 * math.pi)
+        direction = complex(math.cos(angle), math.sin(angle))
+        inner, outer = 0.0, 0.8
+        if not _bounded(inner * direction) or _bounded(outer * direction):
+            continue
+        for _ in range(48):
+            mid = 0.5 * (inner + outer)
+            if _bounded(mid * direction):
+                inner = mid
+            else:
+                outer = mid
+        c = inner * direction
+        return {"seed": seed, "angle": angle, "re": repr(c.real), "im": repr(c.imag)}
+    raise RuntimeError("no Julia boundary constant found")
+
+
+def main() -> int:
+    centres = {
+        # 640x360 at 1e30: 400-bit Newton, 120-digit strings.
+        "field_640x360_e30": misiurewicz_centre(seed=20240, bits=400, digits=120),
+        # FHD keyframe stack to 1e50: 1200-bit Newton, 360-digit strings.
+        "fhd_stack_e50": misiurewicz_centre(seed=20241, bits=1200, digits=360),
+        # 1e100 fields: 1200-bit Newton.
+        "field_e100": misiurewicz_centre(seed=20242, bits=1200, digits=360),
+        "julia_c": [julia_boundary_constant(seed=7000 + i) for i in range(4)],
+        # Minibrot nuclei for BLA-heavy parity views.
+        "nucleus_p34": nucleus_centre(seed=9100, period=34, bits=600, digits=180),
+        "nucleus_p61": nucleus_centre(seed=9101, period=61, bits=600, digits=180),
+    }
+    centres.update({
+        # Deep minibrots on the e100 point's spiral (BLA-heavy views).
+        "deep_nucleus_p70": nucleus_near(centres["field_e100"], 70, -18.0, bits=700, digits=210),
+        "deep_nucleus_p80": nucleus_near(centres["field_e100"], 80, -18.0, bits=700, digits=210),
+    })
+    path = os.path.join(HERE, "centres.json")
+    with open(path, "w", encoding="ascii") as handle:
+        json.dump(centres, handle, indent=1)
+        handle.write("\n")
+    for key, value in centres.items():
+        if isinstance(value, dict):
+            print(key, value.get("preperiod"), value["period"], value.get("size_estimate"),
+                  value["re"][:24], value["im"][:24])
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
