@@ -1,0 +1,414 @@
+"""Benchmark: Gpixel-iter/s of the FHD atlas keyframe stack on one GB300.
+
+Workload (one step): the 55 atlas keyframes of a 1920x1080 field with
+keyframe factor 8 from zoom 1e0 to ~1e48.8 (levels i = 0..54, log10 zoom
+i*log10(8)), iteration cap 2000 + 3000 per decade up to 200k, centred on a
+seeded Misiurewicz point (tests/golden/centres.json "fhd_stack_e50", 1200-bit
+Newton, 360 digits).  Levels below 1e12 take the direct path, deeper ones
+render from the shared MPFR reference and its BLA tiers, as the reference
+pipeline does.  Work unit: a pixel-iteration, i.e. the sum of uint32
+iteration counts (escape index, or the cap for interior pixels); iterations
+skipped by the image series or BLA count as done (the reference's
+logical_iterations + series_jumps).
+
+Arms
+  ours (default)      the GB300 library; `value` is device throughput with
+                      the tables resident in HBM, `e2e` goes through the
+                      renderer.h ABI into host memory (field copied back).
+  --impl reference    the reference's CPU implementation of the path on the
+                      host cores: the reference build in oracle/_ref when it
+                      exists, else the oracle port (a restatement pinned
+                      bit-exact to it), on a bounded sample of the workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+import __graft_entry__  # noqa: E402
+
+WIDTH, HEIGHT = 1920, 1080
+FACTOR = 8.0
+LEVELS = 55
+SAMPLE_DIVISOR = 4  # CPU sample: every keyframe at 480x270 (1/16 of the pixels)
+METRIC = "Gpixel-iter/s on 1e100 FHD atlas, chosen vs plain GPU at ≤1e-4 pixel mismatch"
+
+
+def workload_levels():
+    step = math.log10(FACTOR)
+    levels = []
+    for i in range(LEVELS):
+        cap = min(200_000, max(64, int(2000 + 3000 * max(0.0, min(50.0, (i + 1) * step)))))
+        levels.append((i, i * step, cap))
+    return levels, step
+
+
+def centre():
+    with open(os.path.join(ROOT, "tests", "golden", "centres.json"), encoding="ascii") as handle:
+        data = json.load(handle)["fhd_stack_e50"]
+    return data["re"], data["im"]
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                self.rows.append([v.strip() for v in line.split(",")])
+
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.thread.join(timeout=5)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for name, value in zip(names, r[5:9]):
+                if value.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_flops(stats: dict, series_order: int) -> float:
+    """Flops per unit of work (SURVEY d): exact step 22, linear BLA 14,
+    cubic BLA 60, image series 8 per term per pixel."""
+    return (22.0 * stats["exact_steps"] + 14.0 * stats["linear_blocks"] + 60.0 * stats["cubic_blocks"]
+            + 8.0 * series_order * stats["series_pixels"])
+
+
+def run_reference_arm(args) -> int:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    package = __graft_entry__._package()
+    native = package.native
+    atlas = package.atlas
+    ref_path = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
+    kind = "reference"
+    if not os.path.exists(ref_path):
+        ref_path = os.path.join(ROOT, "oracle", "_ref", "liboracle.so")
+        kind = "port"
+        if not os.path.exists(ref_path):
+            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "port"], check=True,
+                           capture_output=True)
+    library = native.load(ref_path)
+    cores = os.cpu_count() or 1
+    levels, step = workload_levels()
+    x, y = centre()
+    w, h = WIDTH // SAMPLE_DIVISOR, HEIGHT // SAMPLE_DIVISOR
+    t0 = time.perf_counter()
+    stack = atlas.KeyframeStack(library, x, y, levels, step=step)
+    setup_s = time.perf_counter() - t0
+
+    def one_step():
+        total = 0
+        for keyframe in stack.keyframes:
+            field, planes = stack.render_host(keyframe, w, h, threads=cores, planes=True)
+            total += int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
+                         .astype(np.uint64).sum())
+        return total
+
+    for _ in range(args.warmup):
+        one_step()
+    t0 = time.perf_counter()
+    work = 0
+    for _ in range(args.steps):
+        work += one_step()
+    elapsed = time.perf_counter() - t0
+    stack.close()
+    value = work / elapsed / 1e9
+    sample = (f"all {LEVELS} keyframes of the FHD stack at {w}x{h} (1/{SAMPLE_DIVISOR**2} of the pixels), "
+              f"same views and caps")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "Gpixel-iter/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Misiurewicz centre)",
+        "config": {"workload": "fhd_keyframe_stack", "keyframes": LEVELS, "width": w, "height": h,
+                   "keyframe_factor": FACTOR, "max_log10_zoom": levels[-1][1], "threads": cores,
+                   "library": os.path.relpath(ref_path, ROOT), "reference_setup_s": setup_s},
+        "cpu_baseline": {"value": value, "unit": "Gpixel-iter/s", "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def cpu_baseline_sample(native, atlas, levels, step, x, y) -> dict:
+    """Time the CPU implementation on a bounded sample (rank 0, N=1 only)."""
+    ref_path = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
+    kind = "reference"
+    if not os.path.exists(ref_path):
+        ref_path = os.path.join(ROOT, "oracle", "_ref", "liboracle.so")
+        kind = "port"
+        if not os.path.exists(ref_path):
+            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "port"], check=True,
+                           capture_output=True)
+    library = native.load(ref_path)
+    cores = os.cpu_count() or 1
+    w, h = WIDTH // SAMPLE_DIVISOR, HEIGHT // SAMPLE_DIVISOR
+    stack = atlas.KeyframeStack(library, x, y, levels, step=step)
+    try:
+        work = 0
+        t0 = time.perf_counter()
+        for keyframe in stack.keyframes:
+            field, planes = stack.render_host(keyframe, w, h, threads=cores, planes=True)
+            work += int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
+                        .astype(np.uint64).sum())
+        elapsed = time.perf_counter() - t0
+    finally:
+        stack.close()
+    return {"value": work / elapsed / 1e9, "unit": "Gpixel-iter/s", "cores": cores, "kind": kind,
+            "sample": f"all {LEVELS} keyframes at {w}x{h} (1/{SAMPLE_DIVISOR**2} of the pixels), {elapsed:.1f} s"}
+
+
+def run_gpu_arm(args) -> int:
+    import torch
+
+    rank, world, local_rank = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    package = __graft_entry__._package()
+    native = package.native
+    atlas = package.atlas
+    library = package.load_library()
+    levels, step = workload_levels()
+    x, y = centre()
+    t0 = time.perf_counter()
+    stack = atlas.KeyframeStack(library, x, y, levels, step=step)
+    setup_s = time.perf_counter() - t0
+    n_levels = len(stack.keyframes)
+    pixels = WIDTH * HEIGHT
+    fields = torch.empty((n_levels, pixels), dtype=torch.float32, device="cuda")
+    counts = torch.empty((n_levels, pixels), dtype=torch.int32, device="cuda")
+    # A dedicated stream: the library enqueues on the handle it is given, and
+    # the timing events are recorded on the same stream.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    handle = stream.cuda_stream
+    assert handle != 0
+    forms = {"plain": 0, "chosen": 1 if args.form == "chosen" else 0}
+
+    def step_device(form):
+        for i, keyframe in enumerate(stack.keyframes):
+            stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), WIDTH, HEIGHT, form=form,
+                                stream=handle)
+
+    def timed(form, steps, warmup):
+        for _ in range(warmup):
+            step_device(form)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(steps):
+            step_device(form)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        ms = start.elapsed_time(stop)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # Work per step (sum of counts) for the chosen form, verified against the
+    # plain form (the parity form) on the same views.
+    step_device(forms["chosen"])
+    torch.cuda.synchronize()
+    chosen_counts = counts.clone()
+    work = int(counts.to(torch.int64).sum().item())
+    step_device(0)
+    torch.cuda.synchronize()
+    plain_work = int(counts.to(torch.int64).sum().item())
+    mismatch = int((counts != chosen_counts).sum().item())
+    del chosen_counts
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    ms = timed(forms["chosen"], args.steps, args.warmup)
+    clocks = sampler.stop()
+    ms_per_step = ms / args.steps
+    value = world * work * args.steps / (ms * 1e-3) / 1e9
+
+    plain_ms = timed(0, max(1, args.steps // 2), 1) if forms["chosen"] != 0 else ms
+    plain_value = plain_work * max(1, args.steps // 2) / (plain_ms * 1e-3) / 1e9 if forms["chosen"] != 0 else value
+
+    # Per-launch durations of the dominant (deep render) kernel on the
+    # launching stream, and its algorithmic flops from the device counters.
+    deep = [k for k in stack.keyframes if k.reference is not None]
+    events = []
+    for keyframe in deep:
+        i = stack.keyframes.index(keyframe)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), WIDTH, HEIGHT,
+                            form=forms["chosen"], stream=handle)
+        b.record(stream)
+        events.append((a, b))
+    torch.cuda.synchronize()
+    deep_ms = sum(a.elapsed_time(b) for a, b in events)
+    flops = 0.0
+    library.fractal_set_stats_enabled(1)
+    for keyframe in deep:
+        stack.render_host(keyframe, WIDTH, HEIGHT)
+        flops += algorithmic_flops(native.stats(library), 32)
+    library.fractal_set_stats_enabled(0)
+    precision = 32 if forms["chosen"] == 1 else 64
+    peak = ctypes.c_double(0.0)
+    library.fractal_gb300_fma_peak(precision, ctypes.byref(peak))
+    achieved = flops / (deep_ms * 1e-3) / 1e12
+    roofline = {
+        "bound": f"fp{precision}-fma",
+        "achieved": achieved,
+        "peak": peak.value,
+        "unit": "TFLOP/s",
+        "frac": achieved / peak.value if peak.value else None,
+        "traffic": None,
+        "peak_source": f"FP{precision} FMA chains measured on this GPU by fractal_gb300_fma_peak "
+                       "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
+        "kernel": "deep render (floatexp)" if precision == 32 else "deep render (plain FP64)",
+        "launches": len(deep),
+        "avg_launch_ms": deep_ms / max(1, len(deep)),
+    }
+
+    # End to end through the renderer.h ABI: host output buffers, the field
+    # copied back every keyframe.
+    e2e_steps = max(1, args.steps // 2)
+    for keyframe in stack.keyframes[:2]:
+        stack.render_host(keyframe, WIDTH, HEIGHT)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for keyframe in stack.keyframes:
+            stack.render_host(keyframe, WIDTH, HEIGHT)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * plain_work * e2e_steps / e2e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(native, atlas, levels, step, x, y)
+    stack.close()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "Gpixel-iter/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32-floatexp" if forms["chosen"] == 1 else "f64",
+            "data": "synthetic (seeded Misiurewicz centre, tests/golden/centres.json)",
+            "config": {
+                "workload": "fhd_keyframe_stack",
+                "keyframes": n_levels,
+                "width": WIDTH,
+                "height": HEIGHT,
+                "keyframe_factor": FACTOR,
+                "max_log10_zoom": levels[-1][1],
+                "max_cap": max(c for _, _, c in levels),
+                "form": args.form,
+                "pixel_iterations_per_step": work,
+                "count_mismatch_vs_plain": mismatch / (n_levels * pixels),
+                "plain_value": plain_value,
+                "reference_setup_s": setup_s,
+                "l2": "outputs larger than L2 (455 MB field + 455 MB counts per step)",
+            },
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": n_levels * pixels * 4,
+                    "path": "fractal_render_reference_ex / render_fractal_ex into host memory"},
+            "gpu_launches": args.steps * n_levels,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    parser = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=4)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    parser.add_argument("--form", choices=["chosen", "plain"], default="chosen")
+    parser.add_argument("--no-cpu-baseline", action="store_true")
+    args = parser.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

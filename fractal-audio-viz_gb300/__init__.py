@@ -27,6 +27,8 @@ def _load(name: str):
 
 
 native = _load("native")
+atlas = _load("atlas")
+kfp = _load("kfp")
 _builder = _load("build")
 LIBRARY_PATH = _builder.LIBRARY
 

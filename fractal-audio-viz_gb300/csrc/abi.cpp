@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <functional>
 #include <mutex>
@@ -392,6 +393,66 @@ void render_from_reference(ReferenceContext& ctx, const Outputs& out, int width,
                          ctx.julia_re, ctx.julia_im, o, stream);
 }
 
+}  // namespace
+
+// Floatexp form of a reference render.  It covers strict deep Mandelbrot
+// fields (the production atlas path); shallow fields, the other formulas,
+// non-strict cycle detection and time budgets use the plain form.
+void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, int width, int height,
+                                    const char* zoom_text, int max_iter, int series_order, int series_block,
+                                    const FractalRenderOptions& o, ThreadRuntime& rt, cudaStream_t stream) {
+    const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx.precision_bits);
+    const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
+    if (fe_log10(zoom) < 6.0L || ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) {
+        render_from_reference(ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, false, rt,
+                              stream);
+        return;
+    }
+    std::shared_ptr<DeviceTables> dev = device_tables(ctx);
+    floatexp_tables(ctx, *dev);
+    const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+    const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
+    const bool use_deep = fx::fe_cmp(g.current_input_radius, ctx.deep_input_radius) <= 0;
+    const bool use_ultra = fx::fe_cmp(g.current_input_radius, fx::fe_mul(ctx.input_radius, 1.0e-40)) <= 0;
+    FxParams p{};
+    p.orbit = dev->fx_orbit;
+    p.orbit_size = dev->orbit_size;
+    p.cubic = dev->fx_cubic;
+    p.cubic_index = dev->cubic_index;
+    p.linear = use_deep ? dev->fx_deep_linear : dev->fx_linear;
+    p.linear_index = use_deep ? dev->deep_linear_index : dev->linear_index;
+    p.series = dev->fx_series;
+    p.series_terms = dev->series_terms;
+    p.series_iteration = ctx.series.iteration;
+    p.series_on = ctx.series.enabled && ctx.series.order >= o.series_min_terms
+        && ctx.series.order <= o.series_max_terms
+        && fx::fe_cmp(g.current_input_radius, fx::fe_sqrt(ctx.series.r2)) <= 0
+        && ctx.series.iteration < max_iter && dev->series_terms > 1;
+    p.series_r2 = f32x::n_norm(static_cast<float>(ctx.series.r2.m), ctx.series.r2.e);
+    p.view_width = f32x::norm(static_cast<float>(g.view_width.m), 0.0f, g.view_width.e);
+    p.view_height = f32x::norm(static_cast<float>(g.view_height.m), 0.0f, g.view_height.e);
+    p.coordinate_mode = o.coordinate_mode;
+    p.width = width;
+    p.height = height;
+    p.max_iter = max_iter;
+    p.map_end = ctx.map_end;
+    p.disable_bla = (!covers || o.disable_bla != 0) ? 1 : 0;
+    p.strict = o.strict;
+    p.allow_recovery = o.allow_recovery;
+    p.escape_mode = o.escape_radius_mode;
+    p.max_bla_len = std::clamp(std::min(series_block, static_cast<int>(o.max_bla_length)), 2, kMaxSafeBlaLength);
+    p.max_lin_len = std::clamp(std::min(series_block, static_cast<int>(o.max_linear_bla_length)), 2,
+                               use_ultra ? kMaxSafeLinearBlaLength
+                                         : (use_deep ? kMaxSafeDeepLinearBlaLength : kMaxSafeBlaLength));
+    p.approx_order = std::clamp(series_order, 1, 3);
+    p.output_bias = static_cast<float>(o.output_bias);
+    p.out = out.field;
+    p.counts = out.counts;
+    check_cuda(launch_floatexp_mandelbrot(p, stream), "floatexp kernel launch");
+}
+
+namespace {
+
 // Host-buffer wrapper: device scratch, kernel, copies back, stats.
 void render_to_host(float* output, FractalRenderPlanes* planes, int width, int height,
                     const std::function<void(const Outputs&, bool, ThreadRuntime&, cudaStream_t)>& launch) {
@@ -587,6 +648,185 @@ const std::uint8_t* aurora_lut(ThreadRuntime& rt, int max_iter, double phase, do
 
 bool valid_colour_controls(double a, double b, double c, double d) {
     return std::isfinite(a) && std::isfinite(b) && std::isfinite(c) && std::isfinite(d);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ KFP
+namespace {
+
+// valid_kfp_options (renderer.cpp:7396-7454).
+bool valid_kfp(const FractalKfpOptions* o, int lut_size) {
+    const std::uint32_t legacy = static_cast<std::uint32_t>(offsetof(FractalKfpOptions, show_glitches));
+    if (!o || o->struct_size < legacy || o->version != FRACTAL_KFP_OPTIONS_VERSION || lut_size < 2 || lut_size > 65536
+        || !std::isfinite(o->iter_div) || o->iter_div <= 0.0 || !std::isfinite(o->color_offset)
+        || !std::isfinite(o->ratio) || o->color_method < 0 || o->color_method > 11 || o->smooth_method < 0
+        || o->smooth_method > 2 || o->smooth < 0 || o->smooth > 1 || o->flat < 0 || o->flat > 1
+        || o->inverse_transition < 0 || o->inverse_transition > 1 || !std::isfinite(o->phase_color_strength)
+        || o->multi_color < 0 || o->multi_color > 1 || o->blend_multi_color < 0 || o->blend_multi_color > 1
+        || o->multi_color_count > FRACTAL_KFP_MAX_MULTI_COLORS || !std::isfinite(o->power) || o->power <= 0.0
+        || o->slopes < 0 || o->slopes > 1 || !std::isfinite(o->slope_power) || o->slope_power < 0.0
+        || !std::isfinite(o->slope_ratio) || o->slope_ratio < 0.0 || !std::isfinite(o->slope_angle)
+        || o->differences < 0 || o->differences > 7 || !std::isfinite(o->field_bias) || o->field_bias < 0.0
+        || o->bailout_radius_preset < 0 || o->bailout_radius_preset > 3 || !std::isfinite(o->bailout_radius_custom)
+        || o->bailout_radius_custom <= 0.0 || o->bailout_norm_preset < 0 || o->bailout_norm_preset > 3
+        || !std::isfinite(o->bailout_norm_custom) || o->bailout_norm_custom <= 0.0 || o->texture_enabled < 0
+        || o->texture_enabled > 1 || !std::isfinite(o->texture_merge) || !std::isfinite(o->texture_power)
+        || !std::isfinite(o->texture_ratio) || o->texture_resize < 0 || o->texture_resize > 1 || o->use_opengl < 0
+        || o->use_opengl > 1 || o->use_srgb < 0 || o->use_srgb > 1) {
+        return false;
+    }
+    if (o->struct_size >= legacy + sizeof(o->show_glitches) && (o->show_glitches < 0 || o->show_glitches > 1)) {
+        return false;
+    }
+    for (std::uint32_t i = 0; i < o->multi_color_count; ++i) {
+        if (!std::isfinite(o->multi_color_period[i]) || o->multi_color_period[i] == 0.0
+            || o->multi_color_type[i] < 0 || o->multi_color_type[i] > 2) {
+            return false;
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (o->interior_color[c] < 0 || o->interior_color[c] > 255) return false;
+    }
+    return true;
+}
+
+// kfp_smooth_offset (renderer.cpp:5398-5421).
+double kfp_smooth_offset(const FractalKfpOptions& o) {
+    if (o.smooth_method != 0 || !std::isfinite(o.power) || o.power <= 0.0 || std::abs(o.power - 1.0) < 1.0e-12) {
+        return 0.0;
+    }
+    double radius = 10000.0;
+    switch (o.bailout_radius_preset) {
+        case 0: radius = 10000.0; break;
+        case 1: radius = 2.0; break;
+        case 2: radius = std::pow(2.0, 1.0 / (o.power - 1.0)); break;
+        case 3: radius = o.bailout_radius_custom; break;
+        default: return 0.0;
+    }
+    if (!std::isfinite(radius) || radius <= 1.0) return 0.0;
+    return std::log(std::log(radius)) / std::log(o.power);
+}
+
+struct KfpDeviceInputs {
+    const std::uint8_t* lut = nullptr;
+    const double* period = nullptr;
+    const int* type = nullptr;
+};
+
+// Uploads the LUT and multi-colour waves into the thread's scratch.
+KfpDeviceInputs kfp_inputs(ThreadRuntime& rt, const FractalKfpOptions& o, const std::uint8_t* lut, int lut_size,
+                           bool lut_on_device) {
+    KfpDeviceInputs in;
+    // Layout: [LUT padded to 16 B][256 wave periods][256 wave types].
+    const std::size_t lut_bytes = static_cast<std::size_t>(lut_size) * 3;
+    const std::size_t lut_padded = (lut_bytes + 15) / 16 * 16;
+    const std::size_t waves = o.multi_color_count;
+    char* base = static_cast<char*>(scratch(rt, kScratchKfpAux,
+                                            lut_padded + FRACTAL_KFP_MAX_MULTI_COLORS * (sizeof(double) + sizeof(int))));
+    std::uint8_t* lut_copy = reinterpret_cast<std::uint8_t*>(base);
+    double* period = reinterpret_cast<double*>(base + lut_padded);
+    int* type = reinterpret_cast<int*>(base + lut_padded + FRACTAL_KFP_MAX_MULTI_COLORS * sizeof(double));
+    if (waves > 0) {
+        check_cuda(cudaMemcpyAsync(period, o.multi_color_period, waves * sizeof(double), cudaMemcpyHostToDevice,
+                                   rt.stream), "upload KFP waves");
+        check_cuda(cudaMemcpyAsync(type, o.multi_color_type, waves * sizeof(int), cudaMemcpyHostToDevice, rt.stream),
+                   "upload KFP waves");
+    }
+    if (lut_on_device) {
+        in.lut = lut;
+    } else {
+        check_cuda(cudaMemcpyAsync(lut_copy, lut, lut_bytes, cudaMemcpyHostToDevice, rt.stream), "upload KFP LUT");
+        in.lut = lut_copy;
+    }
+    in.period = period;
+    in.type = type;
+    return in;
+}
+
+// Resolves the per-pass constants and launches (write_kfp_pixel inputs).
+void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height, int max_iter,
+                const FractalKfpOptions& o, const KfpDeviceInputs& in, int lut_size, ThreadRuntime& rt,
+                cudaStream_t stream) {
+    KfpLaunch k{};
+    k.width = width;
+    k.height = height;
+    k.max_iter = max_iter;
+    k.field_bias = o.field_bias;
+    k.smooth_offset = kfp_smooth_offset(o);
+    k.color_method = o.color_method;
+    k.differences = o.differences;
+    k.smooth = o.smooth;
+    k.flat = o.flat;
+    k.inverse_transition = o.inverse_transition;
+    k.needs_difference = o.color_method >= 5 && o.color_method <= 8;
+    k.needs_slopes = o.slopes && o.slope_power > 0.0 && o.slope_ratio > 0.0;
+    k.iter_div = o.iter_div;
+    k.color_offset = o.color_offset;
+    k.transfer_min = 0.0;
+    k.transfer_max = 1.0;
+    k.multi_color = o.multi_color;
+    k.blend_multi_color = o.blend_multi_color;
+    k.multi_count = static_cast<int>(o.multi_color_count);
+    if (o.slopes) {
+        const double angle = o.slope_angle * 3.14159265358979323846 / 180.0;
+        k.slope_cos = std::cos(angle);
+        k.slope_sin = std::sin(angle);
+    } else {
+        k.slope_cos = 1.0;
+        k.slope_sin = 0.0;
+    }
+    k.slope_power = o.slope_power;
+    k.slope_ratio = o.slope_ratio;
+    for (int c = 0; c < 3; ++c) k.interior[c] = o.interior_color[c];
+    k.lut_size = lut_size;
+    if (o.color_method == 4) {
+        unsigned long long* bounds = static_cast<unsigned long long*>(scratch(rt, kScratchWork, 16));
+        check_cuda(launch_kfp_bounds(d_field, static_cast<long long>(width) * height, max_iter, o.field_bias,
+                                     k.smooth_offset, bounds, stream), "KFP bounds launch");
+        unsigned long long host[2];
+        check_cuda(cudaMemcpyAsync(host, bounds, sizeof host, cudaMemcpyDeviceToHost, stream), "KFP bounds");
+        check_cuda(cudaStreamSynchronize(stream), "KFP bounds");
+        auto unorder = [](unsigned long long v) {
+            const unsigned long long bits = (v & 0x8000000000000000ull) ? (v & 0x7fffffffffffffffull) : ~v;
+            double d;
+            std::memcpy(&d, &bits, sizeof d);
+            return d;
+        };
+        if (host[0] != ~0ull && host[1] != 0ull) {
+            k.transfer_min = unorder(host[0]);
+            k.transfer_max = unorder(host[1]);
+        }
+    }
+    check_cuda(launch_kfp(d_field, d_rgb, k, in.lut, in.period, in.type, stream), "KFP kernel launch");
+}
+
+int kfp_host(const float* field, uint8_t* output, int width, int height, int max_iter, double phase, double vocal,
+             double instrumental, double pitch, const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+             int threads) {
+    return guarded("native KFP colouriser failed with an unknown exception", [&] {
+        if (!field || !output || !valid_dims(width, height) || !valid_iterations(max_iter) || !valid_threads(threads)
+            || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut || !valid_kfp(options, lut_size)) {
+            throw Failure{"invalid native KFP colour dimensions or controls"};
+        }
+        if (options->field_bias > static_cast<double>(max_iter)) {
+            throw Failure{"native KFP field bias exceeds iteration cap"};
+        }
+        ThreadRuntime& rt = thread_runtime();
+        const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
+        float* d_field = static_cast<float*>(scratch(rt, kScratchField, pixels * sizeof(float)));
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, false);
+        check_cuda(cudaMemcpyAsync(d_field, field, pixels * sizeof(float), cudaMemcpyHostToDevice, rt.stream),
+                   "copy field to device");
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        kfp_colour(d_field, d_rgb, width, height, max_iter, *options, in, lut_size, rt, rt.stream);
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream), "copy RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP colour");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
 }
 
 }  // namespace
@@ -856,7 +1096,40 @@ int fractal_colourise(const float* field, uint8_t* output, int width, int height
     });
 }
 
+int fractal_colourise_kfp(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
+                          double vocal, double instrumental, double pitch, const FractalKfpOptions* options,
+                          const uint8_t* lut, int lut_size, int threads) {
+    return kfp_host(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, options, lut, lut_size,
+                    threads);
+}
+
+int fractal_colourise_kfp_precise(const float* field, uint8_t* output, int width, int height, int max_iter,
+                                  double phase, double vocal, double instrumental, double pitch,
+                                  const FractalKfpOptions* options, const uint8_t* lut, int lut_size, int threads) {
+    return kfp_host(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, options, lut, lut_size,
+                    threads);
+}
+
 // ------------------------------------------------------------ extensions
+int fractal_gb300_colourise_kfp_device(const float* field, uint8_t* rgb, int width, int height, int max_iter,
+                                       const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                       void* stream_handle) {
+    return guarded("device KFP colour failed with an unknown exception", [&] {
+        if (!field || !rgb || !lut || !valid_dims(width, height) || !valid_iterations(max_iter)
+            || !valid_kfp(options, lut_size)) {
+            throw Failure{"invalid native KFP colour dimensions or controls"};
+        }
+        if (options->field_bias > static_cast<double>(max_iter)) {
+            throw Failure{"native KFP field bias exceeds iteration cap"};
+        }
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true);
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
+        kfp_colour(field, rgb, width, height, max_iter, *options, in, lut_size, rt, stream);
+    });
+}
+
 int fractal_gb300_device_count(void) {
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess) {

@@ -1,0 +1,407 @@
+// Kalles .kfp colour transfer on the scalar field, one thread per pixel.
+//
+// Restates fractal_colourise_kfp_impl / write_kfp_pixel for the scalar-field
+// ABI (renderer.cpp:16314-16545, 6696-7289): reflected stencil samples
+// (:5427-5496), the Differences 0-7 gradient (:5498-5578), the ColorMethod
+// 0-11 transfer with IterDiv and ColorOffset, the cyclic LUT with linear
+// interpolation, MultiColor HSV waves (:5580-5630), slopes (3D relief) and
+// Kalles' ordered dither (:5246-5258, 5314-5332).
+//
+// The kernel is HBM-bound by design (4 B of field in, 3 B of RGB out per
+// pixel; the stencil re-reads hit L1).  Precision: stencil differences are
+// formed in FP32, which is exact for neighbouring values within a factor of
+// two (Sterbenz); the transcendentals (log, sqrt, pow, atan, sin) run in
+// FP32; the palette position (division by IterDiv, offset, modulo, floor) is
+// formed in FP64 so the LUT index follows the reference.  Output agrees with
+// the reference to +-1 LSB per channel.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device.h"
+
+namespace fgb {
+
+namespace {
+
+constexpr float kPiF = 3.14159265358979323846f;
+
+struct KfpDevice {
+    int width, height, max_iter;
+    float field_bias;
+    double field_bias_d;
+    float smooth_offset;
+    double smooth_offset_d;
+    int color_method, differences, smooth, flat, inverse_transition;
+    int needs_difference, needs_slopes;
+    double iter_div, color_offset;
+    double transfer_min, transfer_max;
+    int multi_color, blend_multi_color, multi_count;
+    float slope_cos, slope_sin, slope_power, slope_ratio;
+    int interior[3];
+    int lut_size;
+};
+
+// A stencil sample is kept as its raw field value sv with the sample equal to
+// sv + field_bias + smooth_offset (kfp_colour_sample, renderer.cpp:5427-5458).
+// The bias and offset are common to every sample, so stencil differences are
+// differences of raw float field values, which FP32 forms exactly for
+// neighbouring values; only the special cases (interior, glitch, clamps) are
+// shifted into the same frame.
+__device__ __forceinline__ float sample(const float* __restrict__ field, const KfpDevice& k, int x, int y) {
+    const float v = __ldg(field + static_cast<long long>(y) * k.width + x);
+    const double shift = k.field_bias_d + k.smooth_offset_d;
+    if (!isfinite(v)) return static_cast<float>(fmax(0.0, k.smooth_offset_d) - shift);
+    const double biased = static_cast<double>(v) + k.field_bias_d;
+    if (static_cast<double>(v) >= static_cast<double>(k.max_iter) - k.field_bias_d) {
+        return static_cast<float>(static_cast<double>(k.max_iter) + 1.0 - shift);
+    }
+    if (biased < 0.0 || biased + k.smooth_offset_d < 0.0) {
+        const double s = fmax(0.0, fmin(fmax(biased, 0.0), static_cast<double>(k.max_iter)) + k.smooth_offset_d);
+        return static_cast<float>(s - shift);
+    }
+    return v;
+}
+
+// kfp_reflected_sample: out-of-frame neighbours mirror through the centre.
+__device__ __forceinline__ float reflected(const float* __restrict__ field, const KfpDevice& k, int x, int y,
+                                           int dx, int dy, float centre) {
+    const int sx = x + dx, sy = y + dy;
+    if (sx >= 0 && sx < k.width && sy >= 0 && sy < k.height) return sample(field, k, sx, sy);
+    const int ox = x - dx, oy = y - dy;
+    if (ox >= 0 && ox < k.width && oy >= 0 && oy < k.height) return 2.0f * centre - sample(field, k, ox, oy);
+    return centre;
+}
+
+// kfp_difference_magnitude (renderer.cpp:5498-5578) written on differences
+// from the centre so every term is an exact FP32 difference.
+__device__ float difference_magnitude(int differences, float c, float l, float r, float u, float d, float tl,
+                                      float tr, float bl, float br) {
+    const float s = 2.8284271247461903f;
+    const float dl = l - c, dr = r - c, du = u - c, dd = d - c;
+    const float dtl = tl - c, dtr = tr - c, dbl = bl - c, dbr = br - c;
+    switch (differences) {
+        case 0:
+            return fabsf(dl) * 1.414f + fabsf(du) * 1.414f + fabsf(dtl) + fabsf(dbl);
+        case 1: {
+            const float q = dl * dl + dr * dr + du * du + dd * dd + (dtl * dtl + dbr * dbr) * 0.5f
+                + (dbl * dbl + dtr * dtr) * 0.5f;
+            return sqrtf(fmaxf(0.0f, q * 0.25f)) * s;
+        }
+        case 2: {
+            const float a = r - l, b = d - u, e = br - tl, f = tr - bl;
+            const float q = a * a * 0.25f + b * b * 0.25f + e * e * 0.125f + f * f * 0.125f;
+            return sqrtf(fmaxf(0.0f, q * 0.5f)) * s;
+        }
+        case 3: {
+            const float a = l - u;
+            const float q = dtl * dtl * 0.5f + a * a * 0.5f;
+            return sqrtf(fmaxf(0.0f, q)) * s;
+        }
+        case 4: {
+            const float dx = ((u - tl) + (c - l)) * 0.5f;
+            const float dy = ((l - tl) + (c - u)) * 0.5f;
+            return sqrtf(dx * dx + dy * dy) * s;
+        }
+        case 5: {
+            const float dx = ((r - l) + (tr - tl) + (br - bl)) / 6.0f;
+            const float dy = ((d - u) + (bl - tl) + (br - tr)) / 6.0f;
+            return sqrtf(dx * dx + dy * dy) * s;
+        }
+        case 6: {
+            const float lap = dtl + 4.0f * du + dtr + 4.0f * dl + 4.0f * dr + dbl + 4.0f * dd + dbr;
+            return sqrtf(fabsf(lap / 6.0f * 1.4426950408889634f)) * s;
+        }
+        default:
+            return 0.0f;  // analytic DE needs planes
+    }
+}
+
+__device__ void hsv_to_rgb(float hue, float sat, float val, float& r, float& g, float& b) {
+    const float scaled = hue * 6.0f;
+    const int sector = static_cast<int>(floorf(scaled));
+    float f = scaled - static_cast<float>(sector);
+    if ((sector & 1) == 0) f = 1.0f - f;
+    const float m = val * (1.0f - sat);
+    const float n = val * (1.0f - sat * f);
+    r = g = b = 0.0f;
+    switch (sector) {
+        case 0: case 6: r = m; g = n; b = val; break;
+        case 1: r = m; g = val; b = n; break;
+        case 2: r = n; g = val; b = m; break;
+        case 3: r = val; g = n; b = m; break;
+        case 4: r = val; g = m; b = n; break;
+        case 5: r = n; g = m; b = val; break;
+        default: break;
+    }
+}
+
+__device__ __forceinline__ unsigned char dither_byte(float value, int x, int y, int channel) {
+    if (!isfinite(value)) value = 0.0f;
+    const unsigned int coordinate = (static_cast<unsigned int>(x) + static_cast<unsigned int>(channel) * 67u
+                                     + static_cast<unsigned int>(y) * 236u) * 119u;
+    const float mask = static_cast<float>(coordinate & 255u) / 256.0f;
+    const int q = static_cast<int>(floorf(255.0f * value + mask));
+    return static_cast<unsigned char>(q < 0 ? 0 : (q > 255 ? 255 : q));
+}
+
+__global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
+                                                  const KfpDevice k, const unsigned char* __restrict__ lut_global,
+                                                  const double* __restrict__ mc_period, const int* __restrict__ mc_type) {
+    extern __shared__ unsigned char lut[];
+    for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < k.lut_size * 3; i += blockDim.x * blockDim.y) {
+        lut[i] = lut_global[i];
+    }
+    __syncthreads();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= k.width || y >= k.height) return;
+    const long long index = static_cast<long long>(y) * k.width + x;
+    unsigned char* out = rgb + 3 * index;
+    const float raw = __ldg(field + index);
+    if (isfinite(raw) && static_cast<double>(raw) >= static_cast<double>(k.max_iter) - k.field_bias_d) {
+        out[0] = static_cast<unsigned char>(k.interior[0]);
+        out[1] = static_cast<unsigned char>(k.interior[1]);
+        out[2] = static_cast<unsigned char>(k.interior[2]);
+        return;
+    }
+    const float centre = sample(field, k, x, y);
+    const double centre_value = static_cast<double>(centre) + k.field_bias_d + k.smooth_offset_d;
+    const double colour_iter_d = k.flat ? floor(centre_value) : centre_value;
+    const float colour_iter = static_cast<float>(colour_iter_d);
+    float l = centre, r = centre, u = centre, d = centre, tl = centre, tr = centre, bl = centre, br = centre;
+    if (k.needs_difference || k.needs_slopes) {
+        l = reflected(field, k, x, y, -1, 0, centre);
+        u = reflected(field, k, x, y, 0, -1, centre);
+        if (k.needs_difference) {
+            switch (k.differences) {
+                case 0:
+                    tl = reflected(field, k, x, y, -1, -1, centre);
+                    bl = reflected(field, k, x, y, -1, 1, centre);
+                    break;
+                case 1: case 2: case 5: case 6:
+                    r = reflected(field, k, x, y, 1, 0, centre);
+                    d = reflected(field, k, x, y, 0, 1, centre);
+                    tl = reflected(field, k, x, y, -1, -1, centre);
+                    tr = reflected(field, k, x, y, 1, -1, centre);
+                    bl = reflected(field, k, x, y, -1, 1, centre);
+                    br = reflected(field, k, x, y, 1, 1, centre);
+                    break;
+                case 3: case 4:
+                    tl = reflected(field, k, x, y, -1, -1, centre);
+                    break;
+                default:
+                    r = reflected(field, k, x, y, 1, 0, centre);
+                    d = reflected(field, k, x, y, 0, 1, centre);
+                    break;
+            }
+        }
+        if (k.needs_slopes) {
+            if (x == 0) r = reflected(field, k, x, y, 1, 0, centre);
+            if (y == 0) d = reflected(field, k, x, y, 0, 1, centre);
+        }
+    }
+    float gradient = k.needs_difference ? difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br) : 0.0f;
+    float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.width) / 640.0f;
+    if (distance < 0.0f) distance = 0.0f;
+    double transfer_d = colour_iter_d;  // method 0 keeps the exact value
+    float transfer = colour_iter;
+    switch (k.color_method) {
+        case 1: transfer = sqrtf(fmaxf(0.0f, colour_iter)); break;
+        case 2: transfer = powf(fmaxf(0.0f, colour_iter), 1.0f / 3.0f); break;
+        case 3: transfer = logf(fmaxf(1.0f, colour_iter)); break;
+        case 4:
+            transfer_d = 1024.0 * (colour_iter_d - k.transfer_min) / fmax(k.transfer_max - k.transfer_min, 1.0e-12);
+            transfer = static_cast<float>(transfer_d);
+            break;
+        case 5: transfer = fminf(distance, 1024.0f); break;
+        case 6: {
+            const float dt = fminf(sqrtf(fmaxf(0.0f, distance)), 1024.0f);
+            if (static_cast<double>(dt) > k.iter_div) {
+                transfer_d = centre_value;
+                transfer = static_cast<float>(centre_value);
+            } else {
+                transfer = dt;
+            }
+            break;
+        }
+        case 7: transfer = logf(fmaxf(1.0f, distance + 1.0f)); break;
+        case 8: transfer = sqrtf(fmaxf(0.0f, distance)); break;
+        case 9: transfer = logf(1.0f + logf(1.0f + fmaxf(0.0f, colour_iter))); break;
+        case 10: transfer = atanf(colour_iter); break;
+        case 11: transfer = sqrtf(sqrtf(fmaxf(0.0f, colour_iter))); break;
+        default: break;
+    }
+    const bool exact_transfer = k.color_method == 0 || k.color_method == 4
+        || (k.color_method == 6 && transfer_d == centre_value);
+    double palette_value = exact_transfer ? transfer_d : static_cast<double>(transfer);
+    if (isnan(palette_value) || palette_value < 0.0) palette_value = 0.0;
+    if (k.color_method == 5 || k.color_method == 7 || k.color_method == 8) palette_value = fmin(palette_value, 1024.0);
+    if (k.iter_div != 1.0) palette_value /= k.iter_div;
+    const double base = palette_value + k.color_offset;
+    float red, green, blue;
+    auto palette_rgb = [&](double input, float& o_r, float& o_g, float& o_b) {
+        const double size = static_cast<double>(k.lut_size);
+        double position = fmod(input, size);
+        if (position < 0.0) position += size;
+        const double lower_position = floor(position);
+        int lower = static_cast<int>(lower_position);
+        lower = lower < 0 ? 0 : (lower > k.lut_size - 1 ? k.lut_size - 1 : lower);
+        if (k.smooth) {
+            float f = static_cast<float>(position - lower_position);
+            if (k.inverse_transition) f = 1.0f - f;
+            const int upper = (lower + 1) % k.lut_size;
+            const float g = 1.0f - f;
+            o_r = (static_cast<float>(lut[lower * 3]) * g + static_cast<float>(lut[upper * 3]) * f) / 255.0f;
+            o_g = (static_cast<float>(lut[lower * 3 + 1]) * g + static_cast<float>(lut[upper * 3 + 1]) * f) / 255.0f;
+            o_b = (static_cast<float>(lut[lower * 3 + 2]) * g + static_cast<float>(lut[upper * 3 + 2]) * f) / 255.0f;
+        } else {
+            o_r = static_cast<float>(lut[lower * 3]) / 255.0f;
+            o_g = static_cast<float>(lut[lower * 3 + 1]) / 255.0f;
+            o_b = static_cast<float>(lut[lower * 3 + 2]) / 255.0f;
+        }
+    };
+    if (k.multi_color) {
+        const double wave_input = k.smooth ? base : floor(base);
+        float hs = 0.0f, ss = 0.0f, vs = 0.0f;
+        int hc = 0, sc = 0, vc = 0;
+        for (int i = 0; i < k.multi_count; ++i) {
+            const double period = __ldg(mc_period + i);
+            const float wave = period < 0.0 ? static_cast<float>(-period / 100.0)
+                                            : 0.5f + 0.5f * sinf(static_cast<float>(3.14159265358979323846 * wave_input / period));
+            const int type = __ldg(mc_type + i);
+            if (type == 0) { hs += wave; ++hc; }
+            else if (type == 1) { ss += wave; ++sc; }
+            else { vs += wave; ++vc; }
+        }
+        float mr, mg, mb;
+        hsv_to_rgb(hc ? hs / hc : 0.0f, sc ? ss / sc : 0.0f, vc ? vs / vc : 0.0f, mr, mg, mb);
+        if (k.blend_multi_color) {
+            palette_rgb(base, red, green, blue);
+            red = (red + mr) * 0.5f;
+            green = (green + mg) * 0.5f;
+            blue = (blue + mb) * 0.5f;
+        } else {
+            red = mr;
+            green = mg;
+            blue = mb;
+        }
+    } else {
+        palette_rgb(base, red, green, blue);
+    }
+    if (k.needs_slopes) {
+        const float horizontal = x > 0 ? l - centre : centre - r;
+        const float vertical = y == 0 ? centre - d : u - centre;
+        const float projected = (horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
+            * static_cast<float>(k.width) / 640.0f;
+        const float strength = atanf(fabsf(projected)) / (kPiF / 2.0f) * k.slope_ratio / 100.0f;
+        if (projected >= 0.0f) {
+            red *= 1.0f - strength;
+            green *= 1.0f - strength;
+            blue *= 1.0f - strength;
+        } else {
+            red = red * (1.0f - strength) + strength;
+            green = green * (1.0f - strength) + strength;
+            blue = blue * (1.0f - strength) + strength;
+        }
+    }
+    out[0] = dither_byte(red, x, y, 0);
+    out[1] = dither_byte(green, x, y, 1);
+    out[2] = dither_byte(blue, x, y, 2);
+}
+
+// ColorMethod 4 bounds: min/max of floor(sample) over escaped pixels below
+// max_iter - 1 (kfp_transfer_bounds, renderer.cpp:7296-7331).  Doubles are
+// mapped to order-preserving integers so one atomicMin/atomicMax pair works.
+__device__ __forceinline__ unsigned long long ordered(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void kfp_bounds_kernel(const float* __restrict__ field, long long pixels, int max_iter, double field_bias,
+                                  double smooth_offset, unsigned long long* bounds) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float raw = field[i];
+        if (isfinite(raw) && static_cast<double>(raw) >= static_cast<double>(max_iter) - field_bias) continue;
+        const double safe = isfinite(raw) ? fmin(fmax(static_cast<double>(raw) + field_bias, 0.0),
+                                                 static_cast<double>(max_iter))
+                                          : 0.0;
+        const double value = floor(safe + smooth_offset);
+        if (value >= static_cast<double>(max_iter - 1)) continue;
+        const unsigned long long o = ordered(value);
+        lo = o < lo ? o : lo;
+        hi = o > hi ? o : hi;
+    }
+    for (int offset = 16; offset > 0; offset >>= 1) {
+        const unsigned long long a = __shfl_down_sync(0xffffffffu, lo, offset);
+        const unsigned long long b = __shfl_down_sync(0xffffffffu, hi, offset);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(bounds, lo);
+        atomicMax(bounds + 1, hi);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_kfp_bounds(const float* field, long long pixels, int max_iter, double field_bias,
+                              double smooth_offset, unsigned long long* bounds, cudaStream_t stream) {
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    long long blocks = (pixels + 255) / 256;
+    if (blocks > sms * 4LL) blocks = sms * 4LL;
+    if (blocks < 1) blocks = 1;
+    const unsigned long long init[2] = {~0ull, 0ull};
+    cudaError_t status = cudaMemcpyAsync(bounds, init, sizeof init, cudaMemcpyHostToDevice, stream);
+    if (status != cudaSuccess) return status;
+    kfp_bounds_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(field, pixels, max_iter, field_bias,
+                                                                          smooth_offset, bounds);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
+                       const double* mc_period, const int* mc_type, cudaStream_t stream) {
+    KfpDevice k{};
+    k.width = launch.width;
+    k.height = launch.height;
+    k.max_iter = launch.max_iter;
+    k.field_bias = static_cast<float>(launch.field_bias);
+    k.field_bias_d = launch.field_bias;
+    k.smooth_offset = static_cast<float>(launch.smooth_offset);
+    k.smooth_offset_d = launch.smooth_offset;
+    k.color_method = launch.color_method;
+    k.differences = launch.differences;
+    k.smooth = launch.smooth;
+    k.flat = launch.flat;
+    k.inverse_transition = launch.inverse_transition;
+    k.needs_difference = launch.needs_difference;
+    k.needs_slopes = launch.needs_slopes;
+    k.iter_div = launch.iter_div;
+    k.color_offset = launch.color_offset;
+    k.transfer_min = launch.transfer_min;
+    k.transfer_max = launch.transfer_max;
+    k.multi_color = launch.multi_color;
+    k.blend_multi_color = launch.blend_multi_color;
+    k.multi_count = launch.multi_count;
+    k.slope_cos = static_cast<float>(launch.slope_cos);
+    k.slope_sin = static_cast<float>(launch.slope_sin);
+    k.slope_power = static_cast<float>(launch.slope_power);
+    k.slope_ratio = static_cast<float>(launch.slope_ratio);
+    for (int c = 0; c < 3; ++c) k.interior[c] = launch.interior[c];
+    k.lut_size = launch.lut_size;
+    const dim3 block(32, 8);
+    const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
+    const std::size_t shared = static_cast<std::size_t>(launch.lut_size) * 3;
+    if (shared > 48 * 1024) {
+        cudaFuncSetAttribute(kfp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
+    }
+    kfp_kernel<<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type);
+    return cudaGetLastError();
+}
+
+}  // namespace fgb

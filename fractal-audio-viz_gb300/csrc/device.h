@@ -8,13 +8,14 @@
 //   LinearStep[...] x 2             linear and deep-linear hierarchies
 //   AltStep[...]                    2x2 hierarchy (non-Mandelbrot formulas)
 //   Sc[order + 1]                   image-series coefficients
-//   FloatExp-free FP32 mirrors for the floatexp kernels (see render_fe.cu)
+//   FP32-mantissa mirrors of all of the above for the floatexp kernels
 #pragma once
 
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "fractal_gb300.h"
+#include "floatexp32.h"
 #include "reference.h"
 
 namespace fgb {
@@ -26,27 +27,26 @@ struct LevelIndex {
 };
 
 // FP32-mantissa / int32-exponent mirrors used by the floatexp form.
-struct FeOrbitRec {
-    float zr, zi;   // Z_i mantissas sharing exponent ze
-    int ze;
-    float zd_re;    // Z_i as plain float when representable, else 0
-    float zd_im;
-    float margin_m; // |Z_i|^2 - R^2 as float mantissa/exponent
-    int margin_e;
-    float glitch_m; // 1e-7 |Z_i|^2
-    int glitch_e;
-    float pad[7];
+struct FxOrbitRec {
+    float zr, zi;  // Z_i as plain float (0 below the float range)
+    f32x::F2e z;   // Z_i as floatexp
+    f32x::N1e z2;  // |Z_i|^2
+    int pad;
 };
 
-struct FeLinearStep {
-    float ar, ai;
-    int ae;
-    float br, bi;
-    int be;
-    float r2m;
-    int r2e;
+struct FxLinear {
+    f32x::F2e a;
+    f32x::F2e b;
+    f32x::N1e r2;
     int len;
-    int pad[7];
+    int pad;
+};
+
+struct FxCubic {
+    f32x::F2e c[9];
+    f32x::N1e r2;
+    int len;
+    int pad;
 };
 
 struct DeviceTables {
@@ -63,10 +63,13 @@ struct DeviceTables {
     LevelIndex alt_index;
     fx::Sc* series = nullptr;
     int series_terms = 0;
-    // floatexp mirrors
-    FeOrbitRec* fe_orbit = nullptr;
-    FeLinearStep* fe_linear = nullptr;
-    FeLinearStep* fe_deep_linear = nullptr;
+    // floatexp mirrors (built on the first floatexp render)
+    bool fx_ready = false;
+    FxOrbitRec* fx_orbit = nullptr;
+    FxCubic* fx_cubic = nullptr;
+    FxLinear* fx_linear = nullptr;
+    FxLinear* fx_deep_linear = nullptr;
+    f32x::F2e* fx_series = nullptr;
     ~DeviceTables();
 };
 
@@ -197,8 +200,60 @@ struct Outputs {
     double* p_t2 = nullptr;
 };
 
+// Host-resolved parameters of one KFP colour pass (scalar-field ABI).
+struct KfpLaunch {
+    int width, height, max_iter;
+    double field_bias, smooth_offset;
+    int color_method, differences, smooth, flat, inverse_transition;
+    int needs_difference, needs_slopes;
+    double iter_div, color_offset, transfer_min, transfer_max;
+    int multi_color, blend_multi_color, multi_count;
+    double slope_cos, slope_sin, slope_power, slope_ratio;
+    int interior[3];
+    int lut_size;
+};
+
+cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
+                       const double* mc_period, const int* mc_type, cudaStream_t stream);
+cudaError_t launch_kfp_bounds(const float* field, long long pixels, int max_iter, double field_bias,
+                              double smooth_offset, unsigned long long* bounds, cudaStream_t stream);
+
 // Stats slots (the reference's extended stats order, renderer.cpp:4676-4706).
 constexpr int kStatsSlots = 39;
+
+// Parameters of one floatexp-form deep Mandelbrot field render.
+struct FxParams {
+    const FxOrbitRec* orbit;
+    int orbit_size;
+    const FxCubic* cubic;
+    LevelIndex cubic_index;
+    const FxLinear* linear;
+    LevelIndex linear_index;
+    const f32x::F2e* series;
+    int series_terms;
+    int series_iteration;
+    int series_on;
+    f32x::N1e series_r2;
+    f32x::F2e view_width;   // real parts carry the spans
+    f32x::F2e view_height;
+    int coordinate_mode;
+    int width;
+    int height;
+    int max_iter;
+    int map_end;
+    int disable_bla;
+    int strict;
+    int allow_recovery;
+    int escape_mode;
+    int max_bla_len;
+    int max_lin_len;
+    int approx_order;
+    float output_bias;
+    float* out;
+    std::uint32_t* counts;
+};
+
+cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stream);
 
 struct ThreadRuntime;
 // Floatexp (FP32 mantissa / int32 exponent) form of a reference render.

@@ -27,9 +27,11 @@ DeviceTables::~DeviceTables() {
     cudaFree(deep_linear);
     cudaFree(alt);
     cudaFree(series);
-    cudaFree(fe_orbit);
-    cudaFree(fe_linear);
-    cudaFree(fe_deep_linear);
+    cudaFree(fx_orbit);
+    cudaFree(fx_cubic);
+    cudaFree(fx_linear);
+    cudaFree(fx_deep_linear);
+    cudaFree(fx_series);
     if (device >= 0 && current >= 0 && current != device) cudaSetDevice(current);
 }
 
@@ -61,7 +63,86 @@ T* upload_levels(const std::vector<std::vector<T>>& levels, LevelIndex& index) {
     return upload(flat);
 }
 
+f32x::F2e to_f2e(const fx::Sc& v) {
+    if (v.re == 0.0 && v.im == 0.0) return f32x::zero();
+    return f32x::norm(static_cast<float>(v.re), static_cast<float>(v.im), v.e);
+}
+
+f32x::N1e to_n1e(const fx::Fe& v) {
+    if (v.m == 0.0 || !fx::fe_finite(v)) {
+        f32x::N1e r;
+        r.m = fx::fe_finite(v) ? 0.0f : 3.0e38f;
+        r.e = fx::fe_finite(v) ? 0 : 0x3fffffff;
+        return r;
+    }
+    return f32x::n_norm(static_cast<float>(v.m), v.e);
+}
+
+float plain_float(double mantissa, int exponent) {
+    const double v = fx::scale2(mantissa, exponent);
+    const double a = v < 0 ? -v : v;
+    if (!(a < 3.0e38)) return v < 0 ? -3.0e38f : 3.0e38f;
+    if (a < 1.0e-37) return 0.0f;
+    return static_cast<float>(v);
+}
+
 }  // namespace
+
+// FP32 mirrors of the tables for the floatexp form, made once per handle.
+void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
+    std::lock_guard<std::mutex> lock(ctx.device_mutex);
+    if (dev.fx_ready) return;
+    const OrbitData& orbit = *ctx.orbit;
+    std::vector<FxOrbitRec> records(orbit.scaled.size());
+    for (std::size_t i = 0; i < records.size(); ++i) {
+        const fx::Sc& z = orbit.scaled[i];
+        FxOrbitRec& r = records[i];
+        std::memset(&r, 0, sizeof r);
+        r.zr = plain_float(z.re, z.e);
+        r.zi = plain_float(z.im, z.e);
+        r.z = to_f2e(z);
+        const fx::Nrm n = fx::sc_norm2(z);
+        r.z2 = to_n1e(fx::fe_make(n.m, n.e));
+    }
+    dev.fx_orbit = upload(records);
+    auto cubic_levels = [&](const std::vector<std::vector<CubicStep>>& levels) {
+        std::vector<std::vector<FxCubic>> out;
+        for (const auto& level : levels) {
+            auto& dst = out.emplace_back();
+            for (const CubicStep& s : level) {
+                FxCubic c{};
+                for (int k = 0; k < 9; ++k) c.c[k] = to_f2e(s.c[k]);
+                c.r2 = to_n1e(s.r2);
+                c.len = s.len;
+                dst.push_back(c);
+            }
+        }
+        return out;
+    };
+    auto linear_levels = [&](const std::vector<std::vector<LinearStep>>& levels) {
+        std::vector<std::vector<FxLinear>> out;
+        for (const auto& level : levels) {
+            auto& dst = out.emplace_back();
+            for (const LinearStep& s : level) {
+                FxLinear l{};
+                l.a = to_f2e(s.a);
+                l.b = to_f2e(s.b);
+                l.r2 = to_n1e(s.r2);
+                l.len = s.len;
+                dst.push_back(l);
+            }
+        }
+        return out;
+    };
+    LevelIndex unused;
+    dev.fx_cubic = upload_levels(cubic_levels(ctx.cubic), unused);
+    dev.fx_linear = upload_levels(linear_levels(ctx.linear), unused);
+    dev.fx_deep_linear = upload_levels(linear_levels(ctx.deep_linear), unused);
+    std::vector<f32x::F2e> series;
+    for (const fx::Sc& c : ctx.series.coeff) series.push_back(to_f2e(c));
+    dev.fx_series = upload(series);
+    dev.fx_ready = true;
+}
 
 std::shared_ptr<DeviceTables> device_tables(ReferenceContext& ctx) {
     const int device = current_device();

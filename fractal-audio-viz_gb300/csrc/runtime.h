@@ -57,5 +57,6 @@ ThreadRuntime& thread_runtime();
 void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes);
 
 std::shared_ptr<DeviceTables> device_tables(ReferenceContext& ctx);
+void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev);
 
 }  // namespace fgb

@@ -268,6 +268,10 @@ _GB300_ABI = (
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.POINTER(RenderOptions), ctypes.c_void_p)),
+    ("fractal_gb300_fma_peak", ctypes.c_int, (ctypes.c_int, ctypes.POINTER(ctypes.c_double))),
+    ("fractal_gb300_colourise_kfp_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+      ctypes.POINTER(KfpOptions), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p)),
     ("fractal_gb300_colourise_device", ctypes.c_int,
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,

@@ -211,6 +211,18 @@ int fractal_colourise(const float *field, uint8_t *output, int width, int height
                       double phase, double vocal, double instrumental, double pitch,
                       int threads);
 
+/* renderer.h:450-463: Kalles .kfp transfer on the scalar field (1024-entry
+ * cyclic LUT supplied by the caller, distance/slope shading, dither). */
+int fractal_colourise_kfp(const float *field, uint8_t *output, int width, int height, int max_iter,
+                          double phase, double vocal, double instrumental, double pitch,
+                          const FractalKfpOptions *options, const uint8_t *lut, int lut_size,
+                          int threads);
+/* renderer.h:503-516: compatibility name of the same transfer. */
+int fractal_colourise_kfp_precise(const float *field, uint8_t *output, int width, int height,
+                                  int max_iter, double phase, double vocal, double instrumental,
+                                  double pitch, const FractalKfpOptions *options,
+                                  const uint8_t *lut, int lut_size, int threads);
+
 /* ---------------------------------------------------------------------
  * Part 2: GB300 extensions (no counterpart in the reference)
  *
@@ -243,6 +255,18 @@ int fractal_gb300_render_direct_device(float *field, uint32_t *counts, int width
                                        const char *y_center, int max_iter, int formula,
                                        double julia_real, double julia_imag,
                                        const FractalRenderOptions *options, void *stream);
+
+/* FMA-pipe throughput of the current device in TFLOP/s (2 flops per FMA),
+ * measured with eight independent FMA chains per thread; precision_bits is
+ * 64 or 32.  Returns 0 on success.  Used as the roofline denominator of the
+ * iteration kernels. */
+int fractal_gb300_fma_peak(int precision_bits, double *tflops);
+
+/* KFP colour pass from a device field to device RGB8; `lut` is device
+ * memory (lut_size x 3 bytes). */
+int fractal_gb300_colourise_kfp_device(const float *field, uint8_t *rgb, int width, int height,
+                                       int max_iter, const FractalKfpOptions *options,
+                                       const uint8_t *lut, int lut_size, void *stream);
 
 /* Aurora colour pass from a device field to device RGB8. */
 int fractal_gb300_colourise_device(const float *field, uint8_t *rgb, int width, int height,

@@ -148,3 +148,24 @@ def alternate_cases() -> list[dict]:
         cases.append(_m(f"{formula}_e10_96x54", kind="reference", formula=formula, centre=e30,
                         log10_zoom=10.0, width=96, height=54, max_iter=20_000))
     return cases
+
+
+def kfp_cases() -> list[dict]:
+    """KFP colour cases: (field fixture, profile recipe, max_iter, field_bias).
+
+    Profiles are named recipes built by fractal-audio-viz_gb300/kfp.py; the
+    fields are stored parity fixtures, so the colour pass is tested on the
+    reference's own scalar fields.
+    """
+    cases = []
+    fields = [("e30_160x90", 50_000, 0.0), ("fhd_level00_128x72", 4709, 0.0), ("deep_p80_e32_96x54", 50_000, 0.0),
+              ("e100_bias_64x36", 200_000, 400.0), ("odd_37x23", 20_000, 0.0), ("odd_3x5", 20_000, 0.0)]
+    recipes = ["default", "seeded16", "multicolor", "flat_nosmooth", "inverse"]
+    recipes += [f"method{m}" for m in range(12)] + [f"differences{d}" for d in range(8)]
+    for field, max_iter, bias in fields:
+        for recipe in recipes:
+            if field != "e30_160x90" and recipe.startswith(("method", "differences")):
+                continue
+            cases.append(dict(name=f"kfp_{recipe}_{field}", field=field, recipe=recipe, max_iter=max_iter,
+                              field_bias=bias))
+    return cases

@@ -1,0 +1,99 @@
+"""GPU: the floatexp form (FP32 mantissa / int32 exponent) against FP64.
+
+The floatexp form is the throughput form; the plain FP64 form is the parity
+form.  Their iteration counts may differ where FP32 rounding flips an escape
+decision.  The bar (the benchmark spec): at most 1e-4 of pixels with a different
+count (NaN glitch-mask differences included) against the FP64 oracle, over
+the deep Mandelbrot parity fields and the full 1920x1080 keyframes of the
+FHD stack at its deepest levels.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from .conftest import golden_arrays
+from .golden import cases as case_defs
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+MAX_MISMATCH = 1e-4
+
+
+def render_device(product, package, case, form):
+    native = package.native
+    w, h = case["width"], case["height"]
+    x, y = case["centre"]["re"], case["centre"]["im"]
+    root_log = case.get("root_log10_zoom", case["log10_zoom"])
+    bits = case_defs.precision_bits(x, y, root_log)
+    options = native.RenderOptions(**case.get("options", {}))
+    handle = native.create_reference(product, x, y, case_defs.zoom_text(root_log).encode(), case.get("root_max_iter", case["max_iter"]),
+                                     bits, case["image_series_order"], reusable=True,
+                                     options=options if case.get("options") else None)
+    handles = [handle]
+    if case.get("clone"):
+        handles.append(native.clone_reference(product, handle, case_defs.zoom_text(case["log10_zoom"]).encode()))
+    field = torch.empty(w * h, dtype=torch.float32, device="cuda")
+    counts = torch.empty(w * h, dtype=torch.int32, device="cuda")
+    try:
+        status = product.fractal_gb300_render_reference_device(
+            ctypes.c_void_p(field.data_ptr()), ctypes.c_void_p(counts.data_ptr()), w, h,
+            case_defs.zoom_text(case["log10_zoom"]).encode(), ctypes.c_void_p(handles[-1]), case["max_iter"],
+            case["series_order"], case["series_block"], ctypes.byref(options), form, None)
+        assert status == 0, native.last_error(product)
+        torch.cuda.synchronize()
+    finally:
+        for hd in reversed(handles):
+            product.fractal_destroy_reference(hd)
+    return field.cpu().numpy(), counts.cpu().numpy().view(np.uint32)
+
+
+DEEP = [c for c in case_defs.parity_cases()
+        if c["kind"] == "reference" and c["log10_zoom"] >= 6.0 and not c.get("options", {}).get("strict") == 0]
+
+
+def test_plain_device_form_matches_fixtures(product, package):
+    for case in DEEP:
+        stored = golden_arrays(case["name"])
+        if stored is None:
+            continue
+        _, counts = render_device(product, package, case, 0)
+        np.testing.assert_array_equal(counts, stored["counts"], err_msg=case["name"])
+
+
+def test_floatexp_count_mismatch_within_budget(product, package):
+    differing = 0
+    total = 0
+    for case in DEEP:
+        plain_field, plain_counts = render_device(product, package, case, 0)
+        fe_field, fe_counts = render_device(product, package, case, 1)
+        diff = (plain_counts != fe_counts) | (np.isnan(plain_field) != np.isnan(fe_field))
+        differing += int(diff.sum())
+        total += diff.size
+        finite = np.isfinite(plain_field) & np.isfinite(fe_field) & ~diff
+        if finite.any():
+            # Smooth values agree to FP32 accuracy where the counts agree.
+            assert np.max(np.abs(plain_field[finite] - fe_field[finite])) < 1e-2, case["name"]
+    assert differing / total <= MAX_MISMATCH, f"{differing} of {total} pixels differ"
+
+
+def test_floatexp_full_fhd_keyframes(product, package):
+    levels = case_defs.fhd_stack_levels()
+    e50 = case_defs.centres()["fhd_stack_e50"]
+    differing = 0
+    total = 0
+    for level in (20, 38, 54):
+        _, log_zoom, cap = levels[level]
+        case = case_defs._m("fhd", kind="reference", centre=e50, log10_zoom=log_zoom, width=1920, height=1080,
+                            max_iter=cap, root_log10_zoom=levels[-1][1], root_max_iter=levels[-1][2], clone=True)
+        plain_field, plain_counts = render_device(product, package, case, 0)
+        fe_field, fe_counts = render_device(product, package, case, 1)
+        diff = (plain_counts != fe_counts) | (np.isnan(plain_field) != np.isnan(fe_field))
+        differing += int(diff.sum())
+        total += diff.size
+    assert differing / total <= MAX_MISMATCH, f"{differing} of {total} pixels differ"
