@@ -309,14 +309,14 @@ void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outpu
     p.p_t1 = out.p_t1;
     p.p_t2 = out.p_t2;
     // Alternate-formula policy (render_alternate_reference_impl,
-    // renderer.cpp:12064-12140) is completed on the host here.
-    const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
-    p.disable_bla = (!covers || o.disable_bla != 0) ? 1 : 0;
-    p.max_lin_len = std::clamp(static_cast<int>(o.max_linear_bla_length), 1, kMaxSafeLinearBlaLength);
-    p.series_on = ctx.formula == kFormulaJulia && ctx.series.enabled
-        && ctx.series.order >= o.series_min_terms && ctx.series.order <= o.series_max_terms
-        && fx::fe_cmp(g.current_input_radius, fx::fe_sqrt(ctx.series.r2)) <= 0
-        && ctx.series.iteration < max_iter && dev.series_terms > 1;
+    // renderer.cpp:12116-12137): the block table is used whenever it exists
+    // (each block checks the pixel's parameter radius itself), the series
+    // only for Julia, and cycle detection only for non-strict renders.
+    p.disable_bla = o.disable_bla != 0 ? 1 : 0;
+    p.max_lin_len = std::clamp(static_cast<int>(o.max_linear_bla_length), 2, kMaxSafeLinearBlaLength);
+    p.series_on = ctx.formula == kFormulaJulia && ctx.series.enabled && ctx.series.iteration < max_iter
+        && dev.series_terms > 1;
+    p.cycle = (o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0)) ? 1 : 0;
     if (o.time_budget_ms > 0) {
         check_cuda(launch_stamp_time(rt.stamp, stream), "time stamp launch");
         p.deadline_base = rt.stamp;

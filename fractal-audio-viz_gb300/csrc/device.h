@@ -141,6 +141,7 @@ struct AltParams {
     int disable_bla;
     int strict;
     int allow_recovery;
+    int cycle;
     int escape_mode;
     int max_lin_len;
     double output_bias;

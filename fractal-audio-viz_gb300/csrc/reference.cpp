@@ -1105,7 +1105,12 @@ std::vector<OrbitRec> make_orbit_records(const ReferenceContext& ctx) {
         r.zd_re = orbit.re_d[i];
         r.zd_im = orbit.im_d[i];
         r.parts = fx::sc_to_fec(orbit.scaled[i]);
-        r.margin = fx::fe_sub(fx::fec_norm2(r.parts), escape_r2);
+        // Mandelbrot rebuilds the escape margin from the compact orbit
+        // (renderer.cpp:8374-8390); the other formulas use the MPFR margin
+        // of each step (renderer.cpp:12037-12052).
+        r.margin = ctx.formula == kFormulaMandelbrot || i >= orbit.escape_margin.size()
+            ? fx::fe_sub(fx::fec_norm2(r.parts), escape_r2)
+            : orbit.escape_margin[i];
         const fx::Nrm n = fx::sc_norm2(orbit.scaled[i]);
         const fx::Fe norm = fx::fe_make(n.m, n.e);
         r.glitch = (norm.m != 0.0 && fx::fe_finite(norm)) ? fx::fe_mul(norm, 1.0e-7) : fx::fe_zero();

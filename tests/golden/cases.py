@@ -135,18 +135,32 @@ def parity_cases() -> list[dict]:
 
 
 def alternate_cases() -> list[dict]:
-    """Deep alternate-formula fields (render_alternate_reference_impl)."""
+    """Deep fields of the other formulas (render_alternate_reference_impl).
+
+    Julia views centre on the repelling fixed point of z^2 + c (the
+    reference pipeline's Julia zoom target, recovered in MPFR); burning-ship
+    and tricorn views centre on seeded parameter-set boundary points.
+    """
     c = centres()
-    julia = c["julia_c"]
-    e30 = c["field_640x360_e30"]
     cases = []
-    for index, jc in enumerate(julia[:2]):
-        cases.append(_m(f"julia{index}_e20_96x54", kind="reference", formula="julia",
-                        centre=dict(re="0.1", im="0.05"), julia=(jc["re"], jc["im"]),
-                        log10_zoom=8.0, width=96, height=54, max_iter=20_000))
-    for formula in ("burning-ship", "tricorn"):
-        cases.append(_m(f"{formula}_e10_96x54", kind="reference", formula=formula, centre=e30,
-                        log10_zoom=10.0, width=96, height=54, max_iter=20_000))
+    for key in ("julia_fixed_1", "julia_fixed_2"):
+        jf = c[key]
+        for log_zoom, size in ((9.0, (96, 54)), (15.0, (64, 36))):
+            cases.append(_m(f"{key}_e{int(log_zoom)}_{size[0]}x{size[1]}", kind="reference", formula="julia",
+                            centre=dict(re=jf["re"], im=jf["im"]), julia=(jf["c_re"], jf["c_im"]),
+                            log10_zoom=log_zoom, width=size[0], height=size[1], max_iter=20_000))
+    for formula, key in (("burning-ship", "burning_ship_boundary"), ("tricorn", "tricorn_boundary")):
+        for log_zoom, size in ((7.0, (96, 54)), (12.0, (64, 36))):
+            cases.append(_m(f"{formula}_e{int(log_zoom)}_{size[0]}x{size[1]}", kind="reference", formula=formula,
+                            centre=c[key], log10_zoom=log_zoom, width=size[0], height=size[1], max_iter=10_000))
+    # Non-strict (cycle detection) and linear-block-free variants.
+    jf = c["julia_fixed_1"]
+    cases.append(_m("julia_fixed_1_nonstrict_64x36", kind="reference", formula="julia",
+                    centre=dict(re=jf["re"], im=jf["im"]), julia=(jf["c_re"], jf["c_im"]), log10_zoom=9.0,
+                    width=64, height=36, max_iter=20_000, options=dict(strict=0)))
+    cases.append(_m("burning-ship_nobla_48x27", kind="reference", formula="burning-ship",
+                    centre=c["burning_ship_boundary"], log10_zoom=7.0, width=48, height=27, max_iter=10_000,
+                    options=dict(disable_bla=1)))
     return cases
 
 

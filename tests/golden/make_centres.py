@@ -217,6 +217,56 @@ def nucleus_near(centre: dict, period: int, offset_log10: float, bits: int, digi
                 "distance_to_misiurewicz": float(abs(cm - m)), "re": re, "im": im}
 
 
+def julia_fixed_point(c_re: str, c_im: str, digits: int = 120):
+    """Repelling fixed point z* = (1 +- sqrt(1 - 4c)) / 2 (the larger-modulus
+    root) of z^2 + c: the reference pipeline's deep Julia zoom target."""
+    with mpmath.workdps(digits + 20):
+        c = mpmath.mpc(mpmath.mpf(c_re), mpmath.mpf(c_im))
+        root = mpmath.sqrt(1 - 4 * c)
+        a, b = (1 + root) / 2, (1 - root) / 2
+        z = a if abs(a) >= abs(b) else b
+        re = mpmath.nstr(z.real, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+        im = mpmath.nstr(z.imag, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+        return {"re": re, "im": im, "c_re": c_re, "c_im": c_im}
+
+
+def _alt_bounded(formula: str, c, budget: int) -> bool:
+    z = mpmath.mpc(0)
+    for _ in range(budget):
+        if formula == "burning-ship":
+            z = mpmath.mpc(abs(z.real), abs(z.imag)) ** 2 + c
+        else:
+            z = mpmath.conj(z) ** 2 + c
+        if z.real * z.real + z.imag * z.imag > 4:
+            return False
+    return True
+
+
+def alternate_boundary(formula: str, seed: int, digits: int = 40, budget: int = 1500):
+    """A boundary point of the burning-ship or tricorn parameter set found by
+    high-precision bisection along a seeded ray from an interior start."""
+    rng = np.random.default_rng(seed)
+    with mpmath.workdps(digits + 10):
+        for _ in range(200):
+            angle = rng.uniform(0.0, 2.0 * math.pi)
+            start = mpmath.mpc(-0.2, 0.0) if formula == "tricorn" else mpmath.mpc(-0.3, -0.1)
+            direction = mpmath.mpc(math.cos(angle), math.sin(angle))
+            inner, outer = mpmath.mpf(0), mpmath.mpf(2)
+            if not _alt_bounded(formula, start, budget) or _alt_bounded(formula, start + outer * direction, budget):
+                continue
+            for _ in range(int(digits * 3.4)):
+                mid = (inner + outer) / 2
+                if _alt_bounded(formula, start + mid * direction, budget):
+                    inner = mid
+                else:
+                    outer = mid
+            c = start + inner * direction
+            re = mpmath.nstr(c.real, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            im = mpmath.nstr(c.imag, digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            return {"seed": seed, "angle": angle, "re": re, "im": im, "budget": budget}
+    raise RuntimeError("no boundary point found")
+
+
 def _bounded(c: complex, budget: int = 4000) -> bool:
     z = 0j
     for _ in range(budget):
@@ -263,6 +313,10 @@ def main() -> int:
         # Deep minibrots on the e100 point's spiral (BLA-heavy views).
         "deep_nucleus_p70": nucleus_near(centres["field_e100"], 70, -18.0, bits=700, digits=210),
         "deep_nucleus_p80": nucleus_near(centres["field_e100"], 80, -18.0, bits=700, digits=210),
+        "julia_fixed_1": julia_fixed_point(centres["julia_c"][1]["re"], centres["julia_c"][1]["im"]),
+        "julia_fixed_2": julia_fixed_point(centres["julia_c"][2]["re"], centres["julia_c"][2]["im"]),
+        "burning_ship_boundary": alternate_boundary("burning-ship", seed=8101),
+        "tricorn_boundary": alternate_boundary("tricorn", seed=8102),
     })
     path = os.path.join(HERE, "centres.json")
     with open(path, "w", encoding="ascii") as handle:
@@ -270,7 +324,7 @@ def main() -> int:
         handle.write("\n")
     for key, value in centres.items():
         if isinstance(value, dict):
-            print(key, value.get("preperiod"), value["period"], value.get("size_estimate"),
+            print(key, value.get("preperiod"), value.get("period"), value.get("size_estimate"),
                   value["re"][:24], value["im"][:24])
     return 0
 

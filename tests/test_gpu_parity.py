@@ -21,7 +21,7 @@ from .golden.runner import run_case, summary
 
 pytestmark = pytest.mark.gpu
 
-CASES = case_defs.parity_cases()
+CASES = case_defs.parity_cases() + case_defs.alternate_cases()
 
 
 def _field_bits(field):
