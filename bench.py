@@ -338,15 +338,18 @@ def run_gpu_arm(args) -> int:
 
     # End to end through the renderer.h ABI: host output buffers, the field
     # copied back every keyframe.
+    # Backend 4 selects the same floatexp form through the ABI; backend 0 is
+    # the plain form.
+    e2e_options = native.RenderOptions(backend=4 if forms["chosen"] == 1 else 0)
     e2e_steps = max(1, args.steps // 2)
     for keyframe in stack.keyframes[:2]:
-        stack.render_host(keyframe, WIDTH, HEIGHT)
+        stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for keyframe in stack.keyframes:
-            stack.render_host(keyframe, WIDTH, HEIGHT)
+            stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
     e2e_s = time.perf_counter() - t0
-    e2e_value = world * plain_work * e2e_steps / e2e_s / 1e9
+    e2e_value = world * work * e2e_steps / e2e_s / 1e9
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

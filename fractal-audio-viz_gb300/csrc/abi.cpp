@@ -983,8 +983,15 @@ int fractal_render_reference_ex_planes(float* output, int width, int height, con
         if (max_iter > ctx->requested_max_iter) throw Failure{"render iteration count exceeds prepared reference"};
         render_to_host(output, planes, width, height, [&](const Outputs& out, bool collect, ThreadRuntime& rt,
                                                           cudaStream_t stream) {
-            render_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o,
-                                  collect, rt, stream);
+            // Backend 4 selects the floatexp form for field-only renders;
+            // backend 0 (the default) is the plain, reference-identical form.
+            if (o.backend == FRACTAL_BACKEND_CUDA && planes == nullptr && !collect) {
+                render_floatexp_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order,
+                                               series_block, o, rt, stream);
+            } else {
+                render_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o,
+                                      collect, rt, stream);
+            }
         });
     });
 }
@@ -1129,6 +1136,8 @@ int fractal_gb300_colourise_kfp_device(const float* field, uint8_t* rgb, int wid
         kfp_colour(field, rgb, width, height, max_iter, *options, in, lut_size, rt, stream);
     });
 }
+
+void fractal_gb300_set_table_builder(int on_device) { set_device_table_builder(on_device != 0); }
 
 int fractal_gb300_device_count(void) {
     int count = 0;

@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     float gradient = k.needs_difference ? difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br) : 0.0f;
     float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.width) / 640.0f;
     if (distance < 0.0f) distance = 0.0f;
-    double transfer_d = colour_iter_d;  // method 0 keeps the exact value
+    double transfer_d = colour_iter_d;  // kept exact for methods 0, 4 and 6's iteration branch
+    bool exact_transfer = k.color_method == 0 || k.color_method == 4;
     float transfer = colour_iter;
     switch (k.color_method) {
         case 1: transfer = sqrtf(fmaxf(0.0f, colour_iter)); break;
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
             if (static_cast<double>(dt) > k.iter_div) {
                 transfer_d = centre_value;
                 transfer = static_cast<float>(centre_value);
+                exact_transfer = true;
             } else {
                 transfer = dt;
             }
@@ -232,8 +234,6 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         case 11: transfer = sqrtf(sqrtf(fmaxf(0.0f, colour_iter))); break;
         default: break;
     }
-    const bool exact_transfer = k.color_method == 0 || k.color_method == 4
-        || (k.color_method == 6 && transfer_d == centre_value);
     double palette_value = exact_transfer ? transfer_d : static_cast<double>(transfer);
     if (isnan(palette_value) || palette_value < 0.0) palette_value = 0.0;
     if (k.color_method == 5 || k.color_method == 7 || k.color_method == 8) palette_value = fmin(palette_value, 1024.0);

@@ -88,6 +88,8 @@ float plain_float(double mantissa, int exponent) {
 
 }  // namespace
 
+void convert_fx_levels(DeviceTables& dev, cudaStream_t stream);
+
 // FP32 mirrors of the tables for the floatexp form, made once per handle.
 void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
     std::lock_guard<std::mutex> lock(ctx.device_mutex);
@@ -134,10 +136,14 @@ void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
         }
         return out;
     };
-    LevelIndex unused;
-    dev.fx_cubic = upload_levels(cubic_levels(ctx.cubic), unused);
-    dev.fx_linear = upload_levels(linear_levels(ctx.linear), unused);
-    dev.fx_deep_linear = upload_levels(linear_levels(ctx.deep_linear), unused);
+    if (ctx.bla_on_device) {
+        convert_fx_levels(dev, thread_runtime().stream);
+    } else {
+        LevelIndex unused;
+        dev.fx_cubic = upload_levels(cubic_levels(ctx.cubic), unused);
+        dev.fx_linear = upload_levels(linear_levels(ctx.linear), unused);
+        dev.fx_deep_linear = upload_levels(linear_levels(ctx.deep_linear), unused);
+    }
     std::vector<f32x::F2e> series;
     for (const fx::Sc& c : ctx.series.coeff) series.push_back(to_f2e(c));
     dev.fx_series = upload(series);
@@ -147,20 +153,27 @@ void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
 std::shared_ptr<DeviceTables> device_tables(ReferenceContext& ctx) {
     const int device = current_device();
     std::lock_guard<std::mutex> lock(ctx.device_mutex);
-    if (ctx.device && ctx.device->device == device) return ctx.device;
-    auto tables = std::make_shared<DeviceTables>();
-    tables->device = device;
-    const std::vector<OrbitRec> records = make_orbit_records(ctx);
-    tables->orbit = upload(records);
-    tables->orbit_size = static_cast<int>(records.size());
-    tables->cubic = upload_levels(ctx.cubic, tables->cubic_index);
-    tables->linear = upload_levels(ctx.linear, tables->linear_index);
-    tables->deep_linear = upload_levels(ctx.deep_linear, tables->deep_linear_index);
-    tables->alt = upload_levels(ctx.alt, tables->alt_index);
-    tables->series = upload(ctx.series.coeff);
-    tables->series_terms = static_cast<int>(ctx.series.coeff.size());
-    ctx.device = tables;
-    return tables;
+    if (ctx.device && ctx.device->device != device) {
+        if (ctx.bla_on_device) throw Failure{"reference tables were built on another CUDA device"};
+        ctx.device.reset();
+    }
+    if (!ctx.device) ctx.device = std::make_shared<DeviceTables>();
+    DeviceTables& t = *ctx.device;
+    t.device = device;
+    if (t.orbit == nullptr) {
+        const std::vector<OrbitRec> records = make_orbit_records(ctx);
+        t.orbit = upload(records);
+        t.orbit_size = static_cast<int>(records.size());
+        t.series = upload(ctx.series.coeff);
+        t.series_terms = static_cast<int>(ctx.series.coeff.size());
+        if (!ctx.bla_on_device) {
+            t.cubic = upload_levels(ctx.cubic, t.cubic_index);
+            t.linear = upload_levels(ctx.linear, t.linear_index);
+            t.deep_linear = upload_levels(ctx.deep_linear, t.deep_linear_index);
+            t.alt = upload_levels(ctx.alt, t.alt_index);
+        }
+    }
+    return ctx.device;
 }
 
 }  // namespace fgb

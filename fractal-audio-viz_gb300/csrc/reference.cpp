@@ -12,12 +12,15 @@
 #include <locale.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <unordered_map>
+
+#include "bla_math.h"
 
 namespace fgb {
 
@@ -186,7 +189,6 @@ bool parse_classic(const char* text, long double& value) {
     return *end == '\0';
 }
 
-void to_fec(const fx::Fec& v, fx::Fec& out) { out = v; }
 
 }  // namespace
 
@@ -594,126 +596,12 @@ void build_image_series(ReferenceContext& ctx, const std::vector<fx::Fec>* overr
 }
 
 // -------------------------------------------------------- Mandelbrot BLA
-struct BuilderCubic {
-    fx::Fec c[9];  // A B C D E F G H I
-    fx::Fe r2;
-    int len;
-};
-
-struct BuilderLinear {
-    fx::Fec a;
-    fx::Fec b;
-    fx::Fe r2;
-    int len;
-};
-
-// Radius of a composed map y(x(.)) (renderer.cpp:11528-11540).
-fx::Fe merged_radius(const fx::Fe& x_r2, const fx::Fe& y_r2, const fx::Fe& x_a, const fx::Fe& x_b,
-                     const fx::Fe& input_radius) {
-    fx::Fe r = fx::fe_sqrt(x_r2);
-    const fx::Fe remaining = fx::fe_sub(fx::fe_sqrt(y_r2), fx::fe_mul(x_b, input_radius));
-    if (fx::fe_cmp(remaining, fx::fe_zero()) > 0 && fx::fe_cmp(x_a, fx::fe_zero()) > 0) {
-        r = fx::fe_min(r, fx::fe_div(remaining, x_a));
-    } else {
-        r = fx::fe_zero();
-    }
-    return r;
-}
-
-// merge_bla (renderer.cpp:11528-11586): the composition y(x(d, c), c) of two
-// cubic bivariate maps, truncated at degree three.
-BuilderCubic merge_cubic(const BuilderCubic& y, const BuilderCubic& x, const fx::Fe& input_radius) {
-    using namespace fx;
-    const Fe x_a = fe_sqrt(fec_norm2(x.c[0]));
-    const Fe x_b = fe_sqrt(fec_norm2(x.c[1]));
-    const Fe radius = merged_radius(x.r2, y.r2, x_a, x_b, input_radius);
-    const Fe two = fe_from(2.0, 0);
-    const Fe three = fe_from(3.0, 0);
-    const Fec &xA = x.c[0], &xB = x.c[1], &xC = x.c[2], &xD = x.c[3], &xE = x.c[4];
-    const Fec &yA = y.c[0], &yB = y.c[1], &yC = y.c[2], &yD = y.c[3], &yE = y.c[4], &yF = y.c[5],
-              &yG = y.c[6], &yH = y.c[7], &yI = y.c[8];
-    const Fec x_a2 = fec_mul(xA, xA);
-    const Fec x_ab = fec_mul(xA, xB);
-    const Fec x_b2 = fec_mul(xB, xB);
-    const Fec x_a3 = fec_mul(x_a2, xA);
-    const Fec x_a2b = fec_mul(x_a2, xB);
-    const Fec x_ab2 = fec_mul(xA, x_b2);
-    const Fec x_b3 = fec_mul(x_b2, xB);
-    BuilderCubic r;
-    r.c[0] = fec_mul(yA, xA);
-    r.c[1] = fec_add(fec_mul(yA, xB), yB);
-    r.c[2] = fec_add(fec_mul(yA, xC), fec_mul(yC, x_a2));
-    r.c[3] = fec_add(fec_add(fec_mul(yA, xD), fec_mul(yC, fec_scale(x_ab, two))), fec_mul(yD, xA));
-    r.c[4] = fec_add(fec_add(fec_mul(yA, xE), fec_mul(yC, x_b2)), fec_add(fec_mul(yD, xB), yE));
-    r.c[5] = fec_add(fec_add(fec_mul(yA, x.c[5]), fec_mul(yC, fec_scale(fec_mul(xA, xC), two))),
-                     fec_mul(yF, x_a3));
-    r.c[6] = fec_add(
-        fec_add(fec_add(fec_mul(yA, x.c[6]),
-                        fec_mul(yC, fec_scale(fec_add(fec_mul(xA, xD), fec_mul(xB, xC)), two))),
-                fec_add(fec_mul(yD, xC), fec_mul(yF, fec_scale(x_a2b, three)))),
-        fec_mul(yG, x_a2));
-    r.c[7] = fec_add(
-        fec_add(fec_add(fec_mul(yA, x.c[7]),
-                        fec_mul(yC, fec_scale(fec_add(fec_mul(xA, xE), fec_mul(xB, xD)), two))),
-                fec_add(fec_mul(yD, xD), fec_mul(yF, fec_scale(x_ab2, three)))),
-        fec_add(fec_mul(yG, fec_scale(x_ab, two)), fec_mul(yH, xA)));
-    r.c[8] = fec_add(
-        fec_add(fec_add(fec_mul(yA, x.c[8]), fec_mul(yC, fec_scale(fec_mul(xB, xE), two))),
-                fec_add(fec_mul(yD, xE), fec_mul(yF, x_b3))),
-        fec_add(fec_mul(yG, x_b2), fec_add(fec_mul(yH, xB), yI)));
-    r.r2 = fe_sqr(radius);
-    r.len = x.len + y.len;
-    return r;
-}
-
-BuilderLinear merge_linear(const BuilderLinear& y, const BuilderLinear& x, const fx::Fe& input_radius) {
-    using namespace fx;
-    const Fe x_a = fe_sqrt(fec_norm2(x.a));
-    const Fe x_b = fe_sqrt(fec_norm2(x.b));
-    const Fe radius = merged_radius(x.r2, y.r2, x_a, x_b, input_radius);
-    BuilderLinear r;
-    r.a = fec_mul(y.a, x.a);
-    r.b = fec_add(fec_mul(y.a, x.b), y.b);
-    r.r2 = fe_sqr(radius);
-    r.len = x.len + y.len;
-    return r;
-}
-
-CubicStep compact_cubic(const BuilderCubic& s) {
-    bool finite = fx::fe_finite(s.r2);
-    for (int k = 0; k < 9; ++k) finite = finite && fx::fec_finite(s.c[k]);
-    CubicStep r{};
-    for (int k = 0; k < 9; ++k) r.c[k] = fx::sc_from_fe(s.c[k].re, s.c[k].im);
-    r.r2 = finite ? s.r2 : fx::fe_zero();
-    r.len = s.len;
-    return r;
-}
-
-LinearStep compact_linear(const BuilderLinear& s) {
-    const bool finite = fx::fe_finite(s.r2) && fx::fec_finite(s.a) && fx::fec_finite(s.b);
-    LinearStep r{};
-    r.a = fx::sc_from_fe(s.a.re, s.a.im);
-    r.b = fx::sc_from_fe(s.b.re, s.b.im);
-    r.r2 = finite ? s.r2 : fx::fe_zero();
-    r.len = s.len;
-    return r;
-}
-
 std::vector<std::vector<LinearStep>> build_linear_levels(const ReferenceContext& ctx, int base_count,
                                                         const fx::Fe& input_radius) {
-    const fx::Fe tolerance = fx::fe_from(std::ldexp(1.0, -38), 0);
-    const fx::Fe two = fx::fe_from(2.0, 0);
     std::vector<std::vector<BuilderLinear>> levels;
     levels.emplace_back(static_cast<std::size_t>(base_count));
     for (int start = 1; start <= base_count; ++start) {
-        const fx::Fec& ref = ctx.fast_orbit[static_cast<std::size_t>(start)];
-        const fx::Fe radius = fx::fe_mul(tolerance, fx::fe_sqrt(fx::fec_norm2(ref)));
-        BuilderLinear s;
-        s.a = fx::fec_scale(ref, two);
-        s.b = fx::fec_make(fx::fe_from(1.0, 0), fx::fe_zero());
-        s.r2 = fx::fe_sqr(radius);
-        s.len = 1;
-        levels[0][static_cast<std::size_t>(start - 1)] = s;
+        levels[0][static_cast<std::size_t>(start - 1)] = linear_base(ctx.fast_orbit[static_cast<std::size_t>(start)]);
     }
     for (std::size_t level = 1;; ++level) {
         if ((1ULL << level) > static_cast<unsigned long long>(kMaxSafeLinearBlaLength)) break;
@@ -762,22 +650,18 @@ void build_bla(ReferenceContext& ctx, bool retain_builder_orbit) {
         }
         return;
     }
-    const fx::Fe tolerance = fx::fe_from(std::ldexp(1.0, -38), 0);
-    const fx::Fe two = fx::fe_from(2.0, 0);
-    const fx::Fec zero_c = fx::fec_make(fx::fe_zero(), fx::fe_zero());
+    if (device_table_builder()) {
+        build_bla_on_device(ctx, base_count);
+        if (!retain_builder_orbit) {
+            ctx.fast_orbit.clear();
+            ctx.fast_orbit.shrink_to_fit();
+        }
+        return;
+    }
     std::vector<std::vector<BuilderCubic>> levels;
     levels.emplace_back(static_cast<std::size_t>(base_count));
     for (int start = 1; start <= base_count; ++start) {
-        const fx::Fec& ref = ctx.fast_orbit[static_cast<std::size_t>(start)];
-        const fx::Fe radius = fx::fe_mul(tolerance, fx::fe_sqrt(fx::fec_norm2(ref)));
-        BuilderCubic s;
-        for (int k = 0; k < 9; ++k) s.c[k] = zero_c;
-        s.c[0] = fx::fec_scale(ref, two);
-        s.c[1] = fx::fec_make(fx::fe_from(1.0, 0), fx::fe_zero());
-        s.c[2] = fx::fec_make(fx::fe_from(1.0, 0), fx::fe_zero());
-        s.r2 = fx::fe_sqr(radius);
-        s.len = 1;
-        levels[0][static_cast<std::size_t>(start - 1)] = s;
+        levels[0][static_cast<std::size_t>(start - 1)] = cubic_base(ctx.fast_orbit[static_cast<std::size_t>(start)]);
     }
     for (std::size_t level = 1;; ++level) {
         if ((1ULL << level) > static_cast<unsigned long long>(kMaxSafeBlaLength)) break;
@@ -803,21 +687,6 @@ void build_bla(ReferenceContext& ctx, bool retain_builder_orbit) {
         ctx.fast_orbit.clear();
         ctx.fast_orbit.shrink_to_fit();
     }
-}
-
-fx::Fe compact_norm2(const fx::Sc& v) {
-    const fx::Nrm n = fx::sc_norm2(v);
-    return fx::fe_make(n.m, n.e);
-}
-
-// retarget_bla_radius (renderer.cpp:11776-11801).
-fx::Fe retarget_radius(const fx::Fe& x_r2, const fx::Fe& y_r2, const fx::Sc& x_a, const fx::Sc& x_b,
-                       const fx::Fe& input_radius) {
-    const fx::Fe a = fx::fe_sqrt(compact_norm2(x_a));
-    const fx::Fe b = fx::fe_sqrt(compact_norm2(x_b));
-    fx::Fe r = merged_radius(x_r2, y_r2, a, b, input_radius);
-    r = fx::fe_mul(r, 1.0 - std::ldexp(1.0, -40));
-    return fx::fe_sqr(r);
 }
 
 void retarget_cubic(std::vector<std::vector<CubicStep>>& levels, const fx::Fe& input_radius) {
@@ -849,41 +718,6 @@ void retarget_linear(std::vector<std::vector<LinearStep>>& levels, const fx::Fe&
 }
 
 // ------------------------------------------------------ alternate formulas
-fx::Fe alt_matrix_norm(const fx::Fe* c) {
-    fx::Fe sum = fx::fe_zero();
-    for (int k = 0; k < 4; ++k) sum = fx::fe_add(sum, fx::fe_sqr(c[k]));
-    return fx::fe_sqrt(sum);
-}
-
-// merge_alternate_linear_bla (renderer.cpp:11352-11393).
-AltStep merge_alt(const AltStep& y, const AltStep& x, const fx::Fe& input_radius) {
-    using namespace fx;
-    const Fe* yc = y.c;
-    const Fe* xc = x.c;
-    AltStep r{};
-    r.c[0] = fe_add(fe_mul(yc[0], xc[0]), fe_mul(yc[1], xc[2]));
-    r.c[1] = fe_add(fe_mul(yc[0], xc[1]), fe_mul(yc[1], xc[3]));
-    r.c[2] = fe_add(fe_mul(yc[2], xc[0]), fe_mul(yc[3], xc[2]));
-    r.c[3] = fe_add(fe_mul(yc[2], xc[1]), fe_mul(yc[3], xc[3]));
-    r.c[4] = fe_add(fe_add(fe_mul(yc[0], xc[4]), fe_mul(yc[1], xc[6])), yc[4]);
-    r.c[5] = fe_add(fe_add(fe_mul(yc[0], xc[5]), fe_mul(yc[1], xc[7])), yc[5]);
-    r.c[6] = fe_add(fe_add(fe_mul(yc[2], xc[4]), fe_mul(yc[3], xc[6])), yc[6]);
-    r.c[7] = fe_add(fe_add(fe_mul(yc[2], xc[5]), fe_mul(yc[3], xc[7])), yc[7]);
-    const Fe x_state = alt_matrix_norm(xc);
-    const Fe x_param = alt_matrix_norm(xc + 4);
-    Fe radius = merged_radius(x.r2, y.r2, x_state, x_param, input_radius);
-    radius = fe_mul(radius, 1.0 - std::ldexp(1.0, -40));
-    r.r2 = fe_sqr(radius);
-    r.len = x.len + y.len;
-    return r;
-}
-
-fx::Fe alt_reference_radius(const fx::Fec& ref) {
-    const fx::Fe mag = fx::fe_sqrt(fx::fec_norm2(ref));
-    const fx::Fe one = fx::fe_from(1.0, 0);
-    return fx::fe_cmp(mag, one) > 0 ? mag : one;
-}
-
 // build_alternate_linear_bla (renderer.cpp:11414-11526).
 void build_alt_bla(ReferenceContext& ctx, bool retain_builder_orbit) {
     using namespace fx;
@@ -896,52 +730,17 @@ void build_alt_bla(ReferenceContext& ctx, bool retain_builder_orbit) {
     const int last = std::min(ctx.map_end, static_cast<int>(ctx.fast_orbit.size()) - 1);
     const int base_count = last - first;
     if (base_count <= 0) return;
-    const Fe tolerance = fe_from(std::ldexp(1.0, -38), 0);
-    const Fe two = fe_from(2.0, 0);
-    const Fe quarter = fe_from(0.25, 0);
+    if (device_table_builder()) {
+        build_alt_bla_on_device(ctx, first, base_count);
+        if (!retain_builder_orbit) {
+            ctx.fast_orbit.clear();
+            ctx.fast_orbit.shrink_to_fit();
+        }
+        return;
+    }
     auto& base = ctx.alt.emplace_back(static_cast<std::size_t>(base_count));
     for (int k = 0; k < base_count; ++k) {
-        const Fec& ref = ctx.fast_orbit[static_cast<std::size_t>(first + k)];
-        const Fe& re = ref.re;
-        const Fe& im = ref.im;
-        AltStep s{};
-        for (int j = 0; j < 8; ++j) s.c[j] = fe_zero();
-        if (ctx.formula == kFormulaTricorn) {
-            s.c[0] = fe_mul(re, two);
-            s.c[1] = fe_mul(im, -2.0);
-            s.c[2] = fe_mul(im, -2.0);
-            s.c[3] = fe_mul(re, -2.0);
-        } else if (ctx.formula == kFormulaBurningShip) {
-            const Fe ar = fe_abs(re);
-            const Fe ai = fe_abs(im);
-            const double rs = re.m < 0.0 ? -1.0 : 1.0;
-            const double is = im.m < 0.0 ? -1.0 : 1.0;
-            s.c[0] = fe_mul(ar, 2.0 * rs);
-            s.c[1] = fe_mul(ai, -2.0 * is);
-            s.c[2] = fe_mul(ai, 2.0 * rs);
-            s.c[3] = fe_mul(ar, 2.0 * is);
-        } else {
-            s.c[0] = fe_mul(re, two);
-            s.c[1] = fe_mul(im, -2.0);
-            s.c[2] = fe_mul(im, two);
-            s.c[3] = fe_mul(re, two);
-        }
-        if (ctx.formula != kFormulaJulia) {
-            s.c[4] = fe_from(1.0, 0);
-            s.c[7] = fe_from(1.0, 0);
-        }
-        Fe radius = fe_mul(tolerance, alt_reference_radius(ref));
-        if (ctx.formula == kFormulaBurningShip) {
-            if (fe_is_zero(re) || fe_is_zero(im)) {
-                radius = fe_zero();
-            } else {
-                radius = fe_min(radius, fe_mul(fe_abs(re), quarter));
-                radius = fe_min(radius, fe_mul(fe_abs(im), quarter));
-            }
-        }
-        s.r2 = fe_sqr(radius);
-        s.len = 1;
-        base[static_cast<std::size_t>(k)] = s;
+        base[static_cast<std::size_t>(k)] = alt_base(ctx.fast_orbit[static_cast<std::size_t>(first + k)], ctx.formula);
     }
     for (std::size_t level = 1;; ++level) {
         if ((1ULL << level) > static_cast<unsigned long long>(kMaxSafeLinearBlaLength)) break;
@@ -1053,6 +852,11 @@ std::unique_ptr<ReferenceContext> clone_reference_context(const ReferenceContext
     const auto series_started = std::chrono::steady_clock::now();
     build_image_series(*ctx, &source.fast_orbit);
     ctx->series_build_ns = elapsed_ns(series_started);
+    if (source.bla_on_device) {
+        retarget_bla_on_device(*ctx, source);
+        ctx->bla_build_ns = elapsed_ns(bla_started);
+        return ctx;
+    }
     ctx->cubic = source.cubic;
     retarget_cubic(ctx->cubic, ctx->input_radius);
     ctx->linear = source.linear;
@@ -1063,6 +867,13 @@ std::unique_ptr<ReferenceContext> clone_reference_context(const ReferenceContext
     ctx->bla_build_ns = elapsed_ns(bla_started);
     return ctx;
 }
+
+namespace {
+std::atomic<bool> table_builder_on_device{true};
+}
+
+bool device_table_builder() { return table_builder_on_device.load(std::memory_order_relaxed); }
+void set_device_table_builder(bool on_device) { table_builder_on_device.store(on_device, std::memory_order_relaxed); }
 
 void* register_reference(std::unique_ptr<ReferenceContext> context) {
     if (!context) throw Failure{"cannot register an empty reference"};

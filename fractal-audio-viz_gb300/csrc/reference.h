@@ -151,4 +151,12 @@ std::shared_ptr<ReferenceContext> remove_reference(void* handle);
 // Build the per-index records the kernels read (escape-mode specific).
 std::vector<OrbitRec> make_orbit_records(const ReferenceContext& context);
 
+// Where the BLA hierarchies are built: true (default) = on the GPU
+// (bla_build.cu), false = on the host.  Both give identical tables.
+bool device_table_builder();
+void set_device_table_builder(bool on_device);
+void build_bla_on_device(ReferenceContext& ctx, int base_count);
+void build_alt_bla_on_device(ReferenceContext& ctx, int first_index, int base_count);
+void retarget_bla_on_device(ReferenceContext& ctx, const ReferenceContext& source);
+
 }  // namespace fgb

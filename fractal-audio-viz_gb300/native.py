@@ -259,6 +259,7 @@ _ABI = (
 # GB300 extensions (include/fractal_gb300.h).  Absent from the CPU oracles.
 _GB300_ABI = (
     ("fractal_gb300_device_count", ctypes.c_int, ()),
+    ("fractal_gb300_set_table_builder", None, (ctypes.c_int,)),
     ("fractal_gb300_last_kernel_ms", ctypes.c_double, ()),
     ("fractal_gb300_render_reference_device", ctypes.c_int,
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,

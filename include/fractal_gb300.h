@@ -232,6 +232,11 @@ int fractal_colourise_kfp_precise(const float *field, uint8_t *output, int width
  * synchronising; results are ready when the stream reaches them.
  * ------------------------------------------------------------------- */
 
+/* Where reference creation builds the BLA hierarchies: 1 (default) on the
+ * GPU, 0 on the host.  Both builders use the same arithmetic and give
+ * identical tables; the switch exists so tests can compare them. */
+void fractal_gb300_set_table_builder(int on_device);
+
 /* Number of usable CUDA devices (0 when none). */
 int fractal_gb300_device_count(void);
 /* Duration in ms of the last render/colour kernel issued by this thread,

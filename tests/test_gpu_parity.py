@@ -70,3 +70,19 @@ def test_stats_counters_match_reference_fields(product, package):
     # its escape index.
     series_start = stats["series_jumps"] // max(1, stats["series_pixels"])
     assert stats["logical_iterations"] == int((counts - series_start).sum())
+
+
+@pytest.mark.parametrize("name", ["fhd_level33_128x72", "deep_p80_e32_96x54", "deep_p70_e28_linear_96x54",
+                                  "julia_fixed_1_e9_96x54", "burning-ship_e7_96x54", "tricorn_e12_64x36"])
+def test_host_and_gpu_table_builders_agree(product, name):
+    """The BLA hierarchies built on the GPU (default) and on the host use the
+    same arithmetic; renders from either are bit-identical."""
+    case = next(c for c in CASES if c["name"] == name)
+    try:
+        product.fractal_gb300_set_table_builder(0)
+        host = run_case(product, case)
+    finally:
+        product.fractal_gb300_set_table_builder(1)
+    device = run_case(product, case)
+    np.testing.assert_array_equal(host["counts"], device["counts"])
+    np.testing.assert_array_equal(_field_bits(host["field"]), _field_bits(device["field"]))
