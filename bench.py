@@ -118,7 +118,7 @@ class ClockSampler:
 
 
 def algorithmic_flops(stats: dict, series_order: int) -> float:
-    """Flops per unit of work (SURVEY d): exact step 22, linear BLA 14,
+    """Algorithmic flops of the deep render: exact step 22, linear BLA 14,
     cubic BLA 60, image series 8 per term per pixel."""
     return (22.0 * stats["exact_steps"] + 14.0 * stats["linear_blocks"] + 60.0 * stats["cubic_blocks"]
             + 8.0 * series_order * stats["series_pixels"])
@@ -249,15 +249,20 @@ def run_gpu_arm(args) -> int:
     handle = stream.cuda_stream
     assert handle != 0
     forms = {"plain": 0, "chosen": 1 if args.form == "chosen" else 0}
+    targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(n_levels)]
+    direct_levels = [i for i, k in enumerate(stack.keyframes) if k.reference is None]
+    deep_levels = [i for i, k in enumerate(stack.keyframes) if k.reference is not None]
+    # Claim order: the shallow levels with interior (largest per-pixel cost)
+    # first in the direct queue, the deepest levels first in the deep queue.
+    order = direct_levels + deep_levels[::-1]
 
-    def step_device(form):
-        for i, keyframe in enumerate(stack.keyframes):
-            stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), WIDTH, HEIGHT, form=form,
-                                stream=handle)
+    def step_device(form, subset=None, autotune=False):
+        stack.render_batch_device(targets, WIDTH, HEIGHT, form=form, stream=handle, graph=not autotune,
+                                  autotune=autotune, order=subset if subset is not None else order)
 
-    def timed(form, steps, warmup):
+    def timed(form, steps, warmup, subset=None):
         for _ in range(warmup):
-            step_device(form)
+            step_device(form, subset)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -265,7 +270,7 @@ def run_gpu_arm(args) -> int:
         stop = torch.cuda.Event(enable_timing=True)
         start.record(stream)
         for _ in range(steps):
-            step_device(form)
+            step_device(form, subset)
         stop.record(stream)
         torch.cuda.synchronize()
         ms = start.elapsed_time(stop)
@@ -275,12 +280,19 @@ def run_gpu_arm(args) -> int:
             ms = float(t.item())
         return ms
 
+    # Launch shapes tuned once on this batch (schedule only; no pixel changes).
+    step_device(forms["chosen"], autotune=True)
+    shapes = stack.queue_shapes()
+    if forms["chosen"] != 0:
+        step_device(0, autotune=True)
+
     # Work per step (sum of counts) for the chosen form, verified against the
     # plain form (the parity form) on the same views.
     step_device(forms["chosen"])
     torch.cuda.synchronize()
     chosen_counts = counts.clone()
     work = int(counts.to(torch.int64).sum().item())
+    direct_work = int(counts[direct_levels].to(torch.int64).sum().item())
     step_device(0)
     torch.cuda.synchronize()
     plain_work = int(counts.to(torch.int64).sum().item())
@@ -297,21 +309,11 @@ def run_gpu_arm(args) -> int:
     plain_ms = timed(0, max(1, args.steps // 2), 1) if forms["chosen"] != 0 else ms
     plain_value = plain_work * max(1, args.steps // 2) / (plain_ms * 1e-3) / 1e9 if forms["chosen"] != 0 else value
 
-    # Per-launch durations of the dominant (deep render) kernel on the
-    # launching stream, and its algorithmic flops from the device counters.
-    deep = [k for k in stack.keyframes if k.reference is not None]
-    events = []
-    for keyframe in deep:
-        i = stack.keyframes.index(keyframe)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), WIDTH, HEIGHT,
-                            form=forms["chosen"], stream=handle)
-        b.record(stream)
-        events.append((a, b))
-    torch.cuda.synchronize()
-    deep_ms = sum(a.elapsed_time(b) for a, b in events)
+    # Each queue timed alone (same launches, one part of the batch), on the
+    # launching stream.
+    direct_ms = timed(forms["chosen"], 2, 1, subset=direct_levels) / 2
+    deep_ms = timed(forms["chosen"], 2, 1, subset=deep_levels[::-1]) / 2
+    deep = [stack.keyframes[i] for i in deep_levels]
     flops = 0.0
     library.fractal_set_stats_enabled(1)
     for keyframe in deep:
@@ -331,9 +333,10 @@ def run_gpu_arm(args) -> int:
         "traffic": None,
         "peak_source": f"FP{precision} FMA chains measured on this GPU by fractal_gb300_fma_peak "
                        "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
-        "kernel": "deep render (floatexp)" if precision == 32 else "deep render (plain FP64)",
-        "launches": len(deep),
-        "avg_launch_ms": deep_ms / max(1, len(deep)),
+        "kernel": "deep queue (floatexp)" if precision == 32 else "deep render (plain FP64)",
+        "launch_ms": deep_ms,
+        "direct_queue_ms": direct_ms,
+        "direct_pixel_iterations": direct_work,
     }
 
     # End to end through the renderer.h ABI: host output buffers, the field
@@ -383,13 +386,17 @@ def run_gpu_arm(args) -> int:
                 "count_mismatch_vs_plain": mismatch / (n_levels * pixels),
                 "plain_value": plain_value,
                 "reference_setup_s": setup_s,
+                "queue_shapes": {"direct_chunk": shapes[0], "direct_blocks_per_sm": shapes[1],
+                                 "floatexp_chunk": shapes[2], "floatexp_blocks_per_sm": shapes[3]},
+                "launch": "one batched call per step: direct FP64 lane-refill queue (second stream) + "
+                          "floatexp queue, replayed as a CUDA graph",
                 "l2": "outputs larger than L2 (455 MB field + 455 MB counts per step)",
             },
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": n_levels * pixels * 4,
                     "path": "fractal_render_reference_ex / render_fractal_ex into host memory"},
-            "gpu_launches": args.steps * n_levels,
+            "gpu_launches": args.steps * (2 + (1 if forms["chosen"] == 1 else len(deep_levels))),
             "roofline": roofline,
             "cpu_baseline": cpu,
         }

@@ -151,6 +151,42 @@ class KeyframeStack:
         if status != 0:
             raise native.NativeError(native.last_error(self.library))
 
+    def render_batch_device(self, targets, width: int, height: int, *, form: int = 0, series_order: int = 3,
+                            series_block: int = 256, options: Optional[native.RenderOptions] = None,
+                            stream: int = 0, graph: bool = False, autotune: bool = False, order=None,
+                            tiles: int = 0) -> None:
+        """Enqueue every keyframe in one batched call (GB300 extension ABI).
+
+        ``targets`` holds one (field_ptr, counts_ptr) pair per keyframe;
+        ``order`` optionally lists keyframe indices in claim order (costliest
+        first).  Results equal per-keyframe ``render_device`` calls.
+        """
+        options = options or native.RenderOptions()
+        indices = list(order) if order is not None else list(range(len(self.keyframes)))
+        frames = (native.Keyframe * len(indices))()
+        zooms = []
+        for slot, index in enumerate(indices):
+            keyframe = self.keyframes[index]
+            field_ptr, counts_ptr = targets[index]
+            zooms.append(zoom_text(keyframe.log10_zoom))
+            frames[slot].field = field_ptr
+            frames[slot].counts = counts_ptr
+            frames[slot].zoom_text = zooms[-1]
+            frames[slot].reference = keyframe.reference
+            frames[slot].max_iter = keyframe.max_iter
+        flags = (native.BATCH_GRAPH if graph else 0) | (native.BATCH_AUTOTUNE if autotune else 0) | tiles
+        status = self.library.fractal_gb300_render_keyframes_device(
+            frames, len(indices), width, height, self.x.encode("ascii"), self.y.encode("ascii"), series_order,
+            series_block, ctypes.byref(options), form, flags, ctypes.c_void_p(stream))
+        if status != 0:
+            raise native.NativeError(native.last_error(self.library))
+
+    def queue_shapes(self) -> list[int]:
+        values = (ctypes.c_int * 4)()
+        if self.library.fractal_gb300_queue_shapes(values, 4) != 0:
+            raise native.NativeError(native.last_error(self.library))
+        return list(values)
+
     def render_host(self, keyframe: Keyframe, width: int, height: int, *, threads: int = 0,
                     series_order: int = 3, series_block: int = 256, planes: bool = False,
                     options: Optional[native.RenderOptions] = None):

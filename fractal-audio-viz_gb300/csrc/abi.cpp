@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "device.h"
+#include "mlp.h"
 #include "fractal_gb300.h"
 #include "reference.h"
 #include "runtime.h"
@@ -48,6 +49,12 @@ ThreadRuntime::~ThreadRuntime() {
     cudaFree(stamp);
     if (start) cudaEventDestroy(start);
     if (stop) cudaEventDestroy(stop);
+    if (scratch_done) cudaEventDestroy(scratch_done);
+    for (auto& entry : graphs) cudaGraphExecDestroy(entry.second);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
+    if (capture) cudaStreamDestroy(capture);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -68,6 +75,11 @@ ThreadRuntime& thread_runtime() {
         check_cuda(cudaMalloc(&rt.stamp, sizeof(unsigned long long)), "cudaMalloc (stamp)");
         check_cuda(cudaEventCreate(&rt.start), "cudaEventCreate");
         check_cuda(cudaEventCreate(&rt.stop), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&rt.scratch_done, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaStreamCreateWithFlags(&rt.side, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaStreamCreateWithFlags(&rt.capture, cudaStreamNonBlocking), "cudaStreamCreate");
+        check_cuda(cudaEventCreateWithFlags(&rt.fork, cudaEventDisableTiming), "cudaEventCreate");
+        check_cuda(cudaEventCreateWithFlags(&rt.join, cudaEventDisableTiming), "cudaEventCreate");
     }
     return rt;
 }
@@ -75,8 +87,9 @@ ThreadRuntime& thread_runtime() {
 void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes) {
     if (bytes == 0) bytes = 1;
     if (rt.capacity[slot] < bytes) {
-        // The stream may still use the old buffer.
+        // A stream may still use the old buffer.
         check_cuda(cudaStreamSynchronize(rt.stream), "cudaStreamSynchronize");
+        if (rt.scratch_recorded) check_cuda(cudaEventSynchronize(rt.scratch_done), "cudaEventSynchronize");
         cudaFree(rt.scratch[slot]);
         rt.scratch[slot] = nullptr;
         rt.capacity[slot] = 0;
@@ -84,6 +97,19 @@ void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes) {
         rt.capacity[slot] = bytes;
     }
     return rt.scratch[slot];
+}
+
+void wait_scratch(ThreadRuntime& rt, cudaStream_t stream) {
+    if (rt.scratch_recorded && stream != rt.stream) {
+        check_cuda(cudaStreamWaitEvent(stream, rt.scratch_done, 0), "cudaStreamWaitEvent");
+    } else if (rt.scratch_recorded) {
+        check_cuda(cudaStreamWaitEvent(rt.stream, rt.scratch_done, 0), "cudaStreamWaitEvent");
+    }
+}
+
+void release_scratch(ThreadRuntime& rt, cudaStream_t stream) {
+    check_cuda(cudaEventRecord(rt.scratch_done, stream), "cudaEventRecord");
+    rt.scratch_recorded = true;
 }
 
 namespace {
@@ -327,9 +353,13 @@ void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outpu
                "plain alternate-formula kernel launch");
 }
 
-void launch_direct_render(const Outputs& out, int width, int height, long double zoom, long double x_center,
-                          long double y_center, int max_iter, int formula, double julia_re, double julia_im,
-                          const FractalRenderOptions& o, cudaStream_t stream) {
+// Spill-list entries for a direct batch of `pixels` pixels: enough for the
+// long-running pixels of interior-heavy views (a full list only costs speed).
+long long spill_entries(long long pixels) { return std::min<long long>(pixels, 1ll << 20); }
+
+DirectParams make_direct_params(const Outputs& out, int width, int height, long double zoom, long double x_center,
+                                long double y_center, int max_iter, int formula, double julia_re, double julia_im,
+                                const FractalRenderOptions& o) {
     const double zoom_value = static_cast<double>(zoom);
     const double center_re = static_cast<double>(x_center);
     const double center_im = static_cast<double>(y_center);
@@ -341,7 +371,8 @@ void launch_direct_render(const Outputs& out, int width, int height, long double
     if (!std::isfinite(height_span) || !std::isfinite(width_span)) {
         throw Failure{"direct native viewport is outside double range"};
     }
-    DirectParams p{};
+    DirectParams p;
+    std::memset(static_cast<void*>(&p), 0, sizeof p);  // padding too: the bytes key the graph cache
     p.center_re = center_re;
     p.center_im = center_im;
     p.width_span = width_span;
@@ -367,7 +398,18 @@ void launch_direct_render(const Outputs& out, int width, int height, long double
     p.need_phase = (hints & FRACTAL_RENDER_HINT_SKIP_PHASE) == 0;
     p.need_de = (hints & FRACTAL_RENDER_HINT_SKIP_ANALYTIC_DE) == 0;
     p.pixel_spacing = height_span / static_cast<double>(height);
-    check_cuda(launch_direct(p, stream), "direct kernel launch");
+    return p;
+}
+
+void launch_direct_render(const Outputs& out, int width, int height, long double zoom, long double x_center,
+                          long double y_center, int max_iter, int formula, double julia_re, double julia_im,
+                          const FractalRenderOptions& o, cudaStream_t stream) {
+    const DirectParams p = make_direct_params(out, width, height, zoom, x_center, y_center, max_iter, formula,
+                                              julia_re, julia_im, o);
+    ThreadRuntime& rt = thread_runtime();
+    const long long spill = spill_entries(static_cast<long long>(width) * height);
+    void* work = scratch(rt, kScratchDirect, direct_scratch_bytes(&p, 1, spill));
+    check_cuda(launch_direct_batch(&p, 1, work, QueueShape{}, spill, stream), "direct kernel launch");
 }
 
 // Dispatch of a reference render by zoom depth and formula
@@ -398,23 +440,24 @@ void render_from_reference(ReferenceContext& ctx, const Outputs& out, int width,
 // Floatexp form of a reference render.  It covers strict deep Mandelbrot
 // fields (the production atlas path); shallow fields, the other formulas,
 // non-strict cycle detection and time budgets use the plain form.
-void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, int width, int height,
-                                    const char* zoom_text, int max_iter, int series_order, int series_block,
-                                    const FractalRenderOptions& o, ThreadRuntime& rt, cudaStream_t stream) {
+namespace {
+
+// Floatexp kernel parameters of one field, or false when the field is not
+// one the floatexp form covers (shallow, alternate formula, non-strict cycle
+// detection, time budget): those render in the plain form.
+bool make_floatexp_params(ReferenceContext& ctx, const Outputs& out, int width, int height, const char* zoom_text,
+                          int max_iter, int series_order, int series_block, const FractalRenderOptions& o,
+                          FxParams& p) {
     const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx.precision_bits);
     const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
-    if (fe_log10(zoom) < 6.0L || ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) {
-        render_from_reference(ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, false, rt,
-                              stream);
-        return;
-    }
+    if (fe_log10(zoom) < 6.0L || ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) return false;
     std::shared_ptr<DeviceTables> dev = device_tables(ctx);
     floatexp_tables(ctx, *dev);
     const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+    std::memset(static_cast<void*>(&p), 0, sizeof p);  // padding too: the bytes key the graph cache
     const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
     const bool use_deep = fx::fe_cmp(g.current_input_radius, ctx.deep_input_radius) <= 0;
     const bool use_ultra = fx::fe_cmp(g.current_input_radius, fx::fe_mul(ctx.input_radius, 1.0e-40)) <= 0;
-    FxParams p{};
     p.orbit = dev->fx_orbit;
     p.orbit_size = dev->orbit_size;
     p.cubic = dev->fx_cubic;
@@ -448,6 +491,20 @@ void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, i
     p.output_bias = static_cast<float>(o.output_bias);
     p.out = out.field;
     p.counts = out.counts;
+    return true;
+}
+
+}  // namespace
+
+void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, int width, int height,
+                                    const char* zoom_text, int max_iter, int series_order, int series_block,
+                                    const FractalRenderOptions& o, ThreadRuntime& rt, cudaStream_t stream) {
+    FxParams p;
+    if (!make_floatexp_params(ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, p)) {
+        render_from_reference(ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, false, rt,
+                              stream);
+        return;
+    }
     check_cuda(launch_floatexp_mandelbrot(p, stream), "floatexp kernel launch");
 }
 
@@ -457,6 +514,7 @@ namespace {
 void render_to_host(float* output, FractalRenderPlanes* planes, int width, int height,
                     const std::function<void(const Outputs&, bool, ThreadRuntime&, cudaStream_t)>& launch) {
     ThreadRuntime& rt = thread_runtime();
+    wait_scratch(rt, rt.stream);
     const auto started = std::chrono::steady_clock::now();
     const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
     Outputs out;
@@ -813,6 +871,7 @@ int kfp_host(const float* field, uint8_t* output, int width, int height, int max
             throw Failure{"native KFP field bias exceeds iteration cap"};
         }
         ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
         const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
         float* d_field = static_cast<float*>(scratch(rt, kScratchField, pixels * sizeof(float)));
         std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
@@ -834,6 +893,234 @@ int kfp_host(const float* field, uint8_t* output, int width, int height, int max
 }  // namespace fgb
 
 using namespace fgb;
+
+
+// ------------------------------------------------------- keyframe batches
+namespace {
+
+struct BatchShapes {
+    QueueShape direct{64, 8};
+    QueueShape floatexp{256, 0};
+};
+
+std::mutex tuned_mutex;
+std::map<std::string, BatchShapes> tuned_shapes;  // by batch class
+
+// Everything one batch enqueues, resolved on the host first (tables
+// uploaded, zooms parsed) so the enqueue itself can be captured in a graph.
+struct BatchPlan {
+    std::map<int, std::vector<DirectParams>> direct;  // by formula
+    std::vector<FxParams> floatexp;
+    std::vector<float> log_zoom;       // per floatexp field (tile features)
+    unsigned tile_flags = 0;           // FRACTAL_GB300_BATCH_TILES / _LEARNED / _PROBE
+    mlp::CostNet* net = nullptr;
+    int tiles = 0;
+    int feature_rows = 0;
+    std::vector<std::function<void(cudaStream_t)>> plain;
+    std::vector<std::shared_ptr<ReferenceContext>> contexts;
+    std::string key;
+    std::size_t direct_bytes = 0;
+};
+
+template <typename T>
+void append_bytes(std::string& key, const T& value) {
+    key.append(reinterpret_cast<const char*>(&value), sizeof value);
+}
+
+// Tile-mode buffers in one scratch region: per-tile cost, timing, probe,
+// features, predictions, order.
+struct TileBuffers {
+    unsigned long long* cost;
+    unsigned long long* timing;
+    std::uint32_t* probe;
+    __nv_bfloat16* features;
+    float* predicted;
+    unsigned* order;
+    std::size_t bytes;
+};
+
+TileBuffers tile_buffers(char* base, int tiles, int rows) {
+    auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
+    TileBuffers t{};
+    std::size_t at = 0;
+    t.cost = reinterpret_cast<unsigned long long*>(base + at);
+    at += up(sizeof(unsigned long long) * tiles);
+    t.timing = reinterpret_cast<unsigned long long*>(base + at);
+    at += 256;
+    t.probe = reinterpret_cast<std::uint32_t*>(base + at);
+    at += up(sizeof(std::uint32_t) * static_cast<std::size_t>(tiles) * mlp::kProbe);
+    t.features = reinterpret_cast<__nv_bfloat16*>(base + at);
+    at += up(sizeof(__nv_bfloat16) * static_cast<std::size_t>(rows) * mlp::kFeatures);
+    t.predicted = reinterpret_cast<float*>(base + at);
+    at += up(sizeof(float) * rows);
+    t.order = reinterpret_cast<unsigned*>(base + at);
+    at += up(sizeof(unsigned) * tiles);
+    t.bytes = at;
+    return t;
+}
+
+void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime& rt, cudaStream_t main,
+                   void* direct_scratch, unsigned long long* counter) {
+    const bool fork = !plan.direct.empty() && (!plan.floatexp.empty() || !plan.plain.empty());
+    cudaStream_t direct_stream = fork ? rt.side : main;
+    if (fork) {
+        check_cuda(cudaEventRecord(rt.fork, main), "cudaEventRecord (fork)");
+        check_cuda(cudaStreamWaitEvent(rt.side, rt.fork, 0), "cudaStreamWaitEvent (fork)");
+    }
+    for (const auto& group : plan.direct) {
+        const std::vector<DirectParams>& fields = group.second;
+        for (std::size_t i = 0; i < fields.size(); i += kMaxDirectFields) {
+            const int n = static_cast<int>(std::min<std::size_t>(kMaxDirectFields, fields.size() - i));
+            long long pixels = 0;
+            for (int f = 0; f < n; ++f) pixels += static_cast<long long>(fields[i + f].width) * fields[i + f].height;
+            check_cuda(launch_direct_batch(fields.data() + i, n, direct_scratch, shapes.direct, spill_entries(pixels),
+                                           direct_stream),
+                       "direct batch launch");
+        }
+    }
+    if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
+        const TileBuffers t = tile_buffers(static_cast<char*>(scratch(rt, kScratchTiles, 1)), plan.tiles,
+                                           plan.feature_rows);
+        const int n = static_cast<int>(plan.floatexp.size());
+        TileSchedule schedule;
+        schedule.tile_rows = shapes.floatexp.chunk >= 64 && shapes.floatexp.chunk <= 4096
+            ? std::max(1, std::min(64, shapes.floatexp.chunk / 64)) : 8;
+        while (64 % schedule.tile_rows != 0) --schedule.tile_rows;
+        schedule.tile_cost = t.cost;
+        schedule.timing = t.timing;
+        if (plan.tile_flags & (FRACTAL_GB300_BATCH_LEARNED | FRACTAL_GB300_BATCH_PROBE)) {
+            check_cuda(launch_tile_probe(plan.floatexp.data(), plan.log_zoom.data(), n, t.probe, t.features,
+                                         plan.feature_rows, main),
+                       "tile probe launch");
+        }
+        if (plan.tile_flags & FRACTAL_GB300_BATCH_LEARNED) {
+            std::string why;
+            if (!mlp::predict_async(plan.net, t.features, plan.feature_rows, t.predicted, main, why)) {
+                throw Failure{why};
+            }
+            check_cuda(launch_tile_order(t.predicted, plan.tiles, t.order, main), "tile order launch");
+            schedule.order = t.order;
+        }
+        check_cuda(launch_floatexp_tiles(plan.floatexp.data(), plan.log_zoom.data(), n, counter, shapes.floatexp,
+                                         schedule, main),
+                   "floatexp tile queue launch");
+    } else {
+        for (std::size_t i = 0; i < plan.floatexp.size(); i += kMaxFxFields) {
+            const int n = static_cast<int>(std::min<std::size_t>(kMaxFxFields, plan.floatexp.size() - i));
+            check_cuda(launch_floatexp_batch(plan.floatexp.data() + i, n, counter, shapes.floatexp, main),
+                       "floatexp batch launch");
+        }
+    }
+    for (const auto& launch : plan.plain) launch(main);
+    if (fork) {
+        check_cuda(cudaEventRecord(rt.join, rt.side), "cudaEventRecord (join)");
+        check_cuda(cudaStreamWaitEvent(main, rt.join, 0), "cudaStreamWaitEvent (join)");
+    }
+}
+
+void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime& rt, cudaStream_t stream,
+                 bool graph) {
+    void* direct_scratch = plan.direct.empty() ? nullptr : scratch(rt, kScratchDirect, plan.direct_bytes);
+    auto* counter = static_cast<unsigned long long*>(scratch(rt, kScratchQueue, 256));
+    if (!graph) {
+        enqueue_batch(plan, shapes, rt, stream, direct_scratch, counter);
+        return;
+    }
+    std::string key = plan.key;
+    append_bytes(key, shapes);
+    append_bytes(key, direct_scratch);
+    append_bytes(key, counter);
+    auto found = rt.graphs.find(key);
+    if (found == rt.graphs.end()) {
+        if (rt.graphs.size() >= 16) {
+            check_cuda(cudaDeviceSynchronize(), "cudaDeviceSynchronize (graph cache)");
+            for (auto& entry : rt.graphs) cudaGraphExecDestroy(entry.second);
+            rt.graphs.clear();
+        }
+        check_cuda(cudaStreamBeginCapture(rt.capture, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+        try {
+            enqueue_batch(plan, shapes, rt, rt.capture, direct_scratch, counter);
+        } catch (...) {
+            cudaGraph_t broken = nullptr;
+            cudaStreamEndCapture(rt.capture, &broken);
+            if (broken) cudaGraphDestroy(broken);
+            throw;
+        }
+        cudaGraph_t g = nullptr;
+        check_cuda(cudaStreamEndCapture(rt.capture, &g), "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t made = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        check_cuda(made, "cudaGraphInstantiate");
+        found = rt.graphs.emplace(key, exec).first;
+    }
+    check_cuda(cudaGraphLaunch(found->second, stream), "cudaGraphLaunch");
+}
+
+// Coordinate descent over the launch shapes, each candidate timed once with
+// CUDA events on the batch itself.  Shapes change only the schedule, never a
+// pixel: every candidate renders the same values.
+BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stream) {
+    BatchShapes best;
+    void* direct_scratch = plan.direct.empty() ? nullptr : scratch(rt, kScratchDirect, plan.direct_bytes);
+    auto* counter = static_cast<unsigned long long*>(scratch(rt, kScratchQueue, 256));
+    cudaEvent_t a = nullptr, b = nullptr;
+    check_cuda(cudaEventCreate(&a), "cudaEventCreate");
+    check_cuda(cudaEventCreate(&b), "cudaEventCreate");
+    auto time = [&](const BatchShapes& shapes) {
+        float runs[3];
+        for (float& ms : runs) {
+            check_cuda(cudaEventRecord(a, stream), "cudaEventRecord");
+            enqueue_batch(plan, shapes, rt, stream, direct_scratch, counter);
+            check_cuda(cudaEventRecord(b, stream), "cudaEventRecord");
+            check_cuda(cudaEventSynchronize(b), "cudaEventSynchronize");
+            check_cuda(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+        }
+        std::sort(runs, runs + 3);
+        return runs[1];
+    };
+    try {
+        time(best);  // warm-up (occupancy queries, caches)
+        float best_ms = time(best);
+        const int direct_chunks[] = {32, 64, 128, 256};
+        const int direct_blocks[] = {2, 4, 8, 12, 0};
+        const int fx_chunks[] = {64, 128, 256, 512, 1024};
+        const int fx_blocks[] = {4, 6, 8, 0};
+        for (int pass = 0; pass < 2; ++pass) {
+            auto sweep = [&](int* knob, const int* values, int count) {
+                const int keep = *knob;
+                int chosen = keep;
+                for (int i = 0; i < count; ++i) {
+                    if (values[i] == keep) continue;
+                    *knob = values[i];
+                    const float ms = time(best);
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        chosen = values[i];
+                    }
+                }
+                *knob = chosen;
+            };
+            if (!plan.direct.empty()) {
+                sweep(&best.direct.chunk, direct_chunks, 4);
+                sweep(&best.direct.blocks_per_sm, direct_blocks, 5);
+            }
+            if (!plan.floatexp.empty()) {
+                sweep(&best.floatexp.chunk, fx_chunks, 5);
+                sweep(&best.floatexp.blocks_per_sm, fx_blocks, 4);
+            }
+        }
+    } catch (...) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return best;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1084,6 +1371,7 @@ int fractal_colourise(const float* field, uint8_t* output, int width, int height
             throw Failure{"invalid native colour dimensions or palette"};
         }
         ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
         const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
         int lut_size = 0;
         const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size);
@@ -1131,9 +1419,11 @@ int fractal_gb300_colourise_kfp_device(const float* field, uint8_t* rgb, int wid
         }
         ThreadRuntime& rt = thread_runtime();
         cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        wait_scratch(rt, rt.stream);
         const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true);
         check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
         kfp_colour(field, rgb, width, height, max_iter, *options, in, lut_size, rt, stream);
+        release_scratch(rt, stream);
     });
 }
 
@@ -1178,6 +1468,7 @@ int fractal_gb300_render_reference_device(float* field, uint32_t* counts, int wi
         Outputs out;
         out.field = field;
         out.counts = counts;
+        wait_scratch(rt, stream);
         if (form == 1) {
             render_floatexp_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block,
                                            o, rt, stream);
@@ -1185,6 +1476,7 @@ int fractal_gb300_render_reference_device(float* field, uint32_t* counts, int wi
             render_from_reference(*ctx, out, width, height, zoom_text, max_iter, series_order, series_block, o, false,
                                   rt, stream);
         }
+        release_scratch(rt, stream);
     });
 }
 
@@ -1205,9 +1497,11 @@ int fractal_gb300_render_direct_device(float* field, uint32_t* counts, int width
         Outputs out;
         out.field = field;
         out.counts = counts;
+        wait_scratch(rt, stream);
         launch_direct_render(out, width, height, parse_zoom_direct(zoom_text), parse_coordinate(x_center, "real"),
                              parse_coordinate(y_center, "imaginary"), max_iter, formula, julia_real, julia_imag, o,
                              stream);
+        release_scratch(rt, stream);
     });
 }
 
@@ -1222,10 +1516,313 @@ int fractal_gb300_colourise_device(const float* field, uint8_t* rgb, int width, 
         ThreadRuntime& rt = thread_runtime();
         cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
         int lut_size = 0;
+        wait_scratch(rt, rt.stream);
         const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size);
         const float scale = static_cast<float>(lut_size - 1) / static_cast<float>(max_iter);
+        check_cuda(cudaStreamSynchronize(rt.stream), "aurora palette");
         check_cuda(launch_aurora(field, rgb, static_cast<long long>(width) * height, lut, lut_size, scale, max_iter,
                                  stream), "aurora kernel launch");
+        release_scratch(rt, stream);
+    });
+}
+
+int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, int count, int width, int height,
+                                          const char* x_center, const char* y_center, int series_order,
+                                          int series_block, const FractalRenderOptions* supplied, int form,
+                                          unsigned flags, void* stream_handle) {
+    return guarded("keyframe batch render failed with an unknown exception", [&] {
+        if (!frames || count <= 0 || !valid_dims(width, height) || !valid_series(series_order, series_block)
+            || (form != 0 && form != 1)) {
+            throw Failure{"invalid native keyframe batch"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        BatchPlan plan;
+        append_bytes(plan.key, width);
+        append_bytes(plan.key, height);
+        append_bytes(plan.key, form);
+        std::size_t direct_doubles = 0;
+        bool centre_parsed = false;
+        long double cx = 0.0L, cy = 0.0L;
+        for (int i = 0; i < count; ++i) {
+            const FractalGb300Keyframe& frame = frames[i];
+            if (!frame.field || !frame.zoom_text || !valid_iterations(frame.max_iter)) {
+                throw Failure{"invalid native keyframe " + std::to_string(i)};
+            }
+            Outputs out;
+            out.field = frame.field;
+            out.counts = frame.counts;
+            if (!frame.reference) {
+                if (!centre_parsed) {
+                    if (!x_center || !y_center) throw Failure{"keyframe batch without a centre for direct frames"};
+                    cx = parse_coordinate(x_center, "real");
+                    cy = parse_coordinate(y_center, "imaginary");
+                    centre_parsed = true;
+                }
+                plan.direct[kFormulaMandelbrot].push_back(make_direct_params(
+                    out, width, height, parse_zoom_direct(frame.zoom_text), cx, cy, frame.max_iter,
+                    kFormulaMandelbrot, 0.0, 0.0, o));
+                direct_doubles += static_cast<std::size_t>(width) + height;
+                append_bytes(plan.key, plan.direct[kFormulaMandelbrot].back());
+                continue;
+            }
+            std::shared_ptr<ReferenceContext> ctx = acquire_reference(frame.reference);
+            if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
+            if (ctx->escape_mode != o.escape_radius_mode) {
+                throw Failure{"reference escape-radius mode does not match render options"};
+            }
+            if (frame.max_iter > ctx->requested_max_iter) {
+                throw Failure{"render iteration count exceeds prepared reference"};
+            }
+            plan.contexts.push_back(ctx);
+            FxParams fx;
+            if (form == 1 && make_floatexp_params(*ctx, out, width, height, frame.zoom_text, frame.max_iter,
+                                                  series_order, series_block, o, fx)) {
+                plan.floatexp.push_back(fx);
+                plan.log_zoom.push_back(static_cast<float>(fe_log10(parse_zoom_fe(frame.zoom_text,
+                                                                                  ctx->precision_bits))));
+                append_bytes(plan.key, fx);
+                continue;
+            }
+            const fx::Fe zoom = parse_zoom_fe(frame.zoom_text, ctx->precision_bits);
+            if (fe_log10(zoom) < 6.0L) {
+                plan.direct[ctx->formula].push_back(make_direct_params(
+                    out, width, height, parse_zoom_direct(frame.zoom_text), ctx->x_center, ctx->y_center,
+                    frame.max_iter, ctx->formula, ctx->julia_re, ctx->julia_im, o));
+                direct_doubles += static_cast<std::size_t>(width) + height;
+                append_bytes(plan.key, plan.direct[ctx->formula].back());
+                continue;
+            }
+            std::shared_ptr<DeviceTables> dev = device_tables(*ctx);
+            ReferenceContext* raw = ctx.get();
+            const int max_iter = frame.max_iter;
+            plan.plain.push_back([raw, dev, out, width, height, zoom, max_iter, series_order, series_block, o,
+                                  &rt](cudaStream_t s) {
+                if (raw->formula != kFormulaMandelbrot) {
+                    launch_deep_alternate(*raw, *dev, out, width, height, zoom, max_iter, o, false, rt, s);
+                } else {
+                    launch_deep_mandelbrot(*raw, *dev, out, width, height, zoom, max_iter, series_order,
+                                           series_block, o, false, rt, s);
+                }
+            });
+            append_bytes(plan.key, raw);
+            append_bytes(plan.key, raw->generation);
+            append_bytes(plan.key, out);
+            append_bytes(plan.key, zoom);
+            append_bytes(plan.key, max_iter);
+            append_bytes(plan.key, series_order);
+            append_bytes(plan.key, series_block);
+            append_bytes(plan.key, o);
+        }
+        for (const auto& group : plan.direct) {
+            const std::vector<DirectParams>& fields = group.second;
+            for (std::size_t i = 0; i < fields.size(); i += kMaxDirectFields) {
+                const int n = static_cast<int>(std::min<std::size_t>(kMaxDirectFields, fields.size() - i));
+                long long pixels = 0;
+                for (int f = 0; f < n; ++f) pixels += static_cast<long long>(fields[i + f].width) * fields[i + f].height;
+                plan.direct_bytes = std::max(plan.direct_bytes,
+                                             direct_scratch_bytes(fields.data() + i, n, spill_entries(pixels)));
+            }
+        }
+        plan.tile_flags = flags & (FRACTAL_GB300_BATCH_TILES | FRACTAL_GB300_BATCH_LEARNED | FRACTAL_GB300_BATCH_PROBE);
+        if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
+            if (plan.floatexp.size() > static_cast<std::size_t>(kMaxFxFields)) {
+                throw Failure{"tile-scheduled batches take at most 64 floatexp keyframes"};
+            }
+            plan.tiles = batch_tiles(plan.floatexp.data(), static_cast<int>(plan.floatexp.size()));
+            plan.feature_rows = (plan.tiles + 127) / 128 * 128;
+            if (plan.tile_flags & FRACTAL_GB300_BATCH_LEARNED) {
+                if (!rt.costnet) throw Failure{"learned tile order requested but no cost network is attached"};
+                plan.net = static_cast<mlp::CostNet*>(rt.costnet);
+                std::string why;
+                if (!mlp::reserve_rows(plan.net, plan.feature_rows, why)) throw Failure{why};
+                append_bytes(plan.key, plan.net);
+            }
+            scratch(rt, kScratchTiles, tile_buffers(nullptr, plan.tiles, plan.feature_rows).bytes);
+            append_bytes(plan.key, plan.tile_flags);
+            rt.tile_stream = stream;
+            rt.last_tiles = plan.tiles;
+        }
+        std::string shape_key;
+        append_bytes(shape_key, plan.tile_flags);
+        append_bytes(shape_key, width);
+        append_bytes(shape_key, height);
+        append_bytes(shape_key, form);
+        append_bytes(shape_key, static_cast<int>(plan.floatexp.size()));
+        append_bytes(shape_key, static_cast<int>(plan.plain.size()));
+        append_bytes(shape_key, static_cast<int>(direct_doubles));
+        BatchShapes shapes;
+        {
+            std::lock_guard<std::mutex> lock(tuned_mutex);
+            auto known = tuned_shapes.find(shape_key);
+            if (known != tuned_shapes.end()) shapes = known->second;
+        }
+        if (rt.shapes_pinned) {
+            if (rt.pinned_shapes[0] > 0) shapes.direct.chunk = rt.pinned_shapes[0];
+            shapes.direct.blocks_per_sm = rt.pinned_shapes[1];
+            if (rt.pinned_shapes[2] > 0) shapes.floatexp.chunk = rt.pinned_shapes[2];
+            shapes.floatexp.blocks_per_sm = rt.pinned_shapes[3];
+        }
+        wait_scratch(rt, stream);
+        if ((flags & FRACTAL_GB300_BATCH_AUTOTUNE) && !rt.shapes_pinned) {
+            shapes = autotune(plan, rt, stream);
+            std::lock_guard<std::mutex> lock(tuned_mutex);
+            tuned_shapes[shape_key] = shapes;
+        }
+        rt.last_shapes[0] = shapes.direct.chunk;
+        rt.last_shapes[1] = shapes.direct.blocks_per_sm;
+        rt.last_shapes[2] = shapes.floatexp.chunk;
+        rt.last_shapes[3] = shapes.floatexp.blocks_per_sm;
+        launch_plan(plan, shapes, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
+        release_scratch(rt, stream);
+    });
+}
+
+int fractal_gb300_set_queue_shapes(const int* values, int count) {
+    return guarded("queue shape setting failed", [&] {
+        ThreadRuntime& rt = thread_runtime();
+        if (!values || count <= 0) {
+            rt.shapes_pinned = false;
+            return;
+        }
+        if (count < 4) throw Failure{"queue shapes need four values"};
+        for (int i = 0; i < 4; ++i) {
+            if (values[i] < 0 || values[i] > (i % 2 == 0 ? 1 << 20 : 64)) throw Failure{"queue shape out of range"};
+            rt.pinned_shapes[i] = values[i];
+        }
+        rt.shapes_pinned = true;
+    });
+}
+
+int fractal_gb300_set_cost_network(void* net) {
+    return guarded("attaching the cost network failed", [&] { thread_runtime().costnet = net; });
+}
+
+int fractal_gb300_last_tiles(int* tiles, float* cost, uint16_t* features, int capacity, double* timing_ms) {
+    return guarded("reading the last tile schedule failed", [&] {
+        ThreadRuntime& rt = thread_runtime();
+        if (rt.last_tiles <= 0) throw Failure{"no tile-scheduled batch has run on this thread"};
+        if (tiles) *tiles = rt.last_tiles;
+        if ((cost || features) && capacity < rt.last_tiles) throw Failure{"tile buffer too small"};
+        check_cuda(cudaStreamSynchronize(rt.tile_stream ? rt.tile_stream : rt.stream), "tile batch");
+        const int rows = (rt.last_tiles + 127) / 128 * 128;
+        const TileBuffers t = tile_buffers(static_cast<char*>(scratch(rt, kScratchTiles, 1)), rt.last_tiles, rows);
+        if (cost) {
+            std::vector<unsigned long long> cycles(rt.last_tiles);
+            check_cuda(cudaMemcpy(cycles.data(), t.cost, cycles.size() * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost), "tile costs");
+            for (int i = 0; i < rt.last_tiles; ++i) cost[i] = static_cast<float>(cycles[i]);
+        }
+        if (features) {
+            check_cuda(cudaMemcpy(features, t.features,
+                                  sizeof(std::uint16_t) * static_cast<std::size_t>(rt.last_tiles) * mlp::kFeatures,
+                                  cudaMemcpyDeviceToHost), "tile features");
+        }
+        if (timing_ms) {
+            unsigned long long ns[3];
+            check_cuda(cudaMemcpy(ns, t.timing, sizeof ns, cudaMemcpyDeviceToHost), "tile timing");
+            timing_ms[0] = static_cast<double>(ns[2] - ns[0]) * 1e-6;
+            timing_ms[1] = static_cast<double>(ns[2] - ns[1]) * 1e-6;
+        }
+    });
+}
+
+int fractal_gb300_queue_shapes(int* values, int capacity) {
+    return guarded("queue shape query failed", [&] {
+        if (!values || capacity < 4) throw Failure{"queue shape buffer too small"};
+        ThreadRuntime& rt = thread_runtime();
+        for (int i = 0; i < 4; ++i) values[i] = rt.last_shapes[i];
+    });
+}
+
+// ------------------------------------------------------ tile-cost network
+
+void* fractal_gb300_costnet_create(unsigned seed) {
+    return guarded_handle("cost network creation failed", [&]() -> void* {
+        thread_runtime();
+        std::string why;
+        mlp::CostNet* net = mlp::create(seed, why);
+        if (!net) throw Failure{why};
+        return net;
+    });
+}
+
+void fractal_gb300_costnet_destroy(void* net) { mlp::destroy(static_cast<mlp::CostNet*>(net)); }
+
+int fractal_gb300_costnet_parameter_count(void) { return static_cast<int>(mlp::parameter_count()); }
+
+int fractal_gb300_costnet_parameters(void* net, float* values, int count, int write) {
+    return guarded("cost network parameter access failed", [&] {
+        if (!net || !values || count != static_cast<int>(mlp::parameter_count())) {
+            throw Failure{"cost network parameter buffer must hold exactly the parameter count"};
+        }
+        std::string why;
+        auto* n = static_cast<mlp::CostNet*>(net);
+        if (write) {
+            if (!mlp::set_parameters(n, values, static_cast<std::size_t>(count), why)) throw Failure{why};
+        } else {
+            std::vector<float> host;
+            if (!mlp::get_parameters(n, host, why)) throw Failure{why};
+            std::memcpy(values, host.data(), host.size() * sizeof(float));
+        }
+    });
+}
+
+int fractal_gb300_costnet_train_step(void* net, const void* features, const float* targets, int batch,
+                                     float learning_rate, int update, float* loss, float* gradients,
+                                     void* stream_handle) {
+    return guarded("cost network training step failed", [&] {
+        if (!net || !features || !targets) throw Failure{"invalid cost network training arguments"};
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        std::string why;
+        std::vector<float> grads;
+        float host_loss = 0.0f;
+        if (!mlp::train_step(static_cast<mlp::CostNet*>(net), static_cast<const __nv_bfloat16*>(features), targets,
+                             batch, learning_rate, update != 0, &host_loss, gradients ? &grads : nullptr, stream,
+                             why)) {
+            throw Failure{why};
+        }
+        if (loss) *loss = host_loss;
+        if (gradients) std::memcpy(gradients, grads.data(), grads.size() * sizeof(float));
+    });
+}
+
+int fractal_gb300_costnet_predict(void* net, const void* features, int rows, float* out, void* stream_handle) {
+    return guarded("cost network prediction failed", [&] {
+        if (!net || !features || !out) throw Failure{"invalid cost network prediction arguments"};
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        std::string why;
+        if (!mlp::predict(static_cast<mlp::CostNet*>(net), static_cast<const __nv_bfloat16*>(features), rows, out,
+                          stream, why)) {
+            throw Failure{why};
+        }
+    });
+}
+
+int fractal_gb300_gemm_bf16(const void* a, const void* b, float* c, int m, int n, int k, int b_rows,
+                            void* stream_handle) {
+    return guarded("tensor-core GEMM failed", [&] {
+        if (!a || !b || !c) throw Failure{"invalid GEMM arguments"};
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        int* error = static_cast<int*>(scratch(rt, kScratchWork, 256));
+        check_cuda(cudaMemsetAsync(error, 0, sizeof(int), stream), "cudaMemsetAsync");
+        mlp::Epilogue e;
+        std::memset(&e, 0, sizeof e);
+        e.out_f32 = c;
+        e.ld_out = n;
+        e.rows = m;
+        e.cols = n;
+        std::string why;
+        if (!mlp::gemm(mlp::GemmShape{a, b, m, n, k, b_rows}, e, error, stream, why)) throw Failure{why};
+        int flag = 0;
+        check_cuda(cudaMemcpyAsync(&flag, error, sizeof flag, cudaMemcpyDeviceToHost, stream), "GEMM status");
+        check_cuda(cudaStreamSynchronize(stream), "GEMM");
+        if (flag) throw Failure{"tensor-core GEMM gave up waiting on its barrier"};
     });
 }
 

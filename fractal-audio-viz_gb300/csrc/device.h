@@ -12,7 +12,9 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <string>
 
 #include "fractal_gb300.h"
 #include "floatexp32.h"
@@ -256,6 +258,58 @@ struct FxParams {
 
 cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stream);
 
+// Launch shape of a persistent queue kernel: pixels per warp claim and
+// resident blocks per SM (0 = as many as fit).
+struct QueueShape {
+    int chunk = 0;
+    int blocks_per_sm = 0;
+};
+
+constexpr int kMaxFxFields = 64;
+constexpr int kTileSide = 64;      // scheduling tile (pixels per side)
+constexpr int kProbeStride = 4;    // coarse probe: every 4th pixel each way
+struct FxBatch {
+    FxParams field[kMaxFxFields];
+    long long first[kMaxFxFields + 1];
+    int tiles_first[kMaxFxFields + 1];  // 64x64-tile prefix over the batch
+    int tiles_x[kMaxFxFields];
+    float log_zoom[kMaxFxFields];       // log10 zoom of each field (tile features)
+    int count;
+    int chunk;
+    unsigned long long* counter;
+    // Tile mode (tile_rows > 0): a work unit is a band of tile_rows rows of
+    // one tile; tiles are claimed in `order` (tile ids; nullptr = ascending),
+    // per-tile warp time is accumulated in tile_cost (SM cycles; optional)
+    // and timing[] gets {first claim, last claim, last finish} (%globaltimer
+    // ns; optional).
+    int tile_rows;
+    const unsigned* order;
+    unsigned long long* tile_cost;
+    unsigned long long* timing;
+};
+// Many floatexp fields in one persistent launch (counter: 8 bytes of device
+// memory, zeroed on the stream before the kernel).
+cudaError_t launch_floatexp_batch(const FxParams* fields, int count, unsigned long long* counter,
+                                  const QueueShape& shape, cudaStream_t stream);
+
+// Tile scheduling of a floatexp batch (64x64 tiles of every field).
+struct TileSchedule {
+    int tile_rows = 8;                   // rows per work unit (divides 64)
+    const unsigned* order = nullptr;     // claim order (nullptr = ascending tile id)
+    unsigned long long* tile_cost = nullptr;
+    unsigned long long* timing = nullptr;
+};
+int batch_tiles(const FxParams* fields, int count);
+cudaError_t launch_floatexp_tiles(const FxParams* fields, const float* log_zoom, int count,
+                                  unsigned long long* counter, const QueueShape& shape, const TileSchedule& schedule,
+                                  cudaStream_t stream);
+// Coarse probe (16x16 samples per tile, iteration counts) and the network's
+// BF16 features (rows padded to a multiple of 128 with zero rows).
+cudaError_t launch_tile_probe(const FxParams* fields, const float* log_zoom, int count, std::uint32_t* probe,
+                              __nv_bfloat16* features, int feature_rows, cudaStream_t stream);
+// Heaviest-first claim order from predicted (normalised log) tile costs.
+cudaError_t launch_tile_order(const float* predicted, int tiles, unsigned* order, cudaStream_t stream);
+
 struct ThreadRuntime;
 // Floatexp (FP32 mantissa / int32 exponent) form of a reference render.
 void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, int width, int height,
@@ -266,7 +320,41 @@ void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, i
 cudaError_t launch_plain_mandelbrot(const PlainParams& params, bool planes, bool stats, cudaStream_t stream);
 cudaError_t launch_plain_alternate(const AltParams& params, bool planes, bool stats,
                                    cudaStream_t stream);
-cudaError_t launch_direct(const DirectParams& params, cudaStream_t stream);
+// A batch of direct fields (one kernel over all of them); the batch struct
+// travels as a __grid_constant__ kernel parameter.
+constexpr int kMaxDirectFields = 64;
+// A pixel that ran past its phase's iteration budget, parked with its whole
+// state so a later phase resumes it bit for bit.
+struct DirectSpill {
+    double zr, zi, dr, di, test1, test2;
+    unsigned long long saved_r, saved_i;
+    int it, check_at, field, local;
+};
+constexpr int kDirectPhases = 4;
+struct DirectBatch {
+    DirectParams field[kMaxDirectFields];
+    long long first[kMaxDirectFields + 1];  // pixel prefix over the batch
+    int coord_offset[kMaxDirectFields];     // cx then cy table of each field
+    int interior_test[kMaxDirectFields];    // cardioid/bulb culling needed
+    int count;
+    int chunk;                              // pixels per warp claim
+    double* coords;
+    unsigned long long* counter;            // kDirectPhases claim counters, then kDirectPhases spill counts
+    // Phase p claims fresh pixels (p = 0) or the spills of phase p-1, runs
+    // each for at most `budget` more steps (0 = to the cap) and spills the
+    // rest into `spill_out` (capacity entries; when full the lane goes on).
+    int phase;
+    int budget;
+    const DirectSpill* spill_in;
+    long long spill_in_capacity;
+    DirectSpill* spill_out;
+    long long spill_capacity;
+};
+// Device scratch for one batch: counters, coordinate tables and two spill
+// lists of `spill_entries` each (0: one phase, no spilling).
+std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries);
+cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
+                                long long spill_entries, cudaStream_t stream);
 // Records %globaltimer into *slot (the time-budget origin of the next kernel).
 cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream);
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels,

@@ -1,4 +1,5 @@
-// Direct (shallow) field render in plain double, one thread per pixel.
+// Direct (shallow) field render in plain double: a persistent lane-refill
+// queue over a batch of fields.
 //
 // Restates render_direct_scalar_formula and render_direct_with_planes_formula
 // (renderer.cpp:10054-10135, 10281-10438): cardioid/bulb culling for the
@@ -68,116 +69,518 @@ __device__ bool direct_de(double zr, double zi, double dr, double di, const Fe& 
     return is_finite(out_re) && is_finite(out_im);
 }
 
-template <int Formula, bool Planes>
-__global__ void __launch_bounds__(128) direct_kernel(const DirectParams p) {
-    const long long pixels = static_cast<long long>(p.width) * p.height;
-    const long long index = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (index >= pixels) return;
-    const int py = static_cast<int>(index / p.width);
-    const int px = static_cast<int>(index - static_cast<long long>(py) * p.width);
-    // Pixel coordinates (renderer.cpp:10185-10196): centre + offset * span / size.
-    const double x_origin = p.coordinate_mode == 1 ? static_cast<double>(p.width / 2)
-                                                   : static_cast<double>(p.width - 1) / 2.0;
-    const double y_origin = p.coordinate_mode == 1 ? static_cast<double>(p.height / 2)
-                                                   : static_cast<double>(p.height - 1) / 2.0;
-    const double x_offset = (static_cast<double>(px) - x_origin) * p.width_span / static_cast<double>(p.width);
-    const double y_offset = -(static_cast<double>(py) - y_origin) * p.height_span / static_cast<double>(p.height);
-    const double cx = p.center_re + x_offset;
-    const double cy = p.center_im + y_offset;
-    const float inside = static_cast<float>(static_cast<double>(p.max_iter) - p.output_bias);
-    auto mark_inside = [&] {
-        p.out[index] = inside;
-        if (p.counts) p.counts[index] = static_cast<std::uint32_t>(p.max_iter);
-        if constexpr (Planes) {
-            p.p_iter[index] = p.max_iter;
-            p.p_phase[index] = 0.0;
-            p.p_dex[index] = 0.0;
-            p.p_dey[index] = 0.0;
-            p.p_t1[index] = 0.0;
-            p.p_t2[index] = 0.0;
-        }
-    };
-    if constexpr (Formula == kFormulaMandelbrot) {
-        const double q = (cx - 0.25) * (cx - 0.25) + cy * cy;
-        const bool cardioid = q * (q + cx - 0.25) <= 0.25 * cy * cy;
-        const bool bulb = (cx + 1.0) * (cx + 1.0) + cy * cy <= 0.0625;
-        if (cardioid || bulb) {
-            mark_inside();
-            return;
-        }
+// 2 a b for doubles a, b, formed as the product a*b with its exponent raised
+// by one.  That equals the reference's (2 a) b bit for bit when a*b lies in
+// the normal range away from its lowest binade (rounding commutes with the
+// exact doubling there) and below the overflow binade; an exactly zero
+// operand gives the signed zero of the product.  Everything else (underflow,
+// subnormal, huge, infinite, NaN) returns false and the caller multiplies.
+__device__ __forceinline__ bool twice_product(double a, double b, double& out) {
+    const double product = a * b;
+    const long long bits = __double_as_longlong(product);
+    const unsigned biased = static_cast<unsigned>((bits >> 52) & 0x7ff);
+    if (biased - 2u < 2044u) {
+        out = __longlong_as_double(bits + (1ll << 52));
+        return true;
     }
-    constexpr bool julia = Formula == kFormulaJulia;
-    constexpr bool has_de = Formula == kFormulaMandelbrot || Formula == kFormulaJulia;
-    double zr = julia ? cx : 0.0;
-    double zi = julia ? cy : 0.0;
-    const double pr = julia ? p.julia_re : cx;
-    const double pi = julia ? p.julia_im : cy;
-    double dr = julia ? 1.0 : 0.0;
-    double di = 0.0;
-    const double add_re = julia ? 0.0 : 1.0;
-    double test1 = 0.0, test2 = 0.0;
-    const double escape2 = escape_r2_d(p.escape_mode);
-    const double safe2 = escape2 + 1.0e-7;
-    const bool track_de = Planes && has_de && p.need_de;
-    for (int iteration = 0; iteration < p.max_iter; ++iteration) {
-        if (track_de) {
-            // d' = 2 z d + 1 (parameter plane) or 2 z d (Julia), on the
-            // pre-step z (renderer.cpp:336-338).
-            const double ndr = 2.0 * zr * dr - 2.0 * zi * di + add_re;
-            const double ndi = 2.0 * zr * di + 2.0 * zi * dr + 0.0;
-            dr = ndr;
-            di = ndi;
-        }
-        double nr, ni;
-        step<Formula>(zr, zi, pr, pi, nr, ni);
-        zr = nr;
-        zi = ni;
-        const double m2 = zr * zr + zi * zi;
-        if constexpr (Planes) {
-            test2 = test1;
-            test1 = m2;
-        }
-        if (m2 > escape2 || !is_finite(m2)) {
-            const double safe = is_finite(m2) ? dmax(m2, safe2) : 1.7976931348623157e308;
-            const double magnitude = sqrt(safe);
-            p.out[index] = static_cast<float>(
-                (static_cast<double>(iteration + 1) - log(log(magnitude)) / kLogTwoD) - p.output_bias);
-            if (p.counts) p.counts[index] = static_cast<std::uint32_t>(iteration + 1);
-            if constexpr (Planes) {
-                p.p_iter[index] = iteration;
-                double phase = 0.0;
-                if (p.need_phase && is_finite(zr) && is_finite(zi)) {
-                    phase = atan2(zi, zr) / kTwoPi;
-                    phase -= floor(phase);
-                }
-                p.p_phase[index] = phase;
-                double de_re = 0.0, de_im = 0.0;
-                if (track_de && is_finite(zr) && is_finite(zi) && is_finite(dr) && is_finite(di)) {
-                    if (!direct_de(zr, zi, dr, di, fe_from(p.pixel_spacing, 0), de_re, de_im)) {
-                        de_re = 0.0;
-                        de_im = 0.0;
-                    }
-                }
-                p.p_dex[index] = de_re;
-                p.p_dey[index] = de_im;
-                p.p_t1[index] = test1;
-                p.p_t2[index] = test2;
-            }
-            return;
-        }
-    }
-    mark_inside();
+    out = product;
+    const unsigned long long magnitude = 0x7fffffffffffffffull;
+    return (static_cast<unsigned long long>(__double_as_longlong(a)) & magnitude) == 0
+        || (static_cast<unsigned long long>(__double_as_longlong(b)) & magnitude) == 0;
+}
+
+__device__ __forceinline__ unsigned long long dbits(double v) {
+    return static_cast<unsigned long long>(__double_as_longlong(v));
+}
+
+// Per-lane state of one pixel in flight.
+struct Lane {
+    double zr, zi;      // z_n
+    double rs, is;      // zr*zr, zi*zi of z_n (the escape test's products)
+    double pr, pi;      // additive parameter
+    double dr, di;      // derivative (planes with DE only)
+    double test1, test2;
+    double escape2;
+    unsigned long long saved_r, saved_i;  // cycle probe (Brent)
+    int it;             // completed steps
+    int check_at;
+    int max_iter;
+    int stop_at;        // spill when `it` reaches this (phase budget)
+    int field;
+    int local;          // pixel index inside the field
+};
+
+__device__ __forceinline__ int phase_stop(const DirectBatch& b, int it, int max_iter) {
+    if (b.budget <= 0 || b.spill_capacity <= 0) return max_iter;
+    const long long stop = static_cast<long long>(it) + b.budget;
+    return stop < max_iter ? static_cast<int>(stop) : max_iter;
 }
 
 template <bool Planes>
-cudaError_t launch_formula(const DirectParams& p, dim3 grid, dim3 block, cudaStream_t s) {
-    switch (p.formula) {
-        case kFormulaMandelbrot: direct_kernel<kFormulaMandelbrot, Planes><<<grid, block, 0, s>>>(p); break;
-        case kFormulaJulia: direct_kernel<kFormulaJulia, Planes><<<grid, block, 0, s>>>(p); break;
-        case kFormulaBurningShip: direct_kernel<kFormulaBurningShip, Planes><<<grid, block, 0, s>>>(p); break;
-        default: direct_kernel<kFormulaTricorn, Planes><<<grid, block, 0, s>>>(p); break;
+__device__ void write_inside(const DirectParams& p, int local) {
+    p.out[local] = static_cast<float>(static_cast<double>(p.max_iter) - p.output_bias);
+    if (p.counts) p.counts[local] = static_cast<std::uint32_t>(p.max_iter);
+    if constexpr (Planes) {
+        p.p_iter[local] = p.max_iter;
+        p.p_phase[local] = 0.0;
+        p.p_dex[local] = 0.0;
+        p.p_dey[local] = 0.0;
+        p.p_t1[local] = 0.0;
+        p.p_t2[local] = 0.0;
     }
+}
+
+// Smooth escape value n + 1 - log(log|z|)/log 2 (renderer.cpp:10108-10116).
+__device__ float smooth_value(const DirectParams& p, int iteration, double m2) {
+    const double safe2 = escape_r2_d(p.escape_mode) + 1.0e-7;
+    const double safe = is_finite(m2) ? dmax(m2, safe2) : 1.7976931348623157e308;
+    const double magnitude = sqrt(safe);
+    return static_cast<float>((static_cast<double>(iteration + 1) - log(log(magnitude)) / kLogTwoD) - p.output_bias);
+}
+
+template <int Formula>
+__device__ void write_escape_planes(const DirectParams& p, const Lane& l, double m2) {
+    constexpr bool has_de = Formula == kFormulaMandelbrot || Formula == kFormulaJulia;
+    const int local = l.local;
+    p.out[local] = smooth_value(p, l.it, m2);
+    if (p.counts) p.counts[local] = static_cast<std::uint32_t>(l.it + 1);
+    p.p_iter[local] = l.it;
+    double phase = 0.0;
+    if (p.need_phase && is_finite(l.zr) && is_finite(l.zi)) {
+        phase = atan2(l.zi, l.zr) / kTwoPi;
+        phase -= floor(phase);
+    }
+    p.p_phase[local] = phase;
+    double de_re = 0.0, de_im = 0.0;
+    if (has_de && p.need_de && is_finite(l.zr) && is_finite(l.zi) && is_finite(l.dr) && is_finite(l.di)) {
+        if (!direct_de(l.zr, l.zi, l.dr, l.di, fe_from(p.pixel_spacing, 0), de_re, de_im)) {
+            de_re = 0.0;
+            de_im = 0.0;
+        }
+    }
+    p.p_dex[local] = de_re;
+    p.p_dey[local] = de_im;
+    p.p_t1[local] = l.test1;
+    p.p_t2[local] = l.test2;
+}
+
+// Warp-private staging in shared memory.  Pixel starts and escapes happen
+// on single lanes at scattered times; doing their FP64 work (the
+// cardioid/bulb test, the smooth value's logs) there would issue a full warp
+// instruction for one lane each time.  Instead the warp classifies 32 new
+// pixels at once into a start stack and parks escaped pixels until 32 are
+// waiting, then finishes them with every lane busy (ballot + popc compaction).
+struct StartSlot {
+    double cx, cy;
+    int field, local;
+};
+struct ParkSlot {
+    double m2;
+    int it, field, local, pad;
+};
+constexpr int kStage = 64;
+struct WarpStage {
+    StartSlot start[kStage];
+    ParkSlot park[kStage];
+};
+
+// Warp-uniform queue state (every lane holds the same values).
+struct WarpQueue {
+    long long next, end;  // claimed pixel range not yet classified
+    int field;            // field of `next` (search hint)
+    int starts;           // pixels waiting in the start stack
+    int parked;           // escapes waiting in the park buffer
+    bool drained;         // the batch counter ran out
+};
+
+// Classify up to 32 pixels of the warp's claimed range (claiming a new chunk
+// when it is empty): interior-culled pixels are written at once, the others
+// pushed on the start stack with their coordinates.
+template <int Formula, bool Planes>
+__device__ void classify(const DirectBatch& b, WarpQueue& q, WarpStage& st, unsigned long long* claim,
+                         unsigned lane, unsigned below, long long total) {
+    constexpr unsigned kFull = 0xffffffffu;
+    if (q.next >= q.end) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(claim, static_cast<unsigned long long>(b.chunk));
+        base = __shfl_sync(kFull, base, 0);
+        if (static_cast<long long>(base) >= total) {
+            q.drained = true;
+            return;
+        }
+        q.next = static_cast<long long>(base);
+        q.end = q.next + b.chunk < total ? q.next + b.chunk : total;
+    }
+    const long long avail = q.end - q.next;
+    const int n = avail < 32 ? static_cast<int>(avail) : 32;
+    const long long g = q.next + lane;
+    bool keep = false;
+    double cx = 0.0, cy = 0.0;
+    int f = q.field, local = 0;
+    if (static_cast<int>(lane) < n) {
+        while (g >= b.first[f + 1]) ++f;
+        const DirectParams& p = b.field[f];
+        local = static_cast<int>(g - b.first[f]);
+        const int py = local / p.width;
+        const int px = local - py * p.width;
+        const double* coords = b.coords + b.coord_offset[f];
+        cx = coords[px];
+        cy = coords[p.width + py];
+        keep = true;
+        if constexpr (Formula == kFormulaMandelbrot) {
+            if (b.interior_test[f]) {
+                // renderer.cpp:10060-10066
+                const double qq = (cx - 0.25) * (cx - 0.25) + cy * cy;
+                const bool cardioid = qq * (qq + cx - 0.25) <= 0.25 * cy * cy;
+                const bool bulb = (cx + 1.0) * (cx + 1.0) + cy * cy <= 0.0625;
+                if (cardioid || bulb) keep = false;
+            }
+        }
+        if (p.max_iter <= 0) keep = false;
+        if (!keep) write_inside<Planes>(p, local);
+    }
+    q.field = __shfl_sync(kFull, f, n - 1);
+    q.next += n;
+    const unsigned kept = __ballot_sync(kFull, keep);
+    if (keep) {
+        StartSlot& slot = st.start[q.starts + __popc(kept & below)];
+        slot.cx = cx;
+        slot.cy = cy;
+        slot.field = f;
+        slot.local = local;
+    }
+    q.starts += __popc(kept);
+    __syncwarp();
+}
+
+template <int Formula>
+__device__ void begin_pixel(const DirectBatch& b, const StartSlot& slot, Lane& l) {
+    constexpr bool julia = Formula == kFormulaJulia;
+    const DirectParams& p = b.field[slot.field];
+    l.field = slot.field;
+    l.local = slot.local;
+    l.zr = julia ? slot.cx : 0.0;
+    l.zi = julia ? slot.cy : 0.0;
+    l.rs = l.zr * l.zr;
+    l.is = l.zi * l.zi;
+    l.pr = julia ? p.julia_re : slot.cx;
+    l.pi = julia ? p.julia_im : slot.cy;
+    l.dr = julia ? 1.0 : 0.0;
+    l.di = 0.0;
+    l.test1 = 0.0;
+    l.test2 = 0.0;
+    l.escape2 = escape_r2_d(p.escape_mode);
+    l.saved_r = dbits(l.zr);
+    l.saved_i = dbits(l.zi);
+    l.it = 0;
+    l.check_at = 1;
+    l.max_iter = p.max_iter;
+    l.stop_at = phase_stop(b, 0, p.max_iter);
+}
+
+// Resume a spilled pixel of an earlier phase.
+template <int Formula>
+__device__ void resume_pixel(const DirectBatch& b, const DirectSpill& e, Lane& l) {
+    constexpr bool julia = Formula == kFormulaJulia;
+    const DirectParams& p = b.field[e.field];
+    l.field = e.field;
+    l.local = e.local;
+    l.zr = e.zr;
+    l.zi = e.zi;
+    l.rs = l.zr * l.zr;
+    l.is = l.zi * l.zi;
+    if (julia) {
+        l.pr = p.julia_re;
+        l.pi = p.julia_im;
+    } else {
+        const int py = e.local / p.width;
+        const int px = e.local - py * p.width;
+        const double* coords = b.coords + b.coord_offset[e.field];
+        l.pr = coords[px];
+        l.pi = coords[p.width + py];
+    }
+    l.dr = e.dr;
+    l.di = e.di;
+    l.test1 = e.test1;
+    l.test2 = e.test2;
+    l.escape2 = escape_r2_d(p.escape_mode);
+    l.saved_r = e.saved_r;
+    l.saved_i = e.saved_i;
+    l.it = e.it;
+    l.check_at = e.check_at;
+    l.max_iter = p.max_iter;
+    l.stop_at = phase_stop(b, e.it, p.max_iter);
+}
+
+__device__ void finish_parked(const DirectBatch& b, const ParkSlot& e) {
+    const DirectParams& p = b.field[e.field];
+    p.out[e.local] = smooth_value(p, e.it, e.m2);
+    if (p.counts) p.counts[e.local] = static_cast<std::uint32_t>(e.it + 1);
+}
+
+// Direct field render over a batch of fields with lane refill.
+//
+// Restates render_direct_scalar_formula / render_direct_with_planes_formula
+// (renderer.cpp:10054-10135, 10281-10438) pixel for pixel: the same
+// coordinates, cardioid/bulb culling, the map z^2 + c with the reference's
+// operation order (this translation unit is built without FMA contraction),
+// escape at |z|^2 > R^2 and the smooth value.  Two rewrites leave every
+// output bit unchanged:
+//   * the squares zr*zr and zi*zi of the escape test are the next step's
+//     squares, and 2 zr zi is formed as the product zr*zi with its exponent
+//     raised by one (exact for normal numbers; the multiply otherwise);
+//   * an orbit that returns bit for bit to an earlier z (Brent's cycle
+//     probe) repeats forever and can never escape, so it is settled as
+//     interior at once; interior outputs do not depend on z.
+// FP64 is the bottleneck on this part (1/64 of the FP32 rate), so a warp
+// never waits on a finished lane: each warp claims chunks of pixels from a
+// device counter over all fields of the batch and refills idle lanes every
+// step from its start stack; escapes are parked and finished 32 at a time.
+template <int Formula, bool Planes>
+__global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant__ DirectBatch b) {
+    constexpr unsigned kFull = 0xffffffffu;
+    __shared__ WarpStage stages[4];
+    WarpStage& st = stages[threadIdx.x >> 5];
+    const unsigned lane_id = threadIdx.x & 31u;
+    const unsigned below = (1u << lane_id) - 1u;
+    const bool fresh = b.phase == 0;
+    unsigned long long* claim = b.counter + b.phase;
+    unsigned long long* spill_count = b.counter + kDirectPhases + b.phase;
+    const long long total = fresh ? b.first[b.count]
+                                  : static_cast<long long>(*(b.counter + kDirectPhases + b.phase - 1));
+    const long long spilled_in = fresh ? 0 : (total < b.spill_in_capacity ? total : b.spill_in_capacity);
+    WarpQueue q{0, 0, 0, 0, 0, false};
+    bool active = false;
+    Lane l;
+    l.field = 0;
+    l.zr = l.zi = l.rs = l.is = l.pr = l.pi = 0.0;
+    l.dr = l.di = l.test1 = l.test2 = 0.0;
+    l.escape2 = 4.0;
+    l.saved_r = l.saved_i = 0;
+    l.it = 0;
+    l.check_at = 1;
+    l.max_iter = 0;
+    l.stop_at = 0;
+    l.local = 0;
+
+    while (true) {
+        unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && fresh) {
+            const int need = __popc(idle);
+            while (q.starts < need && !q.drained) classify<Formula, Planes>(b, q, st, claim, lane_id, below, total);
+            const int rank = __popc(idle & below);
+            if (!active && rank < q.starts) {
+                begin_pixel<Formula>(b, st.start[q.starts - 1 - rank], l);
+                active = true;
+            }
+            q.starts -= need < q.starts ? need : q.starts;
+            __syncwarp();
+        } else if (idle != 0u) {
+            // Resume phase: idle lanes take spilled pixels of the last phase.
+            while (idle != 0u && !q.drained) {
+                if (q.next >= q.end) {
+                    unsigned long long base = 0;
+                    if (lane_id == 0) base = atomicAdd(claim, static_cast<unsigned long long>(b.chunk));
+                    base = __shfl_sync(kFull, base, 0);
+                    if (static_cast<long long>(base) >= spilled_in) {
+                        q.drained = true;
+                        break;
+                    }
+                    q.next = static_cast<long long>(base);
+                    q.end = q.next + b.chunk < spilled_in ? q.next + b.chunk : spilled_in;
+                }
+                const int rank = __popc(idle & below);
+                const bool mine = ((idle >> lane_id) & 1u) != 0u && rank < q.end - q.next;
+                if (mine) {
+                    resume_pixel<Formula>(b, b.spill_in[q.next + rank], l);
+                    active = true;
+                }
+                const unsigned took = __ballot_sync(kFull, mine);
+                q.next += __popc(took);
+                idle &= ~took;
+            }
+        }
+        if (__ballot_sync(kFull, active) == 0u) {
+            // Drained: finish what is parked (fewer than 32) and stop.
+            if constexpr (!Planes) {
+                if (static_cast<int>(lane_id) < q.parked) finish_parked(b, st.park[lane_id]);
+            }
+            break;
+        }
+
+        // One step on every lane (idle lanes compute on stale values and
+        // discard them: the FP64 pipe costs the same per warp instruction).
+        constexpr bool has_de = Formula == kFormulaMandelbrot || Formula == kFormulaJulia;
+        if constexpr (Planes && has_de) {
+            if (b.field[l.field].need_de) {
+                // d' = 2 z d + 1 (parameter plane) or 2 z d (Julia) on the
+                // pre-step z (renderer.cpp:336-338).
+                const double add_re = Formula == kFormulaJulia ? 0.0 : 1.0;
+                const double ndr = 2.0 * l.zr * l.dr - 2.0 * l.zi * l.di + add_re;
+                const double ndi = 2.0 * l.zr * l.di + 2.0 * l.zi * l.dr + 0.0;
+                l.dr = ndr;
+                l.di = ndi;
+            }
+        }
+        const double ar = Formula == kFormulaBurningShip ? fabs_(l.zr) : l.zr;
+        const double ai = Formula == kFormulaBurningShip ? fabs_(l.zi) : l.zi;
+        double cross;
+        const bool fast = twice_product(ar, ai, cross);
+        if (__any_sync(kFull, active && !fast)) {
+            if (!fast) cross = Formula == kFormulaTricorn ? -2.0 * l.zr * l.zi : 2.0 * ar * ai;
+            else if (Formula == kFormulaTricorn) cross = -cross;
+        } else if (Formula == kFormulaTricorn) {
+            cross = -cross;
+        }
+        const double nr = (l.rs - l.is) + l.pr;
+        const double ni = cross + l.pi;
+        l.zr = nr;
+        l.zi = ni;
+        l.rs = nr * nr;
+        l.is = ni * ni;
+        const double m2 = l.rs + l.is;
+        if constexpr (Planes) {
+            l.test2 = l.test1;
+            l.test1 = m2;
+        }
+        // m2 > R^2 or not finite.  m2 is a sum of squares (sign bit clear),
+        // so the IEEE order equals the integer order of the bit patterns, and
+        // NaN and infinity compare above every finite R^2.
+        const bool escaped = active && (dbits(m2) & 0x7fffffffffffffffull) > dbits(l.escape2);
+        bool inside = false;
+        bool spill = false;
+        if (active && !escaped) {
+            ++l.it;
+            if ((dbits(l.zr) == l.saved_r && dbits(l.zi) == l.saved_i) || l.it >= l.max_iter) {
+                inside = true;
+            } else {
+                if (l.it == l.check_at) {
+                    l.saved_r = dbits(l.zr);
+                    l.saved_i = dbits(l.zi);
+                    l.check_at = l.check_at < (1 << 30) ? l.check_at << 1 : l.check_at;
+                }
+                spill = l.it >= l.stop_at;
+            }
+        }
+        if (inside) {
+            write_inside<Planes>(b.field[l.field], l.local);
+            active = false;
+        }
+        const unsigned spilling = __ballot_sync(kFull, spill);
+        if (spilling != 0u) {
+            // Park lanes past the phase budget in the next phase's list (one
+            // atomic per warp); a full list lets them run on here.
+            unsigned long long base = 0;
+            if (lane_id == static_cast<unsigned>(__ffs(spilling) - 1)) {
+                base = atomicAdd(spill_count, static_cast<unsigned long long>(__popc(spilling)));
+            }
+            base = __shfl_sync(kFull, base, __ffs(spilling) - 1);
+            if (spill) {
+                const long long slot = static_cast<long long>(base) + __popc(spilling & below);
+                if (slot < b.spill_capacity) {
+                    DirectSpill& e = b.spill_out[slot];
+                    e.zr = l.zr;
+                    e.zi = l.zi;
+                    e.dr = l.dr;
+                    e.di = l.di;
+                    e.test1 = l.test1;
+                    e.test2 = l.test2;
+                    e.saved_r = l.saved_r;
+                    e.saved_i = l.saved_i;
+                    e.it = l.it;
+                    e.check_at = l.check_at;
+                    e.field = l.field;
+                    e.local = l.local;
+                    active = false;
+                } else {
+                    l.stop_at = l.max_iter;
+                }
+            }
+        }
+        if constexpr (Planes) {
+            if (escaped) {
+                write_escape_planes<Formula>(b.field[l.field], l, m2);
+                active = false;
+            }
+        } else {
+            const unsigned esc = __ballot_sync(kFull, escaped);
+            if (esc != 0u) {
+                if (escaped) {
+                    ParkSlot& slot = st.park[q.parked + __popc(esc & below)];
+                    slot.m2 = m2;
+                    slot.it = l.it;
+                    slot.field = l.field;
+                    slot.local = l.local;
+                    active = false;
+                }
+                q.parked += __popc(esc);
+                __syncwarp();
+                if (q.parked >= 32) {
+                    finish_parked(b, st.park[q.parked - 32 + static_cast<int>(lane_id)]);
+                    q.parked -= 32;
+                    __syncwarp();
+                }
+            }
+        }
+    }
+}
+
+// Per-field coordinate tables (renderer.cpp:10185-10196): cx per column and
+// cy per row, each centre + offset * span / size in double; also zeroes the
+// batch's claim counter.
+__global__ void direct_coords_kernel(const __grid_constant__ DirectBatch b) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < 2 * kDirectPhases) b.counter[i] = 0ull;
+    for (int f = 0; f < b.count; ++f) {
+        const DirectParams& p = b.field[f];
+        const long long span = static_cast<long long>(p.width) + p.height;
+        const long long start = b.coord_offset[f];
+        if (i < start || i >= start + span) continue;
+        const int k = static_cast<int>(i - start);
+        double value;
+        if (k < p.width) {
+            const double x_origin = p.coordinate_mode == 1 ? static_cast<double>(p.width / 2)
+                                                           : static_cast<double>(p.width - 1) / 2.0;
+            const double x_offset = (static_cast<double>(k) - x_origin) * p.width_span / static_cast<double>(p.width);
+            value = p.center_re + x_offset;
+        } else {
+            const int py = k - p.width;
+            const double y_origin = p.coordinate_mode == 1 ? static_cast<double>(p.height / 2)
+                                                           : static_cast<double>(p.height - 1) / 2.0;
+            const double y_offset =
+                -(static_cast<double>(py) - y_origin) * p.height_span / static_cast<double>(p.height);
+            value = p.center_im + y_offset;
+        }
+        b.coords[i] = value;
+    }
+}
+
+template <int Formula, bool Planes>
+cudaError_t launch_queue(const DirectBatch& b, int sms, int blocks_per_sm, cudaStream_t s) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int blocks = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, direct_queue_kernel<Formula, Planes>, 128, 0);
+        per_sm = blocks > 0 ? blocks : 1;
+    }
+    const long long pixels = b.first[b.count];
+    const int use = blocks_per_sm > 0 && blocks_per_sm < per_sm ? blocks_per_sm : per_sm;
+    long long grid = static_cast<long long>(sms) * use;
+    const long long needed = (pixels + 127) / 128;
+    if (grid > needed) grid = needed;
+    if (grid < 1) grid = 1;
+    direct_queue_kernel<Formula, Planes><<<static_cast<unsigned>(grid), 128, 0, s>>>(b);
     return cudaGetLastError();
+}
+
+template <bool Planes>
+cudaError_t launch_formula(const DirectBatch& b, int formula, int sms, int blocks_per_sm, cudaStream_t s) {
+    switch (formula) {
+        case kFormulaMandelbrot: return launch_queue<kFormulaMandelbrot, Planes>(b, sms, blocks_per_sm, s);
+        case kFormulaJulia: return launch_queue<kFormulaJulia, Planes>(b, sms, blocks_per_sm, s);
+        case kFormulaBurningShip: return launch_queue<kFormulaBurningShip, Planes>(b, sms, blocks_per_sm, s);
+        default: return launch_queue<kFormulaTricorn, Planes>(b, sms, blocks_per_sm, s);
+    }
 }
 
 // Aurora palette lookup (write_colour_pixel, renderer.cpp:5210-5237): the
@@ -248,12 +651,79 @@ cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_direct(const DirectParams& p, cudaStream_t stream) {
-    const long long pixels = static_cast<long long>(p.width) * p.height;
-    const dim3 block(128);
-    const dim3 grid(static_cast<unsigned>((pixels + 127) / 128));
-    const bool planes = p.p_iter != nullptr;
-    return planes ? launch_formula<true>(p, grid, block, stream) : launch_formula<false>(p, grid, block, stream);
+std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries) {
+    std::size_t doubles = 0;
+    for (int f = 0; f < count; ++f) doubles += static_cast<std::size_t>(fields[f].width) + fields[f].height;
+    std::size_t bytes = 256 + doubles * sizeof(double);
+    if (spill_entries > 0) {
+        bytes = (bytes + 255) / 256 * 256;
+        bytes += 2 * static_cast<std::size_t>(spill_entries) * sizeof(DirectSpill);
+    }
+    return bytes;
+}
+
+// Interior culling can matter only where the view reaches the cardioid's or
+// the period-2 bulb's bounding box (with a wide margin).
+static bool view_meets_interior(const DirectParams& p) {
+    const double half_w = 0.5 * p.width_span + 0.05, half_h = 0.5 * p.height_span + 0.05;
+    const double x0 = p.center_re - half_w, x1 = p.center_re + half_w;
+    const double y0 = p.center_im - half_h, y1 = p.center_im + half_h;
+    const bool cardioid = x1 >= -0.80 && x0 <= 0.40 && y1 >= -0.70 && y0 <= 0.70;
+    const bool bulb = x1 >= -1.30 && x0 <= -0.70 && y1 >= -0.30 && y0 <= 0.30;
+    return cardioid || bulb;
+}
+
+cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
+                                long long spill_entries, cudaStream_t stream) {
+    if (count < 1 || count > kMaxDirectFields || !scratch) return cudaErrorInvalidValue;
+    DirectBatch b{};
+    b.count = count;
+    b.counter = static_cast<unsigned long long*>(scratch);
+    b.coords = reinterpret_cast<double*>(static_cast<char*>(scratch) + 256);
+    b.chunk = shape.chunk > 0 ? shape.chunk : 64;
+    const int formula = fields[0].formula;
+    const bool planes = fields[0].p_iter != nullptr;
+    long long pixels = 0, coords = 0;
+    for (int f = 0; f < count; ++f) {
+        if (fields[f].formula != formula || (fields[f].p_iter != nullptr) != planes) return cudaErrorInvalidValue;
+        b.field[f] = fields[f];
+        b.first[f] = pixels;
+        b.coord_offset[f] = static_cast<int>(coords);
+        b.interior_test[f] = formula == kFormulaMandelbrot && view_meets_interior(fields[f]) ? 1 : 0;
+        pixels += static_cast<long long>(fields[f].width) * fields[f].height;
+        coords += static_cast<long long>(fields[f].width) + fields[f].height;
+    }
+    b.first[count] = pixels;
+    DirectSpill* lists[2] = {nullptr, nullptr};
+    if (spill_entries > 0) {
+        const std::size_t head = (256 + static_cast<std::size_t>(coords) * sizeof(double) + 255) / 256 * 256;
+        lists[0] = reinterpret_cast<DirectSpill*>(static_cast<char*>(scratch) + head);
+        lists[1] = lists[0] + spill_entries;
+    }
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    direct_coords_kernel<<<static_cast<unsigned>((coords + 255) / 256), 256, 0, stream>>>(b);
+    cudaError_t status = cudaGetLastError();
+    if (status != cudaSuccess) return status;
+    // Iteration budgets of the phases: short pixels finish in phase 0; the
+    // long ones (interior pixels the cycle probe has not settled yet, slow
+    // escapes) are repacked 32 to a warp in the later phases instead of
+    // holding a warp each at the end of the queue.
+    static const int budgets[kDirectPhases] = {256, 1024, 4096, 0};
+    const int phases = spill_entries > 0 ? kDirectPhases : 1;
+    for (int phase = 0; phase < phases; ++phase) {
+        b.phase = phase;
+        b.budget = phase + 1 < phases ? budgets[phase] : 0;
+        b.spill_capacity = phase + 1 < phases ? spill_entries : 0;
+        b.spill_in = phase > 0 ? lists[(phase - 1) % 2] : nullptr;
+        b.spill_in_capacity = phase > 0 ? spill_entries : 0;
+        b.spill_out = phase + 1 < phases ? lists[phase % 2] : nullptr;
+        status = planes ? launch_formula<true>(b, formula, sms, shape.blocks_per_sm, stream)
+                        : launch_formula<false>(b, formula, sms, shape.blocks_per_sm, stream);
+        if (status != cudaSuccess) return status;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels, const std::uint8_t* lut,

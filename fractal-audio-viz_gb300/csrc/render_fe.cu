@@ -1,190 +1,18 @@
-// Floatexp form: deep Mandelbrot perturbation with FP32-mantissa / int32-
-// exponent deltas, one thread per pixel.
-//
-// The decision structure is the plain form's (render_bla_impl,
-// renderer.cpp:12673-13583): image-series jump, glitch sentinel, escape,
-// rebasing, map_end continuation, cubic/linear BLA with endpoint replay and
-// the plain tail once |delta|^2 > 2^-90 and no BLA block applies.  The
-// arithmetic is FP32: floatexp (floatexp32.h) while deltas are tiny, plain
-// float in the tail.  FP64 stays in the host-side table construction (BLA
-// coefficient merging, validity radii) and the orbit downcast; the tables are
-// converted once per handle.  Per-field agreement with the FP64 form is
-// measured by the bench (count mismatch fraction) and by
-// tests/test_gpu_floatexp.py.
+// Floatexp form kernels: one deep Mandelbrot field per launch (the
+// per-field entry point), the batched persistent queue over many fields, the
+// tile-scheduled queue (64x64 tiles claimed in a given order, per-tile cost
+// and tail timing recorded), the coarse tile probe with the cost network's
+// features, and the heaviest-first ordering of tiles.  All run the same
+// per-pixel code (render_fe.cuh), so scheduling never changes a pixel.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-#include "device.h"
-#include "runtime.h"
+#include "mlp.h"
+#include "render_fe.cuh"
 
 namespace fgb {
 namespace {
-
-using namespace f32x;
-
-constexpr float kLn2 = 0.693147180559945309f;
-constexpr float kInvLn2 = 1.442695040888963407f;
-
-__device__ __forceinline__ float nan32() { return __int_as_float(0x7fc00000); }
-
-__device__ __forceinline__ float axis_offset(int index, int dimension, int mode) {
-    const float origin = mode == 1 ? static_cast<float>(dimension / 2) : static_cast<float>(dimension - 1) * 0.5f;
-    return static_cast<float>(index) - origin;
-}
-
-__device__ __forceinline__ N1e bailout(int mode) {
-    N1e r;
-    if (mode == 1) {
-        r.m = 0.7450580596923828f;  // 1e8 = 0.745... * 2^27
-        r.e = 27;
-    } else {
-        r.m = 0.5f;
-        r.e = 3;
-    }
-    return r;
-}
-
-__device__ __forceinline__ F2e ld_f2e(const F2e* p) { return make(__ldg(&p->x), __ldg(&p->y), __ldg(&p->e)); }
-__device__ __forceinline__ N1e ld_n1e(const N1e* p) {
-    N1e r;
-    r.m = __ldg(&p->m);
-    r.e = __ldg(&p->e);
-    return r;
-}
-
-// Smooth escape value n - log2(ln|z|) from a squared norm (renderer.cpp:8170-8181).
-__device__ __forceinline__ float smooth_from_norm(int iteration, const N1e& n, float bias) {
-    const float log_mag = 0.5f * (__logf(n.m) + static_cast<float>(n.e) * kLn2);
-    if (!(log_mag > 0.0f) || !isfinite(log_mag)) return static_cast<float>(iteration) - bias;
-    return (static_cast<float>(iteration) - __logf(log_mag) * kInvLn2) - bias;
-}
-
-__device__ const FxCubic* find_cubic(const FxParams& p, int start, const N1e& dn, int max_length) {
-    if (start <= 0 || max_length <= 0) return nullptr;
-    const int levels = p.cubic_index.levels;
-    if (levels == 0 || start > p.cubic_index.count[0]) return nullptr;
-    int top = 31 - __clz(max_length);
-    top = top < levels - 1 ? top : levels - 1;
-    const int offset = start - 1;
-    for (int level = top; level >= 1; --level) {
-        if ((offset & ((1 << level) - 1)) != 0) continue;
-        const int index = offset >> level;
-        if (index >= p.cubic_index.count[level]) continue;
-        const FxCubic* c = p.cubic + p.cubic_index.offset[level] + index;
-        const N1e r2 = ld_n1e(&c->r2);
-        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
-    }
-    return nullptr;
-}
-
-__device__ const FxLinear* find_linear(const FxParams& p, int start, const N1e& dn, int max_length) {
-    if (start <= 0 || max_length <= 0) return nullptr;
-    const int levels = p.linear_index.levels;
-    if (levels == 0 || start > p.linear_index.count[0]) return nullptr;
-    int top = 31 - __clz(max_length);
-    top = top < levels - 1 ? top : levels - 1;
-    const int offset = start - 1;
-    for (int level = top; level >= 1; --level) {
-        if ((offset & ((1 << level) - 1)) != 0) continue;
-        const int index = offset >> level;
-        if (index >= p.linear_index.count[level]) continue;
-        const FxLinear* c = p.linear + p.linear_index.offset[level] + index;
-        const N1e r2 = ld_n1e(&c->r2);
-        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
-    }
-    return nullptr;
-}
-
-// Cubic bivariate map in Horner form (renderer.cpp:8686-8730).
-__device__ F2e apply_cubic(const FxCubic* s, const F2e& d, const F2e& c, int order) {
-    const F2e k0 = ld_f2e(&s->c[0]);
-    const F2e k1 = ld_f2e(&s->c[1]);
-    if (order <= 1) return add(mul(k0, d), mul(k1, c));
-    const F2e k2 = ld_f2e(&s->c[2]);
-    const F2e k3 = ld_f2e(&s->c[3]);
-    const F2e k4 = ld_f2e(&s->c[4]);
-    if (order == 2) {
-        return add(mul(d, add(k0, add(mul(k2, d), mul(k3, c)))), mul(c, add(k1, mul(k4, c))));
-    }
-    const F2e dcub = add(add(mul(ld_f2e(&s->c[5]), d), mul(ld_f2e(&s->c[6]), c)), k2);
-    const F2e ccub = add(k3, mul(ld_f2e(&s->c[7]), c));
-    const F2e din = add(k0, add(mul(d, dcub), mul(c, ccub)));
-    const F2e cin = add(k1, mul(c, add(k4, mul(ld_f2e(&s->c[8]), c))));
-    return add(mul(d, din), mul(c, cin));
-}
-
-struct PixelOut {
-    float value;
-    std::uint32_t count;
-};
-
-// Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).
-__device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc) {
-    const float dcr = to_float_x(dc), dci = to_float_y(dc);
-    float dr = to_float_x(delta), di = to_float_y(delta);
-    const float escape2 = p.escape_mode == 1 ? 1.0e8f : 4.0f;
-    const float safe2 = escape2 + 1.0e-7f;
-    int steps = 0, rebases = 0;
-    const bool strict = p.strict != 0;
-    float zr = __ldg(&p.orbit[ref].zr), zi = __ldg(&p.orbit[ref].zi);
-    while (iteration < p.max_iter && ref + 1 < p.orbit_size) {
-        const float lr = 2.0f * (zr * dr - zi * di);
-        const float li = 2.0f * (zr * di + zi * dr);
-        const float sr = dr * dr - di * di;
-        const float si = 2.0f * dr * di;
-        dr = lr + sr + dcr;
-        di = li + si + dci;
-        ++ref;
-        ++iteration;
-        if (++steps > 65536) return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                                             strict ? 0u : static_cast<std::uint32_t>(iteration)};
-        zr = __ldg(&p.orbit[ref].zr);
-        zi = __ldg(&p.orbit[ref].zi);
-        const float tr = zr + dr, ti = zi + di;
-        const float m2 = tr * tr + ti * ti;
-        if (!isfinite(m2)) {
-            return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                            strict ? 0u : static_cast<std::uint32_t>(iteration)};
-        }
-        if (m2 > escape2) {
-            const float mag = sqrtf(fmaxf(m2, safe2));
-            return PixelOut{(static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
-                            static_cast<std::uint32_t>(iteration)};
-        }
-        if (m2 < dr * dr + di * di) {
-            dr = tr;
-            di = ti;
-            ref = 0;
-            zr = __ldg(&p.orbit[0].zr);
-            zi = __ldg(&p.orbit[0].zi);
-            if (++rebases > 64) {
-                return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                                strict ? 0u : static_cast<std::uint32_t>(iteration)};
-            }
-        }
-    }
-    if (iteration < p.max_iter) {
-        return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                        strict ? 0u : static_cast<std::uint32_t>(iteration)};
-    }
-    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
-}
-
-// Direct recurrence from the total once the pixel has left the reference.
-__device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc) {
-    const F2e parameter = add(ld_f2e(&p.orbit[1].z), dc);
-    const N1e limit = bailout(p.escape_mode);
-    while (iteration < p.max_iter) {
-        total = add(mul(total, total), parameter);
-        ++iteration;
-        const N1e n = norm2(total);
-        if (n_cmp(n, limit) > 0) {
-            return PixelOut{smooth_from_norm(iteration, n, p.output_bias), static_cast<std::uint32_t>(iteration)};
-        }
-    }
-    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
-}
 
 __global__ void __launch_bounds__(128) floatexp_kernel(const FxParams p) {
     const long long pixels = static_cast<long long>(p.width) * p.height;
@@ -192,141 +20,275 @@ __global__ void __launch_bounds__(128) floatexp_kernel(const FxParams p) {
     if (index >= pixels) return;
     const int py = static_cast<int>(index / p.width);
     const int px = static_cast<int>(index - static_cast<long long>(py) * p.width);
-    const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
-    const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
-    const F2e dx = norm(p.view_width.x * xf, 0.0f, p.view_width.e);
-    const F2e dy = norm(p.view_height.x * yf, 0.0f, p.view_height.e);
-    const F2e dc = add(make(dx.x, 0.0f, dx.e), make(0.0f, dy.x, dy.e));
-
-    F2e delta = dc;
-    int ref = 1;
-    int iteration = 1;
-    if (p.series_on && n_cmp(norm2(dc), p.series_r2) <= 0) {
-        F2e value = ld_f2e(&p.series[p.series_terms - 1]);
-        for (int k = p.series_terms - 1; k > 1; --k) value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
-        delta = mul(value, dc);
-        ref = p.series_iteration;
-        iteration = p.series_iteration;
-    }
-    const N1e limit = bailout(p.escape_mode);
-    const N1e three = N1e{0.75f, 2};
-    PixelOut result{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
-    bool have_total = false;
-    F2e total = zero();
-    N1e total_norm = n_norm(0.0f, 0);
-    bool no_pixel_bla = false;
-    int rebases = 0;
-    while (iteration < p.max_iter) {
-        if (ref < 0 || ref >= p.orbit_size) {
-            result = PixelOut{static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration)};
-            break;
-        }
-        const F2e z = ld_f2e(&p.orbit[ref].z);
-        if (!have_total) {
-            total = add(z, delta);
-            total_norm = norm2(total);
-        }
-        have_total = false;
-        const N1e z2 = ld_n1e(&p.orbit[ref].z2);
-        if (z2.m != 0.0f && z2.e != 0x3fffffff) {
-            // Glitch when |Z + d|^2 < 1e-7 |Z|^2.
-            const N1e bound = n_norm(z2.m * 1.0e-7f, z2.e);
-            if (n_cmp(total_norm, bound) < 0) {
-                if (p.allow_recovery && finite(total) && ++rebases <= 64) {
-                    delta = total;
-                    ref = 0;
-                    continue;
-                }
-                result = PixelOut{nan32(), 0u};
-                break;
-            }
-        }
-        if (n_cmp(total_norm, limit) > 0) {
-            result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
-                              static_cast<std::uint32_t>(iteration)};
-            break;
-        }
-        const N1e dn = norm2(delta);
-        if (n_cmp(total_norm, dn) < 0) {
-            if (++rebases > 64) {
-                result = continue_direct(p, total, iteration, dc);
-                break;
-            }
-            delta = total;
-            ref = 0;
-            continue;
-        }
-        if (p.map_end > 1 && ref >= p.map_end) {
-            result = continue_direct(p, total, iteration, dc);
-            break;
-        }
-        const int remaining = p.max_iter - iteration;
-        const int order = p.approx_order >= 3 && dn.e < -115 ? (dn.e < -160 ? 1 : 2) : p.approx_order;
-        const FxLinear* lin = nullptr;
-        const FxCubic* cub = nullptr;
-        const bool bla = !p.disable_bla && !no_pixel_bla;
-        if (bla) {
-            if (order <= 1) {
-                lin = find_linear(p, ref, dn, p.max_lin_len < remaining ? p.max_lin_len : remaining);
-            } else {
-                cub = find_cubic(p, ref, dn, p.max_bla_len < remaining ? p.max_bla_len : remaining);
-            }
-        }
-        const int length = lin ? __ldg(&lin->len) : (cub ? __ldg(&cub->len) : 0);
-        if (bla && (length <= 0 || ref + length > p.max_iter) && dn.e > -90) {
-            result = float_tail(p, iteration, ref, delta, dc);
-            break;
-        }
-        if (length > 0 && ref + length <= p.max_iter) {
-            const F2e previous = delta;
-            delta = lin ? add(mul(ld_f2e(&lin->a), previous), mul(ld_f2e(&lin->b), dc))
-                        : apply_cubic(cub, previous, dc, order);
-            const F2e z_end = ld_f2e(&p.orbit[ref + length].z);
-            const F2e end = add(z_end, delta);
-            const N1e end_norm = norm2(end);
-            if (!finite(delta) || !finite(end)) {
-                delta = previous;
-                no_pixel_bla = true;
-                continue;
-            }
-            if (n_cmp(end_norm, three) >= 0) {
-                // Replay the block exactly near escape.
-                delta = previous;
-                bool escaped = false;
-                for (int k = 0; k < length && iteration < p.max_iter; ++k) {
-                    const F2e zk = ld_f2e(&p.orbit[ref].z);
-                    delta = add(twice(mul(zk, delta)), add(mul(delta, delta), dc));
-                    ++ref;
-                    ++iteration;
-                    total = add(ld_f2e(&p.orbit[ref].z), delta);
-                    total_norm = norm2(total);
-                    if (n_cmp(total_norm, limit) > 0) {
-                        result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
-                                          static_cast<std::uint32_t>(iteration)};
-                        escaped = true;
-                        break;
-                    }
-                }
-                if (escaped) break;
-                have_total = true;
-            } else {
-                ref += length;
-                iteration += length;
-                total = end;
-                total_norm = end_norm;
-                have_total = true;
-            }
-            continue;
-        }
-        delta = add(twice(mul(z, delta)), add(mul(delta, delta), dc));
-        ++ref;
-        ++iteration;
-    }
+    const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
     p.out[index] = result.value;
     if (p.counts) p.counts[index] = result.count;
 }
 
+// Batched persistent form: every warp claims chunks of pixels from one
+// device counter over all fields of the batch (fields in the order given,
+// heaviest first when the caller orders them so) and renders them with the
+// per-pixel code above.  Lanes of a warp stay on neighbouring pixels, whose
+// paths through the series/BLA/tail code coincide (31.5 of 32 lanes active
+// per instruction on the 1920x1080 keyframes), so no lane refill is needed.
+__global__ void __launch_bounds__(128) floatexp_queue_kernel(const __grid_constant__ FxBatch b) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const long long total = b.first[b.count];
+    int f = 0;
+    while (true) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(b.counter, static_cast<unsigned long long>(b.chunk));
+        base = __shfl_sync(kFull, base, 0);
+        if (static_cast<long long>(base) >= total) break;
+        const long long end = static_cast<long long>(base) + b.chunk < total ? static_cast<long long>(base) + b.chunk
+                                                                              : total;
+        for (long long g = static_cast<long long>(base) + lane; g < end; g += 32) {
+            while (g >= b.first[f + 1]) ++f;
+            const FxParams& p = b.field[f];
+            const int local = static_cast<int>(g - b.first[f]);
+            const int py = local / p.width;
+            const int px = local - py * p.width;
+            const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
+            p.out[local] = result.value;
+            if (p.counts) p.counts[local] = result.count;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Field of a batch tile id (binary search over the tile prefix).
+__device__ __forceinline__ int tile_field(const FxBatch& b, int tile) {
+    int lo = 0, hi = b.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.tiles_first[mid] <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Tile-scheduled persistent queue: a warp claims one band (tile_rows rows)
+// of a 64x64 tile at a time, tiles in `order`.
+__global__ void __launch_bounds__(128) floatexp_tile_kernel(const __grid_constant__ FxBatch b) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const int bands = kTileSide / b.tile_rows;
+    const long long units = static_cast<long long>(b.tiles_first[b.count]) * bands;
+    while (true) {
+        unsigned long long unit = 0;
+        if (lane == 0) unit = atomicAdd(b.counter, 1ull);
+        unit = __shfl_sync(kFull, unit, 0);
+        if (static_cast<long long>(unit) >= units) break;
+        const long long start = clock64();
+        if (b.timing && lane == 0) {
+            const unsigned long long now = global_ns();
+            atomicMin(&b.timing[0], now);
+            atomicMax(&b.timing[1], now);
+        }
+        const int rank = static_cast<int>(unit / bands);
+        const int band = static_cast<int>(unit - static_cast<long long>(rank) * bands);
+        const int tile = b.order ? static_cast<int>(b.order[rank]) : rank;
+        const int f = tile_field(b, tile);
+        const FxParams& p = b.field[f];
+        const int t = tile - b.tiles_first[f];
+        const int ty = t / b.tiles_x[f];
+        const int tx = t - ty * b.tiles_x[f];
+        const int x0 = tx * kTileSide;
+        const int y0 = ty * kTileSide + band * b.tile_rows;
+        for (int i = static_cast<int>(lane); i < kTileSide * b.tile_rows; i += 32) {
+            const int px = x0 + (i & (kTileSide - 1));
+            const int py = y0 + i / kTileSide;
+            if (px >= p.width || py >= p.height) continue;
+            const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
+            const long long local = static_cast<long long>(py) * p.width + px;
+            p.out[local] = result.value;
+            if (p.counts) p.counts[local] = result.count;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (b.tile_cost) atomicAdd(&b.tile_cost[tile], static_cast<unsigned long long>(clock64() - start));
+            if (b.timing) atomicMax(&b.timing[2], global_ns());
+        }
+    }
+}
+
+// Coarse probe: 16x16 samples (every 4th pixel each way, centred in its 4x4
+// block and clamped to the field) of every tile, through the same per-pixel
+// code; glitched samples count 0.
+__global__ void __launch_bounds__(128) tile_probe_kernel(const __grid_constant__ FxBatch b, std::uint32_t* probe) {
+    const long long samples = static_cast<long long>(b.tiles_first[b.count]) * mlp::kProbe;
+    for (long long s = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; s < samples;
+         s += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int tile = static_cast<int>(s / mlp::kProbe);
+        const int k = static_cast<int>(s - static_cast<long long>(tile) * mlp::kProbe);
+        const int f = tile_field(b, tile);
+        const FxParams& p = b.field[f];
+        const int t = tile - b.tiles_first[f];
+        const int ty = t / b.tiles_x[f];
+        const int tx = t - ty * b.tiles_x[f];
+        int px = tx * kTileSide + (k % mlp::kProbeSide) * kProbeStride + kProbeStride / 2;
+        int py = ty * kTileSide + (k / mlp::kProbeSide) * kProbeStride + kProbeStride / 2;
+        px = px < p.width ? px : p.width - 1;
+        py = py < p.height ? py : p.height - 1;
+        probe[s] = fxk::floatexp_pixel(p, px, py).count;
+    }
+}
+
+// Network features of each tile: log(1 + count) / log(1 + cap) for the 256
+// probe samples, log10 zoom / 100, log10 cap / 7, zeros to 320; zero rows
+// pad to `rows`.
+__global__ void tile_features_kernel(const __grid_constant__ FxBatch b, const std::uint32_t* probe,
+                                     __nv_bfloat16* features, int rows) {
+    const long long total = static_cast<long long>(rows) * mlp::kFeatures;
+    const int tiles = b.tiles_first[b.count];
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int tile = static_cast<int>(i / mlp::kFeatures);
+        const int k = static_cast<int>(i - static_cast<long long>(tile) * mlp::kFeatures);
+        float v = 0.0f;
+        if (tile < tiles) {
+            const int f = tile_field(b, tile);
+            const float cap = static_cast<float>(b.field[f].max_iter);
+            if (k < mlp::kProbe) {
+                v = log1pf(static_cast<float>(probe[static_cast<long long>(tile) * mlp::kProbe + k])) / log1pf(cap);
+            } else if (k == mlp::kProbe) {
+                v = b.log_zoom[f] / 100.0f;
+            } else if (k == mlp::kProbe + 1) {
+                v = log10f(cap) / 7.0f;
+            }
+        }
+        features[i] = __float2bfloat16_rn(v);
+    }
+}
+
+// Heaviest-first order from predicted normalised log costs: a counting sort
+// over 1024 buckets of [-8, 8) in one block (descending).
+__global__ void __launch_bounds__(1024) tile_order_kernel(const float* predicted, int tiles, unsigned* order) {
+    __shared__ unsigned count[1024];
+    __shared__ unsigned offset[1024];
+    count[threadIdx.x] = 0;
+    __syncthreads();
+    auto bucket = [](float v) {
+        int k = static_cast<int>(floorf((v + 8.0f) * 64.0f));
+        k = k < 0 ? 0 : (k > 1023 ? 1023 : k);
+        return 1023 - k;  // heaviest first
+    };
+    for (int i = threadIdx.x; i < tiles; i += blockDim.x) {
+        const float v = predicted[i];
+        atomicAdd(&count[bucket(isfinite(v) ? v : 0.0f)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned run = 0;
+        for (int k = 0; k < 1024; ++k) {
+            offset[k] = run;
+            run += count[k];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < tiles; i += blockDim.x) {
+        const float v = predicted[i];
+        const unsigned slot = atomicAdd(&offset[bucket(isfinite(v) ? v : 0.0f)], 1u);
+        order[slot] = static_cast<unsigned>(i);
+    }
+}
+
+FxBatch make_batch(const FxParams* fields, const float* log_zoom, int count) {
+    FxBatch b{};
+    b.count = count;
+    long long pixels = 0;
+    int tiles = 0;
+    for (int f = 0; f < count; ++f) {
+        b.field[f] = fields[f];
+        b.first[f] = pixels;
+        b.tiles_first[f] = tiles;
+        b.tiles_x[f] = (fields[f].width + kTileSide - 1) / kTileSide;
+        b.log_zoom[f] = log_zoom ? log_zoom[f] : 0.0f;
+        pixels += static_cast<long long>(fields[f].width) * fields[f].height;
+        tiles += b.tiles_x[f] * ((fields[f].height + kTileSide - 1) / kTileSide);
+    }
+    b.first[count] = pixels;
+    b.tiles_first[count] = tiles;
+    return b;
+}
+
+int resident_grid(const void* kernel, int blocks_per_sm, long long needed_blocks) {
+    int device = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    if (per_sm <= 0) per_sm = 1;
+    const int use = blocks_per_sm > 0 && blocks_per_sm < per_sm ? blocks_per_sm : per_sm;
+    long long grid = static_cast<long long>(sms) * use;
+    if (grid > needed_blocks) grid = needed_blocks;
+    return grid < 1 ? 1 : static_cast<int>(grid);
+}
+
 }  // namespace
+
+int batch_tiles(const FxParams* fields, int count) {
+    int tiles = 0;
+    for (int f = 0; f < count; ++f) {
+        tiles += ((fields[f].width + kTileSide - 1) / kTileSide) * ((fields[f].height + kTileSide - 1) / kTileSide);
+    }
+    return tiles;
+}
+
+cudaError_t launch_floatexp_tiles(const FxParams* fields, const float* log_zoom, int count,
+                                  unsigned long long* counter, const QueueShape& shape, const TileSchedule& schedule,
+                                  cudaStream_t stream) {
+    if (count < 1 || count > kMaxFxFields || !counter) return cudaErrorInvalidValue;
+    const int rows = schedule.tile_rows;
+    if (rows <= 0 || rows > kTileSide || kTileSide % rows != 0) return cudaErrorInvalidValue;
+    FxBatch b = make_batch(fields, log_zoom, count);
+    b.counter = counter;
+    b.chunk = 1;
+    b.tile_rows = rows;
+    b.order = schedule.order;
+    b.tile_cost = schedule.tile_cost;
+    b.timing = schedule.timing;
+    cudaError_t status = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (status == cudaSuccess && b.tile_cost) {
+        status = cudaMemsetAsync(b.tile_cost, 0, sizeof(unsigned long long) * b.tiles_first[count], stream);
+    }
+    if (status == cudaSuccess && b.timing) {
+        status = cudaMemsetAsync(b.timing, 0xff, sizeof(unsigned long long), stream);
+        if (status == cudaSuccess) status = cudaMemsetAsync(b.timing + 1, 0, 2 * sizeof(unsigned long long), stream);
+    }
+    if (status != cudaSuccess) return status;
+    const long long units = static_cast<long long>(b.tiles_first[count]) * (kTileSide / rows);
+    const int grid = resident_grid(reinterpret_cast<const void*>(floatexp_tile_kernel), shape.blocks_per_sm,
+                                   (units + 3) / 4);
+    floatexp_tile_kernel<<<grid, 128, 0, stream>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_probe(const FxParams* fields, const float* log_zoom, int count, std::uint32_t* probe,
+                              __nv_bfloat16* features, int feature_rows, cudaStream_t stream) {
+    if (count < 1 || count > kMaxFxFields || !probe || !features) return cudaErrorInvalidValue;
+    const FxBatch b = make_batch(fields, log_zoom, count);
+    const long long samples = static_cast<long long>(b.tiles_first[count]) * mlp::kProbe;
+    const int grid = resident_grid(reinterpret_cast<const void*>(tile_probe_kernel), 0, (samples + 127) / 128);
+    tile_probe_kernel<<<grid, 128, 0, stream>>>(b, probe);
+    cudaError_t status = cudaGetLastError();
+    if (status != cudaSuccess) return status;
+    const long long values = static_cast<long long>(feature_rows) * mlp::kFeatures;
+    tile_features_kernel<<<static_cast<unsigned>((values + 255) / 256 < 4096 ? (values + 255) / 256 : 4096), 256, 0,
+                           stream>>>(b, probe, features, feature_rows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_order(const float* predicted, int tiles, unsigned* order, cudaStream_t stream) {
+    if (tiles < 1 || !predicted || !order) return cudaErrorInvalidValue;
+    tile_order_kernel<<<1, 1024, 0, stream>>>(predicted, tiles, order);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_floatexp_mandelbrot(const FxParams& p, cudaStream_t stream) {
     const long long pixels = static_cast<long long>(p.width) * p.height;
@@ -334,4 +296,38 @@ cudaError_t launch_floatexp_mandelbrot(const FxParams& p, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_floatexp_batch(const FxParams* fields, int count, unsigned long long* counter,
+                                  const QueueShape& shape, cudaStream_t stream) {
+    if (count < 1 || count > kMaxFxFields || !counter) return cudaErrorInvalidValue;
+    static_assert(sizeof(FxBatch) <= 32000, "kernel parameter limit");
+    FxBatch b{};
+    b.count = count;
+    b.chunk = shape.chunk > 0 ? shape.chunk : 256;
+    b.counter = counter;
+    long long pixels = 0;
+    for (int f = 0; f < count; ++f) {
+        b.field[f] = fields[f];
+        b.first[f] = pixels;
+        pixels += static_cast<long long>(fields[f].width) * fields[f].height;
+    }
+    b.first[count] = pixels;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int blocks = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, floatexp_queue_kernel, 128, 0);
+        per_sm = blocks > 0 ? blocks : 1;
+    }
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int use = shape.blocks_per_sm > 0 && shape.blocks_per_sm < per_sm ? shape.blocks_per_sm : per_sm;
+    long long grid = static_cast<long long>(sms) * use;
+    const long long needed = (pixels + 127) / 128;
+    if (grid > needed) grid = needed;
+    if (grid < 1) grid = 1;
+    cudaError_t status = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (status != cudaSuccess) return status;
+    floatexp_queue_kernel<<<static_cast<unsigned>(grid), 128, 0, stream>>>(b);
+    return cudaGetLastError();
+}
 }  // namespace fgb

@@ -1,0 +1,342 @@
+// Floatexp form (shared by render_fe.cu and queue.cu): deep Mandelbrot perturbation with FP32-mantissa / int32-
+// exponent deltas, one thread per pixel.
+//
+// The decision structure is the plain form's (render_bla_impl,
+// renderer.cpp:12673-13583): image-series jump, glitch sentinel, escape,
+// rebasing, map_end continuation, cubic/linear BLA with endpoint replay and
+// the plain tail once |delta|^2 > 2^-90 and no BLA block applies.  The
+// arithmetic is FP32: floatexp (floatexp32.h) while deltas are tiny, plain
+// float in the tail.  FP64 stays in the host-side table construction (BLA
+// coefficient merging, validity radii) and the orbit downcast; the tables are
+// converted once per handle.  Per-field agreement with the FP64 form is
+// measured by the bench (count mismatch fraction) and by
+// tests/test_gpu_floatexp.py.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device.h"
+
+namespace fgb {
+namespace fxk {
+namespace {
+
+using namespace f32x;
+
+constexpr float kLn2 = 0.693147180559945309f;
+constexpr float kInvLn2 = 1.442695040888963407f;
+
+__device__ __forceinline__ float nan32() { return __int_as_float(0x7fc00000); }
+
+__device__ __forceinline__ float axis_offset(int index, int dimension, int mode) {
+    const float origin = mode == 1 ? static_cast<float>(dimension / 2) : static_cast<float>(dimension - 1) * 0.5f;
+    return static_cast<float>(index) - origin;
+}
+
+__device__ __forceinline__ N1e bailout(int mode) {
+    N1e r;
+    if (mode == 1) {
+        r.m = 0.7450580596923828f;  // 1e8 = 0.745... * 2^27
+        r.e = 27;
+    } else {
+        r.m = 0.5f;
+        r.e = 3;
+    }
+    return r;
+}
+
+__device__ __forceinline__ F2e ld_f2e(const F2e* p) { return make(__ldg(&p->x), __ldg(&p->y), __ldg(&p->e)); }
+__device__ __forceinline__ N1e ld_n1e(const N1e* p) {
+    N1e r;
+    r.m = __ldg(&p->m);
+    r.e = __ldg(&p->e);
+    return r;
+}
+
+// Smooth escape value n - log2(ln|z|) from a squared norm (renderer.cpp:8170-8181).
+__device__ __forceinline__ float smooth_from_norm(int iteration, const N1e& n, float bias) {
+    const float log_mag = 0.5f * (__logf(n.m) + static_cast<float>(n.e) * kLn2);
+    if (!(log_mag > 0.0f) || !isfinite(log_mag)) return static_cast<float>(iteration) - bias;
+    return (static_cast<float>(iteration) - __logf(log_mag) * kInvLn2) - bias;
+}
+
+// The reference forms the pixel norm as R^2 + ((|Z|^2 - R^2) + 2 Re(conj(Z) d)
+// + |d|^2) in double (renderer.cpp:8374-8390), so its glitch sentinel and
+// rebase test see |Z + d|^2 rounded to a multiple of the last place of R^2:
+// 2^-51 for R^2 = 4, 2^-26 for R^2 = 1e8, and exact zero below half of it.
+// Near a periodic reference (|Z| close to 0) that zero flags a glitch the
+// exact norm would not.  This applies the same quantisation to the FP32 norm
+// where it is coarser than the FP32 mantissa.
+__device__ __forceinline__ N1e reference_norm(const N1e& n, int mode) {
+    const int place = mode == 1 ? -26 : -51;
+    if (n.m == 0.0f || n.e >= place + 24) return n;
+    const float units = rintf(ldexpf(n.m, n.e - place));
+    return n_norm(units, place);
+}
+
+__device__ const FxCubic* find_cubic(const FxParams& p, int start, const N1e& dn, int max_length) {
+    if (start <= 0 || max_length <= 0) return nullptr;
+    const int levels = p.cubic_index.levels;
+    if (levels == 0 || start > p.cubic_index.count[0]) return nullptr;
+    int top = 31 - __clz(max_length);
+    top = top < levels - 1 ? top : levels - 1;
+    const int offset = start - 1;
+    for (int level = top; level >= 1; --level) {
+        if ((offset & ((1 << level) - 1)) != 0) continue;
+        const int index = offset >> level;
+        if (index >= p.cubic_index.count[level]) continue;
+        const FxCubic* c = p.cubic + p.cubic_index.offset[level] + index;
+        const N1e r2 = ld_n1e(&c->r2);
+        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
+    }
+    return nullptr;
+}
+
+__device__ const FxLinear* find_linear(const FxParams& p, int start, const N1e& dn, int max_length) {
+    if (start <= 0 || max_length <= 0) return nullptr;
+    const int levels = p.linear_index.levels;
+    if (levels == 0 || start > p.linear_index.count[0]) return nullptr;
+    int top = 31 - __clz(max_length);
+    top = top < levels - 1 ? top : levels - 1;
+    const int offset = start - 1;
+    for (int level = top; level >= 1; --level) {
+        if ((offset & ((1 << level) - 1)) != 0) continue;
+        const int index = offset >> level;
+        if (index >= p.linear_index.count[level]) continue;
+        const FxLinear* c = p.linear + p.linear_index.offset[level] + index;
+        const N1e r2 = ld_n1e(&c->r2);
+        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
+    }
+    return nullptr;
+}
+
+// Cubic bivariate map in Horner form (renderer.cpp:8686-8730).
+__device__ F2e apply_cubic(const FxCubic* s, const F2e& d, const F2e& c, int order) {
+    const F2e k0 = ld_f2e(&s->c[0]);
+    const F2e k1 = ld_f2e(&s->c[1]);
+    if (order <= 1) return add(mul(k0, d), mul(k1, c));
+    const F2e k2 = ld_f2e(&s->c[2]);
+    const F2e k3 = ld_f2e(&s->c[3]);
+    const F2e k4 = ld_f2e(&s->c[4]);
+    if (order == 2) {
+        return add(mul(d, add(k0, add(mul(k2, d), mul(k3, c)))), mul(c, add(k1, mul(k4, c))));
+    }
+    const F2e dcub = add(add(mul(ld_f2e(&s->c[5]), d), mul(ld_f2e(&s->c[6]), c)), k2);
+    const F2e ccub = add(k3, mul(ld_f2e(&s->c[7]), c));
+    const F2e din = add(k0, add(mul(d, dcub), mul(c, ccub)));
+    const F2e cin = add(k1, mul(c, add(k4, mul(ld_f2e(&s->c[8]), c))));
+    return add(mul(d, din), mul(c, cin));
+}
+
+struct PixelOut {
+    float value;
+    std::uint32_t count;
+};
+
+// Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).
+__device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc) {
+    const float dcr = to_float_x(dc), dci = to_float_y(dc);
+    float dr = to_float_x(delta), di = to_float_y(delta);
+    const float escape2 = p.escape_mode == 1 ? 1.0e8f : 4.0f;
+    const float safe2 = escape2 + 1.0e-7f;
+    int steps = 0, rebases = 0;
+    const bool strict = p.strict != 0;
+    float zr = __ldg(&p.orbit[ref].zr), zi = __ldg(&p.orbit[ref].zi);
+    while (iteration < p.max_iter && ref + 1 < p.orbit_size) {
+        const float lr = 2.0f * (zr * dr - zi * di);
+        const float li = 2.0f * (zr * di + zi * dr);
+        const float sr = dr * dr - di * di;
+        const float si = 2.0f * dr * di;
+        dr = lr + sr + dcr;
+        di = li + si + dci;
+        ++ref;
+        ++iteration;
+        if (++steps > 65536) return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
+                                             strict ? 0u : static_cast<std::uint32_t>(iteration)};
+        zr = __ldg(&p.orbit[ref].zr);
+        zi = __ldg(&p.orbit[ref].zi);
+        const float tr = zr + dr, ti = zi + di;
+        const float m2 = tr * tr + ti * ti;
+        if (!isfinite(m2)) {
+            return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
+                            strict ? 0u : static_cast<std::uint32_t>(iteration)};
+        }
+        if (m2 > escape2) {
+            const float mag = sqrtf(fmaxf(m2, safe2));
+            return PixelOut{(static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                            static_cast<std::uint32_t>(iteration)};
+        }
+        if (m2 < dr * dr + di * di) {
+            dr = tr;
+            di = ti;
+            ref = 0;
+            zr = __ldg(&p.orbit[0].zr);
+            zi = __ldg(&p.orbit[0].zi);
+            if (++rebases > 64) {
+                return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
+                                strict ? 0u : static_cast<std::uint32_t>(iteration)};
+            }
+        }
+    }
+    if (iteration < p.max_iter) {
+        return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
+                        strict ? 0u : static_cast<std::uint32_t>(iteration)};
+    }
+    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+}
+
+// Direct recurrence from the total once the pixel has left the reference.
+__device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc) {
+    const F2e parameter = add(ld_f2e(&p.orbit[1].z), dc);
+    const N1e limit = bailout(p.escape_mode);
+    while (iteration < p.max_iter) {
+        total = add(mul(total, total), parameter);
+        ++iteration;
+        const N1e n = norm2(total);
+        if (n_cmp(n, limit) > 0) {
+            return PixelOut{smooth_from_norm(iteration, n, p.output_bias), static_cast<std::uint32_t>(iteration)};
+        }
+    }
+    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+}
+
+// One pixel of the floatexp form; shared by the per-field kernel and the
+// batched persistent queue (queue.cu).
+__device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int py) {
+    const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
+    const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
+    const F2e dx = norm(p.view_width.x * xf, 0.0f, p.view_width.e);
+    const F2e dy = norm(p.view_height.x * yf, 0.0f, p.view_height.e);
+    const F2e dc = add(make(dx.x, 0.0f, dx.e), make(0.0f, dy.x, dy.e));
+
+    F2e delta = dc;
+    int ref = 1;
+    int iteration = 1;
+    if (p.series_on && n_cmp(norm2(dc), p.series_r2) <= 0) {
+        F2e value = ld_f2e(&p.series[p.series_terms - 1]);
+        for (int k = p.series_terms - 1; k > 1; --k) value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
+        delta = mul(value, dc);
+        ref = p.series_iteration;
+        iteration = p.series_iteration;
+    }
+    const N1e limit = bailout(p.escape_mode);
+    const N1e three = N1e{0.75f, 2};
+    PixelOut result{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    bool have_total = false;
+    F2e total = zero();
+    N1e total_norm = n_norm(0.0f, 0);
+    bool no_pixel_bla = false;
+    int rebases = 0;
+    while (iteration < p.max_iter) {
+        if (ref < 0 || ref >= p.orbit_size) {
+            result = PixelOut{static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration)};
+            break;
+        }
+        const F2e z = ld_f2e(&p.orbit[ref].z);
+        if (!have_total) {
+            total = add(z, delta);
+            total_norm = reference_norm(norm2(total), p.escape_mode);
+        }
+        have_total = false;
+        const N1e z2 = ld_n1e(&p.orbit[ref].z2);
+        if (z2.m != 0.0f && z2.e != 0x3fffffff) {
+            // Glitch when |Z + d|^2 < 1e-7 |Z|^2.
+            const N1e bound = n_norm(z2.m * 1.0e-7f, z2.e);
+            if (n_cmp(total_norm, bound) < 0) {
+                if (p.allow_recovery && finite(total) && ++rebases <= 64) {
+                    delta = total;
+                    ref = 0;
+                    continue;
+                }
+                result = PixelOut{nan32(), 0u};
+                break;
+            }
+        }
+        if (n_cmp(total_norm, limit) > 0) {
+            result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
+                              static_cast<std::uint32_t>(iteration)};
+            break;
+        }
+        const N1e dn = norm2(delta);
+        if (n_cmp(total_norm, dn) < 0) {
+            if (++rebases > 64) {
+                result = continue_direct(p, total, iteration, dc);
+                break;
+            }
+            delta = total;
+            ref = 0;
+            continue;
+        }
+        if (p.map_end > 1 && ref >= p.map_end) {
+            result = continue_direct(p, total, iteration, dc);
+            break;
+        }
+        const int remaining = p.max_iter - iteration;
+        const int order = p.approx_order >= 3 && dn.e < -115 ? (dn.e < -160 ? 1 : 2) : p.approx_order;
+        const FxLinear* lin = nullptr;
+        const FxCubic* cub = nullptr;
+        const bool bla = !p.disable_bla && !no_pixel_bla;
+        if (bla) {
+            if (order <= 1) {
+                lin = find_linear(p, ref, dn, p.max_lin_len < remaining ? p.max_lin_len : remaining);
+            } else {
+                cub = find_cubic(p, ref, dn, p.max_bla_len < remaining ? p.max_bla_len : remaining);
+            }
+        }
+        const int length = lin ? __ldg(&lin->len) : (cub ? __ldg(&cub->len) : 0);
+        if (bla && (length <= 0 || ref + length > p.max_iter) && dn.e > -90) {
+            result = float_tail(p, iteration, ref, delta, dc);
+            break;
+        }
+        if (length > 0 && ref + length <= p.max_iter) {
+            const F2e previous = delta;
+            delta = lin ? add(mul(ld_f2e(&lin->a), previous), mul(ld_f2e(&lin->b), dc))
+                        : apply_cubic(cub, previous, dc, order);
+            const F2e z_end = ld_f2e(&p.orbit[ref + length].z);
+            const F2e end = add(z_end, delta);
+            const N1e end_norm = reference_norm(norm2(end), p.escape_mode);
+            if (!finite(delta) || !finite(end)) {
+                delta = previous;
+                no_pixel_bla = true;
+                continue;
+            }
+            if (n_cmp(end_norm, three) >= 0) {
+                // Replay the block exactly near escape.
+                delta = previous;
+                bool escaped = false;
+                for (int k = 0; k < length && iteration < p.max_iter; ++k) {
+                    const F2e zk = ld_f2e(&p.orbit[ref].z);
+                    delta = add(twice(mul(zk, delta)), add(mul(delta, delta), dc));
+                    ++ref;
+                    ++iteration;
+                    total = add(ld_f2e(&p.orbit[ref].z), delta);
+                    total_norm = reference_norm(norm2(total), p.escape_mode);
+                    if (n_cmp(total_norm, limit) > 0) {
+                        result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
+                                          static_cast<std::uint32_t>(iteration)};
+                        escaped = true;
+                        break;
+                    }
+                }
+                if (escaped) break;
+                have_total = true;
+            } else {
+                ref += length;
+                iteration += length;
+                total = end;
+                total_norm = end_norm;
+                have_total = true;
+            }
+            continue;
+        }
+        delta = add(twice(mul(z, delta)), add(mul(delta, delta), dc));
+        ++ref;
+        ++iteration;
+    }
+    return result;
+}
+
+}  // namespace
+}  // namespace fxk
+}  // namespace fgb

@@ -9,6 +9,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <string>
 
@@ -35,6 +36,9 @@ enum ScratchSlot {
     kScratchKfpSamples,
     kScratchKfpAux,
     kScratchWork,
+    kScratchDirect,
+    kScratchQueue,
+    kScratchTiles,
     kScratchCount
 };
 
@@ -47,6 +51,25 @@ struct ThreadRuntime {
     unsigned long long* stamp = nullptr;  // time-budget origin
     cudaEvent_t start = nullptr;
     cudaEvent_t stop = nullptr;
+    // Completion of the last launch that used the scratch buffers, recorded
+    // on whichever stream it ran (a caller's stream for the device entry
+    // points); the next launch on another stream waits for it.
+    cudaEvent_t scratch_done = nullptr;
+    bool scratch_recorded = false;
+    // Keyframe batches: a second stream for the direct (FP64) fields so they
+    // overlap the floatexp (FP32) fields, a capture stream, fork/join events
+    // and the instantiated CUDA graphs of batches seen before.
+    cudaStream_t side = nullptr;
+    cudaStream_t capture = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join = nullptr;
+    std::map<std::string, cudaGraphExec_t> graphs;
+    int last_shapes[4] = {};
+    int pinned_shapes[4] = {};  // set by fractal_gb300_set_queue_shapes
+    void* costnet = nullptr;    // attached tile-cost network (not owned)
+    cudaStream_t tile_stream = nullptr;  // stream of the last tile-scheduled batch
+    int last_tiles = 0;
+    bool shapes_pinned = false;
     double last_kernel_ms = 0.0;
     ~ThreadRuntime();
 };
@@ -55,6 +78,11 @@ struct ThreadRuntime {
 // CUDA device is usable).
 ThreadRuntime& thread_runtime();
 void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes);
+// Order scratch use across streams of one thread: wait_scratch before the
+// first launch on `stream` that touches scratch, release_scratch after the
+// last one.
+void wait_scratch(ThreadRuntime& rt, cudaStream_t stream);
+void release_scratch(ThreadRuntime& rt, cudaStream_t stream);
 
 std::shared_ptr<DeviceTables> device_tables(ReferenceContext& ctx);
 void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev);

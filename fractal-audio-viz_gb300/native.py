@@ -257,6 +257,25 @@ _ABI = (
 )
 
 # GB300 extensions (include/fractal_gb300.h).  Absent from the CPU oracles.
+class Keyframe(ctypes.Structure):
+    """FractalGb300Keyframe: one frame of a batched device render."""
+
+    _fields_ = [
+        ("field", ctypes.c_void_p),
+        ("counts", ctypes.c_void_p),
+        ("zoom_text", ctypes.c_char_p),
+        ("reference", ctypes.c_void_p),
+        ("max_iter", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+    ]
+
+
+BATCH_GRAPH = 1
+BATCH_AUTOTUNE = 2
+BATCH_TILES = 4
+BATCH_LEARNED = 8
+BATCH_PROBE = 16
+
 _GB300_ABI = (
     ("fractal_gb300_device_count", ctypes.c_int, ()),
     ("fractal_gb300_set_table_builder", None, (ctypes.c_int,)),
@@ -276,6 +295,29 @@ _GB300_ABI = (
     ("fractal_gb300_colourise_device", ctypes.c_int,
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.c_void_p)),
+    ("fractal_gb300_render_keyframes_device", ctypes.c_int,
+     (ctypes.POINTER(Keyframe), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+      ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions), ctypes.c_int,
+      ctypes.c_uint, ctypes.c_void_p)),
+    ("fractal_gb300_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
+    ("fractal_gb300_set_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
+    ("fractal_gb300_set_cost_network", ctypes.c_int, (ctypes.c_void_p,)),
+    ("fractal_gb300_last_tiles", ctypes.c_int,
+     (ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_double))),
+    ("fractal_gb300_costnet_create", ctypes.c_void_p, (ctypes.c_uint,)),
+    ("fractal_gb300_costnet_destroy", None, (ctypes.c_void_p,)),
+    ("fractal_gb300_costnet_parameter_count", ctypes.c_int, ()),
+    ("fractal_gb300_costnet_parameters", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int)),
+    ("fractal_gb300_costnet_train_step", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_void_p)),
+    ("fractal_gb300_costnet_predict", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)),
+    ("fractal_gb300_gemm_bf16", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
       ctypes.c_void_p)),
 )
 

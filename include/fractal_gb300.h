@@ -278,6 +278,104 @@ int fractal_gb300_colourise_device(const float *field, uint8_t *rgb, int width, 
                                    int max_iter, double phase, double vocal, double instrumental,
                                    double pitch, void *stream);
 
+/* One keyframe of a batch: device outputs (`counts` may be NULL), its zoom,
+ * the reference handle it renders from (NULL: the direct FP64 path at the
+ * batch centre, which the reference pipeline takes below 1e12,
+ * visualizer.py:6152) and its iteration cap. */
+typedef struct FractalGb300Keyframe {
+    float *field;
+    uint32_t *counts;
+    const char *zoom_text;
+    void *reference;
+    int max_iter;
+    int reserved;
+} FractalGb300Keyframe;
+
+/* Capture the batch's launches into a CUDA graph and replay the graph when
+ * the same batch (same buffers, zooms, handles and options) comes again. */
+#define FRACTAL_GB300_BATCH_GRAPH 1u
+/* Time the persistent queues' launch shapes (pixels per warp claim, blocks
+ * per SM) on this batch first and keep the fastest for batches of its kind.
+ * The shapes change the schedule only, never a pixel. */
+#define FRACTAL_GB300_BATCH_AUTOTUNE 2u
+/* Floatexp frames run as a queue of 64x64 tiles (work unit: a band of rows
+ * of one tile); per-tile cost (SM cycles) and the queue's makespan and tail
+ * (time from the last claim to the last finish) are recorded for
+ * fractal_gb300_last_tiles.  Without _LEARNED the tiles go in ascending order
+ * (fields in the order given, row-major within a field): the static order. */
+#define FRACTAL_GB300_BATCH_TILES 4u
+/* Tile queue in the order predicted by the attached cost network (heaviest
+ * first), from a 16x16 coarse probe of every tile; implies _TILES. */
+#define FRACTAL_GB300_BATCH_LEARNED 8u
+/* With _TILES: compute the probe and the network features without using them
+ * (training data: fractal_gb300_last_tiles returns features and costs). */
+#define FRACTAL_GB300_BATCH_PROBE 16u
+
+/* Render many keyframes in a few launches: all direct frames in one
+ * persistent lane-refill FP64 queue on a second stream, all floatexp frames
+ * (form 1) in one persistent queue on `stream`, plain-form deep frames
+ * (form 0, or frames the floatexp form does not cover) one launch each;
+ * the second stream joins `stream` before the call's work ends.  Frames are
+ * claimed in the order given: put the costliest first.  Per-frame results are
+ * those of fractal_gb300_render_reference_device / _render_direct_device with
+ * the same arguments. */
+int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe *frames, int count, int width,
+                                          int height, const char *x_center, const char *y_center,
+                                          int series_order, int series_block,
+                                          const FractalRenderOptions *options, int form,
+                                          unsigned flags, void *stream);
+
+/* Pin the launch shapes of the calling thread's next batches (same order as
+ * fractal_gb300_queue_shapes; a 0 chunk keeps the default, a 0 blocks/SM
+ * means as many as fit); values NULL or count 0 unpins.  Pinned shapes
+ * override tuned ones and switch autotuning off. */
+int fractal_gb300_set_queue_shapes(const int *values, int count);
+
+/* Attach a cost network (fractal_gb300_costnet_create) to the calling
+ * thread's batches for FRACTAL_GB300_BATCH_LEARNED; NULL detaches.  The
+ * network is not owned. */
+int fractal_gb300_set_cost_network(void *net);
+
+/* Results of the calling thread's last tile-scheduled batch (synchronises its
+ * stream): the tile count, per-tile cost in SM cycles (float[tiles]), the
+ * features when the batch computed them (BF16 bits [tiles x 320]) and
+ * timing_ms[0] = makespan, timing_ms[1] = tail.  cost/features/timing_ms may
+ * be NULL; capacity is their tile capacity. */
+int fractal_gb300_last_tiles(int *tiles, float *cost, uint16_t *features, int capacity, double *timing_ms);
+
+/* Launch shapes the calling thread's last batch used: direct chunk, direct
+ * blocks per SM, floatexp chunk, floatexp blocks per SM (0 = as many as fit). */
+int fractal_gb300_queue_shapes(int *values, int capacity);
+
+/* ----- Tile-cost network (no counterpart in the reference) -----------
+ * A small MLP predicting the render cost of a 64x64 tile from a 16x16 coarse
+ * probe of its iteration counts plus log zoom and log cap (320 BF16 features
+ * per row: 256 probe values, 2 field values, zeros).  Layers 320 -> 256 ->
+ * 256 -> 1 with ReLU; BF16 weights and activations, FP32 accumulation on the
+ * tensor cores (tcgen05), FP32 master weights updated by Adam.  It orders
+ * work only; it never changes a pixel. */
+void *fractal_gb300_costnet_create(unsigned seed);
+void fractal_gb300_costnet_destroy(void *net);
+int fractal_gb300_costnet_parameter_count(void);
+/* Read (write = 0) or replace (write = 1) the FP32 parameters: W1 [256 x 320],
+ * b1 [256], W2 [256 x 256], b2 [256], w3 [256], b3 [1], row-major. */
+int fractal_gb300_costnet_parameters(void *net, float *values, int count, int write);
+/* One step of mean-squared-error training on `batch` rows (a multiple of
+ * 128): device features (BF16 [batch x 320]) and targets (float [batch]).
+ * update = 0 computes the loss and gradient only.  `loss` and `gradients`
+ * (parameter order, host memory) may be NULL.  Synchronises `stream`. */
+int fractal_gb300_costnet_train_step(void *net, const void *features, const float *targets, int batch,
+                                     float learning_rate, int update, float *loss, float *gradients,
+                                     void *stream);
+/* Predictions for `rows` rows (a multiple of 128) into device `out`. */
+int fractal_gb300_costnet_predict(void *net, const void *features, int rows, float *out, void *stream);
+/* The network's tensor-core product on its own: C[m x n] (float) =
+ * A[m x k] * B[n x k]^T with BF16 row-major A and B; m % 128 == 0,
+ * n % 16 == 0, k % 64 == 0, and B allocated with b_rows >= n rows, b_rows a
+ * multiple of 256 (rows beyond n are read but unused). */
+int fractal_gb300_gemm_bf16(const void *a, const void *b, float *c, int m, int n, int k, int b_rows,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,133 @@
+"""GPU: the batched keyframe path against per-keyframe renders and the oracle.
+
+fractal_gb300_render_keyframes_device renders many keyframes in a few
+launches (a persistent lane-refill FP64 queue for the direct frames on a
+second stream, a persistent floatexp queue or per-field plain launches for
+the deep ones), optionally replayed as a CUDA graph and with autotuned launch
+shapes.  None of that may change a pixel: every test here demands bit
+equality with the single-keyframe entry points (whose parity with the
+reference is tested in test_gpu_parity.py), and the direct queue's exact
+shortcuts (squares reused, doubling by exponent, Brent cycle probe) are
+checked against the oracle on interior-heavy whole-set views.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from .golden import cases as case_defs
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+WIDTH, HEIGHT = 192, 108
+LEVELS = (0, 1, 3, 6, 9, 13, 14, 20, 31, 42, 54)
+
+
+def _stack(package, product):
+    levels = [lv for lv in case_defs.fhd_stack_levels() if lv[0] in LEVELS]
+    e50 = case_defs.centres()["fhd_stack_e50"]
+    return package.atlas.KeyframeStack(product, e50["re"], e50["im"], levels, step=math.log10(8.0))
+
+
+def _buffers(n):
+    fields = torch.full((n, WIDTH * HEIGHT), -1.0, dtype=torch.float32, device="cuda")
+    counts = torch.zeros((n, WIDTH * HEIGHT), dtype=torch.int32, device="cuda")
+    return fields, counts
+
+
+def _bits(tensor):
+    return tensor.cpu().numpy().view(np.uint32)
+
+
+def _singles(stack, form):
+    fields, counts = _buffers(len(stack.keyframes))
+    for i, keyframe in enumerate(stack.keyframes):
+        stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), WIDTH, HEIGHT, form=form)
+    torch.cuda.synchronize()
+    return _bits(fields), _bits(counts)
+
+
+def _batch(stack, form, **kw):
+    fields, counts = _buffers(len(stack.keyframes))
+    targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(len(stack.keyframes))]
+    stack.render_batch_device(targets, WIDTH, HEIGHT, form=form, **kw)
+    torch.cuda.synchronize()
+    return _bits(fields), _bits(counts)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_batch_equals_single_keyframe_renders(package, product, form):
+    stack = _stack(package, product)
+    try:
+        want_field, want_counts = _singles(stack, form)
+        got_field, got_counts = _batch(stack, form)
+    finally:
+        stack.close()
+    np.testing.assert_array_equal(got_counts, want_counts)
+    np.testing.assert_array_equal(got_field, want_field)
+
+
+def test_batch_graph_replay_order_and_autotune_keep_pixels(package, product):
+    stack = _stack(package, product)
+    try:
+        want_field, want_counts = _batch(stack, 1)
+        reverse = list(range(len(stack.keyframes)))[::-1]
+        runs = [
+            _batch(stack, 1, graph=True),
+            _batch(stack, 1, graph=True),          # replay of the cached graph
+            _batch(stack, 1, order=reverse),
+            _batch(stack, 1, autotune=True),
+            _batch(stack, 0, graph=True),
+        ]
+        shapes = stack.queue_shapes()
+    finally:
+        stack.close()
+    for field, counts in runs[:4]:
+        np.testing.assert_array_equal(counts, want_counts)
+        np.testing.assert_array_equal(field, want_field)
+    assert shapes[0] > 0 and shapes[2] > 0 and shapes[1] >= 0 and shapes[3] >= 0
+    # The plain form differs from floatexp only within the floatexp budget.
+    plain_counts = runs[4][1]
+    assert np.count_nonzero(plain_counts != want_counts) <= 1e-4 * want_counts.size + 2
+
+
+@pytest.mark.parametrize("view", [
+    ("whole_set", "-0.5", "0.0", "1", 320, 180, 3000),
+    ("seahorse", "-0.7436", "0.1318", "180", 256, 144, 6000),
+    ("bulbs", "-1.25", "0.0", "6", 200, 120, 5000),
+])
+def test_direct_queue_matches_oracle_on_interior_views(package, product, oracle_port, view):
+    """Interior-heavy direct views, where the cycle probe settles most
+    interior pixels early: counts and field bits equal the oracle's."""
+    native = package.native
+    _, x, y, zoom, w, h, cap = view
+    got = native.render_fractal(product, w, h, zoom.encode(), x, y, cap, 256, False, threads=0)
+    want = native.render_fractal(oracle_port, w, h, zoom.encode(), x, y, cap, 256, False, threads=0)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_direct_queue_device_entry_on_two_streams(package, product):
+    """Back-to-back device calls on different caller streams share the
+    thread's scratch; the library orders them, so both results are exact."""
+    import ctypes
+
+    native = package.native
+    fields, counts = _buffers(2)
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    zooms = [b"1", b"40"]
+    options = native.RenderOptions()
+    for i in range(2):
+        status = product.fractal_gb300_render_direct_device(
+            ctypes.c_void_p(fields[i].data_ptr()), ctypes.c_void_p(counts[i].data_ptr()), WIDTH, HEIGHT, zooms[i],
+            b"-0.5", b"0.0", 2000, 0, 0.0, 0.0, ctypes.byref(options), ctypes.c_void_p(streams[i].cuda_stream))
+        assert status == 0, native.last_error(product)
+    torch.cuda.synchronize()
+    for i in range(2):
+        want = native.render_fractal(product, WIDTH, HEIGHT, zooms[i], "-0.5", "0.0", 2000, 256, False)
+        np.testing.assert_array_equal(_bits(fields[i]), want.view(np.uint32))
