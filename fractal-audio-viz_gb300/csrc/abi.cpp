@@ -1737,6 +1737,30 @@ int fractal_gb300_queue_shapes(int* values, int capacity) {
     });
 }
 
+int fractal_gb300_render_direct_device_noalloc(float* field, uint32_t* counts, int width, int height,
+                                               const char* zoom_text, const char* x_center, const char* y_center,
+                                               int max_iter, int formula, double julia_real, double julia_imag,
+                                               const FractalRenderOptions* supplied, void* stream_handle) {
+    return guarded("no-allocation direct render failed with an unknown exception", [&] {
+        if (!field || !zoom_text || !x_center || !y_center || !valid_dims(width, height)
+            || !valid_iterations(max_iter) || !valid_formula(formula) || !std::isfinite(julia_real)
+            || !std::isfinite(julia_imag)) {
+            throw Failure{"invalid native render dimensions, formula, or argument"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        Outputs out;
+        out.field = field;
+        out.counts = counts;
+        const DirectParams p = make_direct_params(out, width, height, parse_zoom_direct(zoom_text),
+                                                  parse_coordinate(x_center, "real"),
+                                                  parse_coordinate(y_center, "imaginary"), max_iter, formula,
+                                                  julia_real, julia_imag, o);
+        std::string why;
+        if (!launch_direct_noalloc(p, static_cast<cudaStream_t>(stream_handle), why)) throw Failure{why};
+    });
+}
+
 // ------------------------------------------------------ tile-cost network
 
 void* fractal_gb300_costnet_create(unsigned seed) {

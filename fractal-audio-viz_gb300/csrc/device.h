@@ -355,6 +355,10 @@ struct DirectBatch {
 std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries);
 cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
                                 long long spill_entries, cudaStream_t stream);
+// One direct field with its scratch taken from a fixed array compiled into
+// the library (render_noalloc.cu): no device allocation at all.
+bool launch_direct_noalloc(const DirectParams& params, cudaStream_t stream, std::string& why);
+std::size_t noalloc_scratch_limit();
 // Records %globaltimer into *slot (the time-budget origin of the next kernel).
 cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream);
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels,

@@ -347,6 +347,24 @@ int fractal_gb300_last_tiles(int *tiles, float *cost, uint16_t *features, int ca
  * blocks per SM, floatexp chunk, floatexp blocks per SM (0 = as many as fit). */
 int fractal_gb300_queue_shapes(int *values, int capacity);
 
+/* No counterpart in the reference.  The direct render of
+ * fractal_gb300_render_direct_device (same arguments, same pixels) for callers
+ * that cannot allocate device memory: inside an allocator hook, under a
+ * reserve-everything-up-front memory policy, or in a real-time loop where an
+ * allocation's implicit synchronisation is not acceptable.  It calls no
+ * cudaMalloc/cudaFree and creates no stream: `stream` NULL means the legacy
+ * default stream.  Its scratch is a fixed 128 KiB array inside the library,
+ * so width + height must be at most 16352 (larger fields fail with an error,
+ * before any launch).  All calls share that array: calls ordered on one
+ * stream are independent (each call resets what it uses), calls that overlap
+ * on the GPU race.  The first call on each device looks the array's address
+ * up (cudaGetSymbolAddress); make it before any stream capture. */
+int fractal_gb300_render_direct_device_noalloc(float *field, uint32_t *counts, int width, int height,
+                                               const char *zoom_text, const char *x_center,
+                                               const char *y_center, int max_iter, int formula,
+                                               double julia_real, double julia_imag,
+                                               const FractalRenderOptions *options, void *stream);
+
 /* ----- Tile-cost network (no counterpart in the reference) -----------
  * A small MLP predicting the render cost of a 64x64 tile from a 16x16 coarse
  * probe of its iteration counts plus log zoom and log cap (320 BF16 features
