@@ -29,6 +29,7 @@ def _load(name: str):
 native = _load("native")
 atlas = _load("atlas")
 kfp = _load("kfp")
+costnet = _load("costnet")
 _builder = _load("build")
 LIBRARY_PATH = _builder.LIBRARY
 

@@ -505,6 +505,8 @@ void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, i
                               stream);
         return;
     }
+    p.series_scaled = static_cast<FxSeriesScaled*>(scratch(rt, kScratchSeries, sizeof(FxSeriesScaled)));
+    check_cuda(launch_series_prologue(&p, 1, stream), "series prologue launch");
     check_cuda(launch_floatexp_mandelbrot(p, stream), "floatexp kernel launch");
 }
 
@@ -978,6 +980,10 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
                        "direct batch launch");
         }
     }
+    for (std::size_t i = 0; i < plan.floatexp.size(); i += kMaxFxFields) {
+        const int n = static_cast<int>(std::min<std::size_t>(kMaxFxFields, plan.floatexp.size() - i));
+        check_cuda(launch_series_prologue(plan.floatexp.data() + i, n, main), "series prologue launch");
+    }
     if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
         const TileBuffers t = tile_buffers(static_cast<char*>(scratch(rt, kScratchTiles, 1)), plan.tiles,
                                            plan.feature_rows);
@@ -1060,10 +1066,21 @@ void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime
 // Coordinate descent over the launch shapes, each candidate timed once with
 // CUDA events on the batch itself.  Shapes change only the schedule, never a
 // pixel: every candidate renders the same values.
-BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stream) {
+// Coordinate descent over the launch shapes, each candidate timed (median of
+// three, CUDA events) on the batch itself and through the same launch path
+// (graph replay or direct enqueue) the batch will use.  When the batch has
+// both queues, their blocks per SM are chosen together so both stay
+// resident at once (the FP64 direct queue and the FP32 floatexp queue then
+// share every SM instead of waiting on each other).  Shapes change only the
+// schedule, never a pixel.
+BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stream, bool graph) {
     BatchShapes best;
-    void* direct_scratch = plan.direct.empty() ? nullptr : scratch(rt, kScratchDirect, plan.direct_bytes);
-    auto* counter = static_cast<unsigned long long*>(scratch(rt, kScratchQueue, 256));
+    const bool both = !plan.direct.empty() && !plan.floatexp.empty();
+    const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
+    if (both) {
+        best.direct.blocks_per_sm = std::max(1, capacity / 2);
+        best.floatexp.blocks_per_sm = std::max(1, capacity - best.direct.blocks_per_sm);
+    }
     cudaEvent_t a = nullptr, b = nullptr;
     check_cuda(cudaEventCreate(&a), "cudaEventCreate");
     check_cuda(cudaEventCreate(&b), "cudaEventCreate");
@@ -1071,7 +1088,7 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
         float runs[3];
         for (float& ms : runs) {
             check_cuda(cudaEventRecord(a, stream), "cudaEventRecord");
-            enqueue_batch(plan, shapes, rt, stream, direct_scratch, counter);
+            launch_plan(plan, shapes, rt, stream, graph);
             check_cuda(cudaEventRecord(b, stream), "cudaEventRecord");
             check_cuda(cudaEventSynchronize(b), "cudaEventSynchronize");
             check_cuda(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
@@ -1080,35 +1097,59 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
         return runs[1];
     };
     try {
-        time(best);  // warm-up (occupancy queries, caches)
+        time(best);  // warm-up (occupancy queries, graph capture, caches)
         float best_ms = time(best);
-        const int direct_chunks[] = {32, 64, 128, 256};
-        const int direct_blocks[] = {2, 4, 8, 12, 0};
-        const int fx_chunks[] = {64, 128, 256, 512, 1024};
-        const int fx_blocks[] = {4, 6, 8, 0};
-        for (int pass = 0; pass < 2; ++pass) {
-            auto sweep = [&](int* knob, const int* values, int count) {
-                const int keep = *knob;
-                int chosen = keep;
-                for (int i = 0; i < count; ++i) {
-                    if (values[i] == keep) continue;
-                    *knob = values[i];
-                    const float ms = time(best);
-                    if (ms < best_ms) {
-                        best_ms = ms;
-                        chosen = values[i];
-                    }
+        auto sweep = [&](const std::vector<BatchShapes>& candidates) {
+            for (const BatchShapes& c : candidates) {
+                const float ms = time(c);
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = c;
                 }
-                *knob = chosen;
-            };
+            }
+        };
+        for (int pass = 0; pass < 2; ++pass) {
+            std::vector<BatchShapes> c;
             if (!plan.direct.empty()) {
-                sweep(&best.direct.chunk, direct_chunks, 4);
-                sweep(&best.direct.blocks_per_sm, direct_blocks, 5);
+                for (int chunk : {32, 64, 128}) {
+                    if (chunk == best.direct.chunk) continue;
+                    BatchShapes s = best;
+                    s.direct.chunk = chunk;
+                    c.push_back(s);
+                }
+            }
+            if (both) {
+                for (int d = 1; d < capacity; ++d) {
+                    if (d == best.direct.blocks_per_sm) continue;
+                    BatchShapes s = best;
+                    s.direct.blocks_per_sm = d;
+                    s.floatexp.blocks_per_sm = capacity - d;
+                    c.push_back(s);
+                }
+            } else if (!plan.direct.empty()) {
+                for (int d : {2, 4, 6, 0}) {
+                    if (d == best.direct.blocks_per_sm) continue;
+                    BatchShapes s = best;
+                    s.direct.blocks_per_sm = d;
+                    c.push_back(s);
+                }
+            } else if (!plan.floatexp.empty()) {
+                for (int f : {4, 6, 0}) {
+                    if (f == best.floatexp.blocks_per_sm) continue;
+                    BatchShapes s = best;
+                    s.floatexp.blocks_per_sm = f;
+                    c.push_back(s);
+                }
             }
             if (!plan.floatexp.empty()) {
-                sweep(&best.floatexp.chunk, fx_chunks, 5);
-                sweep(&best.floatexp.blocks_per_sm, fx_blocks, 4);
+                for (int chunk : {128, 256, 512}) {
+                    if (chunk == best.floatexp.chunk) continue;
+                    BatchShapes s = best;
+                    s.floatexp.chunk = chunk;
+                    c.push_back(s);
+                }
             }
+            sweep(c);
         }
     } catch (...) {
         cudaEventDestroy(a);
@@ -1626,6 +1667,12 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
                                              direct_scratch_bytes(fields.data() + i, n, spill_entries(pixels)));
             }
         }
+        if (!plan.floatexp.empty()) {
+            auto* slots = static_cast<FxSeriesScaled*>(
+                scratch(rt, kScratchSeries, sizeof(FxSeriesScaled) * plan.floatexp.size()));
+            for (std::size_t f = 0; f < plan.floatexp.size(); ++f) plan.floatexp[f].series_scaled = slots + f;
+            append_bytes(plan.key, slots);
+        }
         plan.tile_flags = flags & (FRACTAL_GB300_BATCH_TILES | FRACTAL_GB300_BATCH_LEARNED | FRACTAL_GB300_BATCH_PROBE);
         if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
             if (plan.floatexp.size() > static_cast<std::size_t>(kMaxFxFields)) {
@@ -1654,10 +1701,20 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
         append_bytes(shape_key, static_cast<int>(plan.plain.size()));
         append_bytes(shape_key, static_cast<int>(direct_doubles));
         BatchShapes shapes;
+        bool tuned = false;
         {
             std::lock_guard<std::mutex> lock(tuned_mutex);
             auto known = tuned_shapes.find(shape_key);
-            if (known != tuned_shapes.end()) shapes = known->second;
+            if (known != tuned_shapes.end()) {
+                shapes = known->second;
+                tuned = true;
+            }
+        }
+        if (!tuned && !plan.direct.empty() && !plan.floatexp.empty()) {
+            // Both queues resident at once: split the SM's blocks between them.
+            const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
+            shapes.direct.blocks_per_sm = std::max(1, capacity / 2);
+            shapes.floatexp.blocks_per_sm = std::max(1, capacity - shapes.direct.blocks_per_sm);
         }
         if (rt.shapes_pinned) {
             if (rt.pinned_shapes[0] > 0) shapes.direct.chunk = rt.pinned_shapes[0];
@@ -1667,7 +1724,7 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
         }
         wait_scratch(rt, stream);
         if ((flags & FRACTAL_GB300_BATCH_AUTOTUNE) && !rt.shapes_pinned) {
-            shapes = autotune(plan, rt, stream);
+            shapes = autotune(plan, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
             std::lock_guard<std::mutex> lock(tuned_mutex);
             tuned_shapes[shape_key] = shapes;
         }

@@ -225,6 +225,18 @@ cudaError_t launch_kfp_bounds(const float* field, long long pixels, int max_iter
 constexpr int kStatsSlots = 39;
 
 // Parameters of one floatexp-form deep Mandelbrot field render.
+// The image series rescaled for one field: delta = 2^shift * sum_k b[k] u^k
+// (k >= 1) with u = dc * 2^-scale, |u| <= 1 over the view, so every pixel
+// evaluates it in plain float (kernel-side prologue, render_fe.cu).
+constexpr int kMaxSeriesTerms = 33;
+struct FxSeriesScaled {
+    float b[kMaxSeriesTerms][2];
+    int terms;
+    int shift;
+    int scale;
+    int pad;
+};
+
 struct FxParams {
     const FxOrbitRec* orbit;
     int orbit_size;
@@ -254,6 +266,7 @@ struct FxParams {
     float output_bias;
     float* out;
     std::uint32_t* counts;
+    FxSeriesScaled* series_scaled;  // per-field slot filled by the series prologue (nullptr: F2e Horner)
 };
 
 cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stream);
@@ -300,6 +313,11 @@ struct TileSchedule {
     unsigned long long* timing = nullptr;
 };
 int batch_tiles(const FxParams* fields, int count);
+// Fill each field's series_scaled slot (before any launch that renders it).
+cudaError_t launch_series_prologue(const FxParams* fields, int count, cudaStream_t stream);
+// Resident 128-thread blocks per SM of the persistent queue kernels.
+int floatexp_queue_occupancy(bool tiles);
+int direct_queue_occupancy();
 cudaError_t launch_floatexp_tiles(const FxParams* fields, const float* log_zoom, int count,
                                   unsigned long long* counter, const QueueShape& shape, const TileSchedule& schedule,
                                   cudaStream_t stream);
@@ -345,6 +363,7 @@ struct DirectBatch {
     // rest into `spill_out` (capacity entries; when full the lane goes on).
     int phase;
     int budget;
+    int steps;                              // steps between refills
     const DirectSpill* spill_in;
     long long spill_in_capacity;
     DirectSpill* spill_out;

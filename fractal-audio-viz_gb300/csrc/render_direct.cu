@@ -408,60 +408,77 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
             break;
         }
 
-        // One step on every lane (idle lanes compute on stale values and
-        // discard them: the FP64 pipe costs the same per warp instruction).
+        // Up to `steps` steps before the next refill: every lane computes
+        // each step (an idle or settled lane on stale values that it then
+        // discards: the FP64 pipe costs the same per warp instruction), and a
+        // lane stops updating at its first event (escape, interior, budget).
         constexpr bool has_de = Formula == kFormulaMandelbrot || Formula == kFormulaJulia;
-        if constexpr (Planes && has_de) {
-            if (b.field[l.field].need_de) {
-                // d' = 2 z d + 1 (parameter plane) or 2 z d (Julia) on the
-                // pre-step z (renderer.cpp:336-338).
-                const double add_re = Formula == kFormulaJulia ? 0.0 : 1.0;
-                const double ndr = 2.0 * l.zr * l.dr - 2.0 * l.zi * l.di + add_re;
-                const double ndi = 2.0 * l.zr * l.di + 2.0 * l.zi * l.dr + 0.0;
-                l.dr = ndr;
-                l.di = ndi;
+        bool running = active;
+        bool escaped = false, inside = false, spill = false;
+        double m2_at_escape = 0.0;
+        for (int s = 0; s < b.steps; ++s) {
+            if (!__any_sync(kFull, running)) break;
+            if constexpr (Planes && has_de) {
+                if (running && b.field[l.field].need_de) {
+                    // d' = 2 z d + 1 (parameter plane) or 2 z d (Julia) on the
+                    // pre-step z (renderer.cpp:336-338).
+                    const double add_re = Formula == kFormulaJulia ? 0.0 : 1.0;
+                    const double ndr = 2.0 * l.zr * l.dr - 2.0 * l.zi * l.di + add_re;
+                    const double ndi = 2.0 * l.zr * l.di + 2.0 * l.zi * l.dr + 0.0;
+                    l.dr = ndr;
+                    l.di = ndi;
+                }
             }
-        }
-        const double ar = Formula == kFormulaBurningShip ? fabs_(l.zr) : l.zr;
-        const double ai = Formula == kFormulaBurningShip ? fabs_(l.zi) : l.zi;
-        double cross;
-        const bool fast = twice_product(ar, ai, cross);
-        if (__any_sync(kFull, active && !fast)) {
-            if (!fast) cross = Formula == kFormulaTricorn ? -2.0 * l.zr * l.zi : 2.0 * ar * ai;
-            else if (Formula == kFormulaTricorn) cross = -cross;
-        } else if (Formula == kFormulaTricorn) {
-            cross = -cross;
-        }
-        const double nr = (l.rs - l.is) + l.pr;
-        const double ni = cross + l.pi;
-        l.zr = nr;
-        l.zi = ni;
-        l.rs = nr * nr;
-        l.is = ni * ni;
-        const double m2 = l.rs + l.is;
-        if constexpr (Planes) {
-            l.test2 = l.test1;
-            l.test1 = m2;
-        }
-        // m2 > R^2 or not finite.  m2 is a sum of squares (sign bit clear),
-        // so the IEEE order equals the integer order of the bit patterns, and
-        // NaN and infinity compare above every finite R^2.
-        const bool escaped = active && (dbits(m2) & 0x7fffffffffffffffull) > dbits(l.escape2);
-        bool inside = false;
-        bool spill = false;
-        if (active && !escaped) {
+            const double ar = Formula == kFormulaBurningShip ? fabs_(l.zr) : l.zr;
+            const double ai = Formula == kFormulaBurningShip ? fabs_(l.zi) : l.zi;
+            double cross;
+            const bool fast = twice_product(ar, ai, cross);
+            if (__any_sync(kFull, running && !fast)) {
+                if (!fast) cross = Formula == kFormulaTricorn ? -2.0 * l.zr * l.zi : 2.0 * ar * ai;
+                else if (Formula == kFormulaTricorn) cross = -cross;
+            } else if (Formula == kFormulaTricorn) {
+                cross = -cross;
+            }
+            const double nr = (l.rs - l.is) + l.pr;
+            const double ni = cross + l.pi;
+            const double rs = nr * nr;
+            const double is = ni * ni;
+            const double m2 = rs + is;
+            if (!running) continue;
+            l.zr = nr;
+            l.zi = ni;
+            l.rs = rs;
+            l.is = is;
+            if constexpr (Planes) {
+                l.test2 = l.test1;
+                l.test1 = m2;
+            }
+            // m2 > R^2 or not finite.  m2 is a sum of squares (sign bit
+            // clear), so the IEEE order equals the integer order of the bit
+            // patterns, and NaN and infinity compare above every finite R^2.
+            if ((dbits(m2) & 0x7fffffffffffffffull) > dbits(l.escape2)) {
+                escaped = true;
+                m2_at_escape = m2;
+                running = false;
+                continue;
+            }
             ++l.it;
             if ((dbits(l.zr) == l.saved_r && dbits(l.zi) == l.saved_i) || l.it >= l.max_iter) {
                 inside = true;
-            } else {
-                if (l.it == l.check_at) {
-                    l.saved_r = dbits(l.zr);
-                    l.saved_i = dbits(l.zi);
-                    l.check_at = l.check_at < (1 << 30) ? l.check_at << 1 : l.check_at;
-                }
-                spill = l.it >= l.stop_at;
+                running = false;
+                continue;
+            }
+            if (l.it == l.check_at) {
+                l.saved_r = dbits(l.zr);
+                l.saved_i = dbits(l.zi);
+                l.check_at = l.check_at < (1 << 30) ? l.check_at << 1 : l.check_at;
+            }
+            if (l.it >= l.stop_at) {
+                spill = true;
+                running = false;
             }
         }
+        const double m2 = m2_at_escape;
         if (inside) {
             write_inside<Planes>(b.field[l.field], l.local);
             active = false;
@@ -651,6 +668,12 @@ cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+int direct_queue_occupancy() {
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, direct_queue_kernel<kFormulaMandelbrot, false>, 128, 0);
+    return blocks > 0 ? blocks : 1;
+}
+
 std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries) {
     std::size_t doubles = 0;
     for (int f = 0; f < count; ++f) doubles += static_cast<std::size_t>(fields[f].width) + fields[f].height;
@@ -715,6 +738,7 @@ cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scr
     for (int phase = 0; phase < phases; ++phase) {
         b.phase = phase;
         b.budget = phase + 1 < phases ? budgets[phase] : 0;
+        b.steps = phase == 0 ? 2 : 16;
         b.spill_capacity = phase + 1 < phases ? spill_entries : 0;
         b.spill_in = phase > 0 ? lists[(phase - 1) % 2] : nullptr;
         b.spill_in_capacity = phase > 0 ? spill_entries : 0;

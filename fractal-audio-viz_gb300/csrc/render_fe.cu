@@ -56,6 +56,38 @@ __global__ void __launch_bounds__(128) floatexp_queue_kernel(const __grid_consta
     }
 }
 
+// Series prologue: one thread per field rescales the F2e coefficients to
+// the field's view (see FxSeriesScaled).
+__global__ void series_prologue_kernel(const __grid_constant__ FxBatch b) {
+    const int f = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    if (f >= b.count) return;
+    const FxParams& p = b.field[f];
+    FxSeriesScaled* out = p.series_scaled;
+    if (!out || !p.series_on) return;
+    const int scale = p.view_width.e > p.view_height.e ? p.view_width.e : p.view_height.e;
+    const int terms = p.series_terms < kMaxSeriesTerms ? p.series_terms : kMaxSeriesTerms;
+    int shift = -0x3fffffff;
+    for (int k = 1; k < terms; ++k) {
+        const f32x::F2e c = p.series[k];
+        if (c.x == 0.0f && c.y == 0.0f) continue;
+        const int e = c.e + k * scale;
+        shift = e > shift ? e : shift;
+    }
+    if (shift == -0x3fffffff) shift = 0;
+    out->b[0][0] = 0.0f;
+    out->b[0][1] = 0.0f;
+    for (int k = 1; k < terms; ++k) {
+        const f32x::F2e c = p.series[k];
+        const long long d = static_cast<long long>(c.e) + static_cast<long long>(k) * scale - shift;
+        const bool keep = d > -200 && !(c.x == 0.0f && c.y == 0.0f);
+        out->b[k][0] = keep ? f32x::ldexpf_fast(c.x, static_cast<int>(d)) : 0.0f;
+        out->b[k][1] = keep ? f32x::ldexpf_fast(c.y, static_cast<int>(d)) : 0.0f;
+    }
+    out->terms = terms;
+    out->shift = shift;
+    out->scale = scale;
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -231,6 +263,23 @@ int resident_grid(const void* kernel, int blocks_per_sm, long long needed_blocks
 }
 
 }  // namespace
+
+cudaError_t launch_series_prologue(const FxParams* fields, int count, cudaStream_t stream) {
+    if (count < 1 || count > kMaxFxFields) return cudaErrorInvalidValue;
+    const FxBatch b = make_batch(fields, nullptr, count);
+    series_prologue_kernel<<<(count + 63) / 64, 64, 0, stream>>>(b);
+    return cudaGetLastError();
+}
+
+int floatexp_queue_occupancy(bool tiles) {
+    int blocks = 0;
+    if (tiles) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, floatexp_tile_kernel, 128, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, floatexp_queue_kernel, 128, 0);
+    }
+    return blocks > 0 ? blocks : 1;
+}
 
 int batch_tiles(const FxParams* fields, int count) {
     int tiles = 0;

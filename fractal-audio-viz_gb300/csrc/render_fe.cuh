@@ -214,9 +214,28 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
     int ref = 1;
     int iteration = 1;
     if (p.series_on && n_cmp(norm2(dc), p.series_r2) <= 0) {
-        F2e value = ld_f2e(&p.series[p.series_terms - 1]);
-        for (int k = p.series_terms - 1; k > 1; --k) value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
-        delta = mul(value, dc);
+        if (p.series_scaled) {
+            // Plain-float Horner on u = dc 2^-scale with the field's
+            // prescaled coefficients (|u| <= 1), rescaled once at the end.
+            const FxSeriesScaled* sc = p.series_scaled;
+            const int scale = __ldg(&sc->scale);
+            const float ur = ldexpf_fast(p.view_width.x * xf, p.view_width.e - scale);
+            const float ui = ldexpf_fast(p.view_height.x * yf, p.view_height.e - scale);
+            const int terms = __ldg(&sc->terms);
+            float vr = __ldg(&sc->b[terms - 1][0]);
+            float vi = __ldg(&sc->b[terms - 1][1]);
+            for (int k = terms - 1; k > 1; --k) {
+                const float nr = fmaf(vr, ur, fmaf(-vi, ui, __ldg(&sc->b[k - 1][0])));
+                const float ni = fmaf(vr, ui, fmaf(vi, ur, __ldg(&sc->b[k - 1][1])));
+                vr = nr;
+                vi = ni;
+            }
+            delta = norm(vr * ur - vi * ui, vr * ui + vi * ur, __ldg(&sc->shift));
+        } else {
+            F2e value = ld_f2e(&p.series[p.series_terms - 1]);
+            for (int k = p.series_terms - 1; k > 1; --k) value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
+            delta = mul(value, dc);
+        }
         ref = p.series_iteration;
         iteration = p.series_iteration;
     }

@@ -39,6 +39,7 @@ enum ScratchSlot {
     kScratchDirect,
     kScratchQueue,
     kScratchTiles,
+    kScratchSeries,
     kScratchCount
 };
 

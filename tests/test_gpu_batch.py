@@ -131,3 +131,41 @@ def test_direct_queue_device_entry_on_two_streams(package, product):
     for i in range(2):
         want = native.render_fractal(product, WIDTH, HEIGHT, zooms[i], "-0.5", "0.0", 2000, 256, False)
         np.testing.assert_array_equal(_bits(fields[i]), want.view(np.uint32))
+
+
+def test_tile_queue_static_and_learned_orders_keep_pixels(package, product):
+    """The tile-scheduled floatexp queue (static order, probe, and the order
+    a cost network predicts) renders exactly the pixels of the pixel-chunk
+    queue, and reports per-tile costs and its makespan/tail."""
+    import ctypes
+
+    native = package.native
+    stack = _stack(package, product)
+    net = product.fractal_gb300_costnet_create(3)
+    assert net, native.last_error(product)
+    try:
+        want_field, want_counts = _batch(stack, 1)
+        static = _batch(stack, 1, tiles=native.BATCH_TILES | native.BATCH_PROBE)
+        count = ctypes.c_int(0)
+        timing = (ctypes.c_double * 2)()
+        deep = [k for k in stack.keyframes if k.reference is not None]
+        tiles_expected = len(deep) * ((WIDTH + 63) // 64) * ((HEIGHT + 63) // 64)
+        cost = np.zeros(tiles_expected, dtype=np.float32)
+        features = np.zeros((tiles_expected, 320), dtype=np.uint16)
+        assert product.fractal_gb300_last_tiles(ctypes.byref(count), cost.ctypes.data, features.ctypes.data,
+                                                tiles_expected, timing) == 0, native.last_error(product)
+        assert count.value == tiles_expected
+        assert np.all(cost > 0)
+        assert timing[0] > 0 and 0 <= timing[1] <= timing[0]
+        probe = (features[:, :256].astype(np.uint32) << 16).view(np.float32)
+        assert np.all((probe >= 0) & (probe <= 1.0))
+        assert product.fractal_gb300_set_cost_network(net) == 0
+        learned = _batch(stack, 1, tiles=native.BATCH_LEARNED | native.BATCH_TILES)
+        learned_graph = _batch(stack, 1, tiles=native.BATCH_LEARNED | native.BATCH_TILES, graph=True)
+    finally:
+        product.fractal_gb300_set_cost_network(None)
+        product.fractal_gb300_costnet_destroy(net)
+        stack.close()
+    for field, counts in (static, learned, learned_graph):
+        np.testing.assert_array_equal(counts, want_counts)
+        np.testing.assert_array_equal(field, want_field)

@@ -132,3 +132,60 @@ def test_costnet_adam_step_and_training(product):
         assert loss < 0.05 * loss0, (loss0, loss)
     finally:
         product.fractal_gb300_costnet_destroy(net)
+
+
+def test_learned_order_on_8k_field_keeps_pixels_and_reports_gain(package, product):
+    """The 7680x4320 field at 1e100 (cap 1e6): pixel-chunk queue, static tile
+    order and the trained network's heaviest-first order render identical
+    pixels; the makespan and tail of both tile orders are printed and the
+    learned order may not be slower than the static one beyond noise."""
+    import json
+
+    native = package.native
+    atlas = package.atlas
+    net = package.costnet.load_default(product)
+    with open(os.path.join(ROOT, "tests", "golden", "centres.json"), encoding="ascii") as handle:
+        centre = json.load(handle)["field_e100"]
+    width, height, cap, log_zoom = 7680, 4320, 1_000_000, 100.0
+    bits = atlas.precision_bits(centre["re"], centre["im"], log_zoom)
+    handle = native.create_reference(product, centre["re"], centre["im"], atlas.zoom_text(log_zoom), cap, bits, 32)
+    field = torch.empty(width * height, dtype=torch.float32, device="cuda")
+    counts = torch.empty(width * height, dtype=torch.int32, device="cuda")
+    frames = (native.Keyframe * 1)()
+    zoom = atlas.zoom_text(log_zoom)
+    frames[0].field = field.data_ptr()
+    frames[0].counts = counts.data_ptr()
+    frames[0].zoom_text = zoom
+    frames[0].reference = handle
+    frames[0].max_iter = cap
+    options = native.RenderOptions()
+
+    def render(flags):
+        status = product.fractal_gb300_render_keyframes_device(frames, 1, width, height, None, None, 3, 256,
+                                                               ctypes.byref(options), 1, flags, None)
+        assert status == 0, native.last_error(product)
+        torch.cuda.synchronize()
+        timing = (ctypes.c_double * 2)()
+        if flags & native.BATCH_TILES:
+            assert product.fractal_gb300_last_tiles(None, None, None, 0, timing) == 0, native.last_error(product)
+        return field.cpu().numpy().view(np.uint32).copy(), counts.cpu().numpy().copy(), (timing[0], timing[1])
+
+    try:
+        net.attach()
+        want_field, want_counts, _ = render(0)
+        results = {}
+        for name, flags in (("static", native.BATCH_TILES), ("learned", native.BATCH_TILES | native.BATCH_LEARNED)):
+            runs = []
+            for _ in range(3):
+                got_field, got_counts, timing = render(flags)
+                np.testing.assert_array_equal(got_counts, want_counts)
+                np.testing.assert_array_equal(got_field, want_field)
+                runs.append(timing)
+            results[name] = sorted(runs)[1]
+        print(f"8K e100 cap 1e6: static makespan {results['static'][0]:.2f} ms tail {results['static'][1]:.2f} ms; "
+              f"learned makespan {results['learned'][0]:.2f} ms tail {results['learned'][1]:.2f} ms")
+        assert results["learned"][0] <= results["static"][0] * 1.05 + 0.5
+    finally:
+        product.fractal_gb300_set_cost_network(None)
+        net.close()
+        product.fractal_destroy_reference(handle)
