@@ -255,14 +255,20 @@ def run_gpu_arm(args) -> int:
     # Claim order: the shallow levels with interior (largest per-pixel cost)
     # first in the direct queue, the deepest levels first in the deep queue.
     order = direct_levels + deep_levels[::-1]
+    schedules = {"chunks": 0, "tiles": native.BATCH_TILES, "learned": native.BATCH_TILES | native.BATCH_LEARNED}
+    net = None
+    if forms["chosen"] == 1:
+        net = package.costnet.load_default(library)
+        net.attach()
 
-    def step_device(form, subset=None, autotune=False):
-        stack.render_batch_device(targets, WIDTH, HEIGHT, form=form, stream=handle, graph=not autotune,
-                                  autotune=autotune, order=subset if subset is not None else order)
+    def step_device(form, subset=None, autotune=False, schedule="chunks"):
+        stack.render_batch_device(targets, WIDTH, HEIGHT, form=form, stream=handle, graph=True, autotune=autotune,
+                                  order=subset if subset is not None else order,
+                                  tiles=schedules[schedule] if form == 1 else 0)
 
-    def timed(form, steps, warmup, subset=None):
+    def timed(form, steps, warmup, subset=None, schedule="chunks"):
         for _ in range(warmup):
-            step_device(form, subset)
+            step_device(form, subset, schedule=schedule)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -270,7 +276,7 @@ def run_gpu_arm(args) -> int:
         stop = torch.cuda.Event(enable_timing=True)
         start.record(stream)
         for _ in range(steps):
-            step_device(form, subset)
+            step_device(form, subset, schedule=schedule)
         stop.record(stream)
         torch.cuda.synchronize()
         ms = start.elapsed_time(stop)
@@ -280,9 +286,10 @@ def run_gpu_arm(args) -> int:
             ms = float(t.item())
         return ms
 
-    # Launch shapes tuned once on this batch (schedule only; no pixel changes).
-    step_device(forms["chosen"], autotune=True)
-    shapes = stack.queue_shapes()
+    # Launch shapes tuned once per schedule on this batch (graph replay; the
+    # shapes change the schedule only, never a pixel).
+    for name in (schedules if forms["chosen"] == 1 else ["chunks"]):
+        step_device(forms["chosen"], autotune=True, schedule=name)
     if forms["chosen"] != 0:
         step_device(0, autotune=True)
 
@@ -291,17 +298,35 @@ def run_gpu_arm(args) -> int:
     step_device(forms["chosen"])
     torch.cuda.synchronize()
     chosen_counts = counts.clone()
+    chosen_field = fields.clone()
     work = int(counts.to(torch.int64).sum().item())
     direct_work = int(counts[direct_levels].to(torch.int64).sum().item())
     step_device(0)
     torch.cuda.synchronize()
     plain_work = int(counts.to(torch.int64).sum().item())
     mismatch = int((counts != chosen_counts).sum().item())
-    del chosen_counts
+    both = torch.isfinite(fields) & torch.isfinite(chosen_field) & (counts == chosen_counts)
+    smooth_err = (fields[both] - chosen_field[both]).abs()
+    smooth_stats = {"median": float(smooth_err.median().item()), "p99": float(torch.quantile(
+        smooth_err[torch.randperm(smooth_err.numel(), device="cuda")[:1_000_000]].float(), 0.99).item()),
+        "max": float(smooth_err.max().item())}
+    del chosen_counts, chosen_field, both, smooth_err
+
+    # The chosen schedule: the fastest of the three, each timed the same way.
+    schedule_ms = {}
+    if forms["chosen"] == 1:
+        for name in schedules:
+            schedule_ms[name] = timed(1, max(2, args.steps // 2), 1, schedule=name) / max(2, args.steps // 2)
+        chosen_schedule = min(schedule_ms, key=schedule_ms.get)
+    else:
+        chosen_schedule = "chunks"
+    step_device(forms["chosen"], schedule=chosen_schedule)
+    torch.cuda.synchronize()
+    shapes = stack.queue_shapes()
 
     sampler = ClockSampler(local_rank)
     sampler.start()
-    ms = timed(forms["chosen"], args.steps, args.warmup)
+    ms = timed(forms["chosen"], args.steps, args.warmup, schedule=chosen_schedule)
     clocks = sampler.stop()
     ms_per_step = ms / args.steps
     value = world * work * args.steps / (ms * 1e-3) / 1e9
@@ -309,10 +334,19 @@ def run_gpu_arm(args) -> int:
     plain_ms = timed(0, max(1, args.steps // 2), 1) if forms["chosen"] != 0 else ms
     plain_value = plain_work * max(1, args.steps // 2) / (plain_ms * 1e-3) / 1e9 if forms["chosen"] != 0 else value
 
-    # Each queue timed alone (same launches, one part of the batch), on the
-    # launching stream.
+    # Each queue timed alone (same launches, one part of the batch).
     direct_ms = timed(forms["chosen"], 2, 1, subset=direct_levels) / 2
-    deep_ms = timed(forms["chosen"], 2, 1, subset=deep_levels[::-1]) / 2
+    steps_done = ctypes.c_ulonglong(0)
+    library.fractal_gb300_last_direct_steps(ctypes.byref(steps_done))
+    deep_ms = timed(forms["chosen"], 2, 1, subset=deep_levels[::-1], schedule=chosen_schedule) / 2
+    fp64 = ctypes.c_double(0.0)
+    library.fractal_gb300_fma_peak(64, ctypes.byref(fp64))
+    fp32 = ctypes.c_double(0.0)
+    library.fractal_gb300_fma_peak(32, ctypes.byref(fp32))
+    # Direct queue: 7 FP64 mul/add per iteration actually computed; a mul or
+    # add issues at the FMA instruction rate, i.e. half the FMA flop peak.
+    direct_achieved = 7.0 * steps_done.value / (direct_ms * 1e-3) / 1e12
+    direct_peak = fp64.value / 2.0
     deep = [stack.keyframes[i] for i in deep_levels]
     flops = 0.0
     library.fractal_set_stats_enabled(1)
@@ -320,23 +354,24 @@ def run_gpu_arm(args) -> int:
         stack.render_host(keyframe, WIDTH, HEIGHT)
         flops += algorithmic_flops(native.stats(library), 32)
     library.fractal_set_stats_enabled(0)
-    precision = 32 if forms["chosen"] == 1 else 64
-    peak = ctypes.c_double(0.0)
-    library.fractal_gb300_fma_peak(precision, ctypes.byref(peak))
-    achieved = flops / (deep_ms * 1e-3) / 1e12
+    deep_achieved = flops / (deep_ms * 1e-3) / 1e12
+    deep_roofline = {"bound": "fp32-fma" if forms["chosen"] == 1 else "fp64-fma", "achieved": deep_achieved,
+                     "peak": fp32.value if forms["chosen"] == 1 else fp64.value, "unit": "TFLOP/s",
+                     "frac": deep_achieved / (fp32.value if forms["chosen"] == 1 else fp64.value),
+                     "launch_ms": deep_ms, "kernel": "floatexp queue (41 deep keyframes)"}
     roofline = {
-        "bound": f"fp{precision}-fma",
-        "achieved": achieved,
-        "peak": peak.value,
+        "bound": "fp64",
+        "achieved": direct_achieved,
+        "peak": direct_peak,
         "unit": "TFLOP/s",
-        "frac": achieved / peak.value if peak.value else None,
+        "frac": direct_achieved / direct_peak if direct_peak else None,
         "traffic": None,
-        "peak_source": f"FP{precision} FMA chains measured on this GPU by fractal_gb300_fma_peak "
+        "peak_source": "FP64 FMA chains measured on this GPU by fractal_gb300_fma_peak, halved for mul/add "
                        "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
-        "kernel": "deep queue (floatexp)" if precision == 32 else "deep render (plain FP64)",
-        "launch_ms": deep_ms,
-        "direct_queue_ms": direct_ms,
-        "direct_pixel_iterations": direct_work,
+        "kernel": "direct_queue_kernel (14 shallow keyframes, the step's critical path)",
+        "launch_ms": direct_ms,
+        "flops_per_unit": "7 FP64 mul/add per computed iteration",
+        "units": int(steps_done.value),
     }
 
     # End to end through the renderer.h ABI: host output buffers, the field
@@ -357,6 +392,9 @@ def run_gpu_arm(args) -> int:
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(native, atlas, levels, step, x, y)
+    if net is not None:
+        library.fractal_gb300_set_cost_network(None)
+        net.close()
     stack.close()
 
     if rank == 0:
@@ -390,13 +428,22 @@ def run_gpu_arm(args) -> int:
                                  "floatexp_chunk": shapes[2], "floatexp_blocks_per_sm": shapes[3]},
                 "launch": "one batched call per step: direct FP64 lane-refill queue (second stream) + "
                           "floatexp queue, replayed as a CUDA graph",
+                "schedule": chosen_schedule,
+                "schedule_ms_per_step": schedule_ms,
+                "smooth_error_vs_plain": smooth_stats,
+                "direct_pixel_iterations": direct_work,
+                "floatexp_roofline": deep_roofline,
                 "l2": "outputs larger than L2 (455 MB field + 455 MB counts per step)",
             },
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": n_levels * pixels * 4,
                     "path": "fractal_render_reference_ex / render_fractal_ex into host memory"},
-            "gpu_launches": args.steps * (2 + (1 if forms["chosen"] == 1 else len(deep_levels))),
+            # Per step: direct coordinates + 4 queue phases; series prologue +
+            # the floatexp queue (learned adds probe, features, 2 GEMMs,
+            # output layer, order); the plain form launches per deep field.
+            "gpu_launches": args.steps * ((6 + (7 if chosen_schedule == "learned" else 1)) if forms["chosen"] == 1
+                                          else 5 + len(deep_levels)),
             "roofline": roofline,
             "cpu_baseline": cpu,
         }

@@ -915,6 +915,7 @@ struct BatchPlan {
     std::vector<FxParams> floatexp;
     std::vector<float> log_zoom;       // per floatexp field (tile features)
     unsigned tile_flags = 0;           // FRACTAL_GB300_BATCH_TILES / _LEARNED / _PROBE
+    bool fast_smooth = false;          // floatexp form: direct frames' smooth value in FP32
     mlp::CostNet* net = nullptr;
     int tiles = 0;
     int feature_rows = 0;
@@ -976,7 +977,7 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
             long long pixels = 0;
             for (int f = 0; f < n; ++f) pixels += static_cast<long long>(fields[i + f].width) * fields[i + f].height;
             check_cuda(launch_direct_batch(fields.data() + i, n, direct_scratch, shapes.direct, spill_entries(pixels),
-                                           direct_stream),
+                                           direct_stream, plan.fast_smooth),
                        "direct batch launch");
         }
     }
@@ -1581,6 +1582,7 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
         ThreadRuntime& rt = thread_runtime();
         cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
         BatchPlan plan;
+        plan.fast_smooth = form == 1;
         append_bytes(plan.key, width);
         append_bytes(plan.key, height);
         append_bytes(plan.key, form);
@@ -1728,6 +1730,7 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
             std::lock_guard<std::mutex> lock(tuned_mutex);
             tuned_shapes[shape_key] = shapes;
         }
+        rt.batch_stream = stream;
         rt.last_shapes[0] = shapes.direct.chunk;
         rt.last_shapes[1] = shapes.direct.blocks_per_sm;
         rt.last_shapes[2] = shapes.floatexp.chunk;
@@ -1783,6 +1786,19 @@ int fractal_gb300_last_tiles(int* tiles, float* cost, uint16_t* features, int ca
             timing_ms[0] = static_cast<double>(ns[2] - ns[0]) * 1e-6;
             timing_ms[1] = static_cast<double>(ns[2] - ns[1]) * 1e-6;
         }
+    });
+}
+
+int fractal_gb300_last_direct_steps(unsigned long long* steps) {
+    return guarded("reading the direct queue's step count failed", [&] {
+        if (!steps) throw Failure{"null step counter"};
+        ThreadRuntime& rt = thread_runtime();
+        if (!rt.scratch[kScratchDirect]) throw Failure{"no direct batch has run on this thread"};
+        check_cuda(cudaStreamSynchronize(rt.batch_stream ? rt.batch_stream : rt.stream), "keyframe batch");
+        check_cuda(cudaStreamSynchronize(rt.side), "keyframe batch");
+        const auto* counters = static_cast<const unsigned long long*>(rt.scratch[kScratchDirect]);
+        check_cuda(cudaMemcpy(steps, counters + 2 * kDirectPhases, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost), "direct step count");
     });
 }
 

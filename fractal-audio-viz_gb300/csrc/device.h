@@ -345,7 +345,7 @@ constexpr int kMaxDirectFields = 64;
 // state so a later phase resumes it bit for bit.
 struct DirectSpill {
     double zr, zi, dr, di, test1, test2;
-    unsigned long long saved_r, saved_i;
+    unsigned long long saved_r, saved_i, mark_r, mark_i;
     int it, check_at, field, local;
 };
 constexpr int kDirectPhases = 4;
@@ -364,6 +364,7 @@ struct DirectBatch {
     int phase;
     int budget;
     int steps;                              // steps between refills
+    int fast_smooth;                        // smooth value in FP32 (floatexp form's direct levels)
     const DirectSpill* spill_in;
     long long spill_in_capacity;
     DirectSpill* spill_out;
@@ -373,7 +374,7 @@ struct DirectBatch {
 // lists of `spill_entries` each (0: one phase, no spilling).
 std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries);
 cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
-                                long long spill_entries, cudaStream_t stream);
+                                long long spill_entries, cudaStream_t stream, bool fast_smooth = false);
 // One direct field with its scratch taken from a fixed array compiled into
 // the library (render_noalloc.cu): no device allocation at all.
 bool launch_direct_noalloc(const DirectParams& params, cudaStream_t stream, std::string& why);

@@ -101,7 +101,8 @@ struct Lane {
     double dr, di;      // derivative (planes with DE only)
     double test1, test2;
     double escape2;
-    unsigned long long saved_r, saved_i;  // cycle probe (Brent)
+    unsigned long long saved_r, saved_i;  // cycle probe (Brent): z at the last power of two
+    unsigned long long mark_r, mark_i;    // and z at the last multiple of 64 steps
     int it;             // completed steps
     int check_at;
     int max_iter;
@@ -272,6 +273,8 @@ __device__ void begin_pixel(const DirectBatch& b, const StartSlot& slot, Lane& l
     l.escape2 = escape_r2_d(p.escape_mode);
     l.saved_r = dbits(l.zr);
     l.saved_i = dbits(l.zi);
+    l.mark_r = l.saved_r;
+    l.mark_i = l.saved_i;
     l.it = 0;
     l.check_at = 1;
     l.max_iter = p.max_iter;
@@ -306,15 +309,28 @@ __device__ void resume_pixel(const DirectBatch& b, const DirectSpill& e, Lane& l
     l.escape2 = escape_r2_d(p.escape_mode);
     l.saved_r = e.saved_r;
     l.saved_i = e.saved_i;
+    l.mark_r = e.mark_r;
+    l.mark_i = e.mark_i;
     l.it = e.it;
     l.check_at = e.check_at;
     l.max_iter = p.max_iter;
     l.stop_at = phase_stop(b, e.it, p.max_iter);
 }
 
+// The smooth value with the logarithms in FP32 (the floatexp form's direct
+// levels): the same formula, within a few float ulps of the FP64 value, at
+// no FP64 cost.  Non-finite |z|^2 keeps the FP64 path.
+__device__ float smooth_value_fast(const DirectParams& p, int iteration, double m2) {
+    if (!is_finite(m2)) return smooth_value(p, iteration, m2);
+    const double safe2 = escape_r2_d(p.escape_mode) + 1.0e-7;
+    const float safe = static_cast<float>(dbits(m2) > dbits(safe2) ? m2 : safe2);
+    const float log_mag = 0.5f * logf(safe);
+    return (static_cast<float>(iteration + 1) - log2f(log_mag)) - static_cast<float>(p.output_bias);
+}
+
 __device__ void finish_parked(const DirectBatch& b, const ParkSlot& e) {
     const DirectParams& p = b.field[e.field];
-    p.out[e.local] = smooth_value(p, e.it, e.m2);
+    p.out[e.local] = b.fast_smooth ? smooth_value_fast(p, e.it, e.m2) : smooth_value(p, e.it, e.m2);
     if (p.counts) p.counts[e.local] = static_cast<std::uint32_t>(e.it + 1);
 }
 
@@ -329,9 +345,11 @@ __device__ void finish_parked(const DirectBatch& b, const ParkSlot& e) {
 //   * the squares zr*zr and zi*zi of the escape test are the next step's
 //     squares, and 2 zr zi is formed as the product zr*zi with its exponent
 //     raised by one (exact for normal numbers; the multiply otherwise);
-//   * an orbit that returns bit for bit to an earlier z (Brent's cycle
-//     probe) repeats forever and can never escape, so it is settled as
-//     interior at once; interior outputs do not depend on z.
+//   * an orbit that returns bit for bit to an earlier z repeats forever and
+//     can never escape, so it is settled as interior at once (interior
+//     outputs do not depend on z); z is kept at every power of two (Brent's
+//     probe, any period) and at every multiple of 64 steps (short periods
+//     found within ~64 steps of the orbit settling).
 // FP64 is the bottleneck on this part (1/64 of the FP32 rate), so a warp
 // never waits on a finished lane: each warp claims chunks of pixels from a
 // device counter over all fields of the batch and refills idle lanes every
@@ -351,6 +369,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
     const long long spilled_in = fresh ? 0 : (total < b.spill_in_capacity ? total : b.spill_in_capacity);
     WarpQueue q{0, 0, 0, 0, 0, false};
     bool active = false;
+    unsigned long long executed = 0;  // steps this lane computed for a pixel
     Lane l;
     l.field = 0;
     l.zr = l.zi = l.rs = l.is = l.pr = l.pi = 0.0;
@@ -405,6 +424,8 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
             if constexpr (!Planes) {
                 if (static_cast<int>(lane_id) < q.parked) finish_parked(b, st.park[lane_id]);
             }
+            for (int o = 16; o > 0; o >>= 1) executed += __shfl_xor_sync(kFull, executed, o);
+            if (lane_id == 0) atomicAdd(b.counter + 2 * kDirectPhases, executed);
             break;
         }
 
@@ -418,6 +439,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
         double m2_at_escape = 0.0;
         for (int s = 0; s < b.steps; ++s) {
             if (!__any_sync(kFull, running)) break;
+            executed += running ? 1u : 0u;
             if constexpr (Planes && has_de) {
                 if (running && b.field[l.field].need_de) {
                     // d' = 2 z d + 1 (parameter plane) or 2 z d (Julia) on the
@@ -463,15 +485,20 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                 continue;
             }
             ++l.it;
-            if ((dbits(l.zr) == l.saved_r && dbits(l.zi) == l.saved_i) || l.it >= l.max_iter) {
+            const unsigned long long br = dbits(l.zr), bi = dbits(l.zi);
+            if ((br == l.saved_r && bi == l.saved_i) || (br == l.mark_r && bi == l.mark_i) || l.it >= l.max_iter) {
                 inside = true;
                 running = false;
                 continue;
             }
             if (l.it == l.check_at) {
-                l.saved_r = dbits(l.zr);
-                l.saved_i = dbits(l.zi);
+                l.saved_r = br;
+                l.saved_i = bi;
                 l.check_at = l.check_at < (1 << 30) ? l.check_at << 1 : l.check_at;
+            }
+            if ((l.it & 63) == 0) {
+                l.mark_r = br;
+                l.mark_i = bi;
             }
             if (l.it >= l.stop_at) {
                 spill = true;
@@ -504,6 +531,8 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                     e.test2 = l.test2;
                     e.saved_r = l.saved_r;
                     e.saved_i = l.saved_i;
+                    e.mark_r = l.mark_r;
+                    e.mark_i = l.mark_i;
                     e.it = l.it;
                     e.check_at = l.check_at;
                     e.field = l.field;
@@ -547,7 +576,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
 // batch's claim counter.
 __global__ void direct_coords_kernel(const __grid_constant__ DirectBatch b) {
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < 2 * kDirectPhases) b.counter[i] = 0ull;
+    if (i <= 2 * kDirectPhases) b.counter[i] = 0ull;  // claims, spill counts, executed steps
     for (int f = 0; f < b.count; ++f) {
         const DirectParams& p = b.field[f];
         const long long span = static_cast<long long>(p.width) + p.height;
@@ -697,10 +726,11 @@ static bool view_meets_interior(const DirectParams& p) {
 }
 
 cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
-                                long long spill_entries, cudaStream_t stream) {
+                                long long spill_entries, cudaStream_t stream, bool fast_smooth) {
     if (count < 1 || count > kMaxDirectFields || !scratch) return cudaErrorInvalidValue;
     DirectBatch b{};
     b.count = count;
+    b.fast_smooth = fast_smooth ? 1 : 0;
     b.counter = static_cast<unsigned long long*>(scratch);
     b.coords = reinterpret_cast<double*>(static_cast<char*>(scratch) + 256);
     b.chunk = shape.chunk > 0 ? shape.chunk : 64;

@@ -69,6 +69,7 @@ struct ThreadRuntime {
     int pinned_shapes[4] = {};  // set by fractal_gb300_set_queue_shapes
     void* costnet = nullptr;    // attached tile-cost network (not owned)
     cudaStream_t tile_stream = nullptr;  // stream of the last tile-scheduled batch
+    cudaStream_t batch_stream = nullptr; // stream of the last keyframe batch
     int last_tiles = 0;
     bool shapes_pinned = false;
     double last_kernel_ms = 0.0;

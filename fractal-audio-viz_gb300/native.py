@@ -303,6 +303,7 @@ _GB300_ABI = (
     ("fractal_gb300_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
     ("fractal_gb300_set_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
     ("fractal_gb300_set_cost_network", ctypes.c_int, (ctypes.c_void_p,)),
+    ("fractal_gb300_last_direct_steps", ctypes.c_int, (ctypes.POINTER(ctypes.c_ulonglong),)),
     ("fractal_gb300_last_tiles", ctypes.c_int,
      (ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
       ctypes.POINTER(ctypes.c_double))),

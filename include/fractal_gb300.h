@@ -318,7 +318,9 @@ typedef struct FractalGb300Keyframe {
  * the second stream joins `stream` before the call's work ends.  Frames are
  * claimed in the order given: put the costliest first.  Per-frame results are
  * those of fractal_gb300_render_reference_device / _render_direct_device with
- * the same arguments. */
+ * the same arguments, except that with form 1 the direct frames' smooth
+ * values take their logarithms in FP32 (iteration counts unchanged, smooth
+ * values within a few float ulps). */
 int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe *frames, int count, int width,
                                           int height, const char *x_center, const char *y_center,
                                           int series_order, int series_block,
@@ -342,6 +344,11 @@ int fractal_gb300_set_cost_network(void *net);
  * timing_ms[0] = makespan, timing_ms[1] = tail.  cost/features/timing_ms may
  * be NULL; capacity is their tile capacity. */
 int fractal_gb300_last_tiles(int *tiles, float *cost, uint16_t *features, int capacity, double *timing_ms);
+
+/* Iterations the direct queue actually computed in the calling thread's last
+ * direct launch (escaped pixels count their escape index, pixels the cycle
+ * probe settled count the steps taken before it did); synchronises. */
+int fractal_gb300_last_direct_steps(unsigned long long *steps);
 
 /* Launch shapes the calling thread's last batch used: direct chunk, direct
  * blocks per SM, floatexp chunk, floatexp blocks per SM (0 = as many as fit). */

@@ -66,10 +66,19 @@ def test_batch_equals_single_keyframe_renders(package, product, form):
     try:
         want_field, want_counts = _singles(stack, form)
         got_field, got_counts = _batch(stack, form)
+        direct = np.array([k.reference is None for k in stack.keyframes])
     finally:
         stack.close()
     np.testing.assert_array_equal(got_counts, want_counts)
-    np.testing.assert_array_equal(got_field, want_field)
+    if form == 0:
+        np.testing.assert_array_equal(got_field, want_field)
+        return
+    # The floatexp form's batch takes the direct frames' smooth logarithms in
+    # FP32: counts identical, smooth values within a few float ulps.
+    np.testing.assert_array_equal(got_field[~direct], want_field[~direct])
+    got = got_field[direct].view(np.float32).astype(np.float64)
+    want = want_field[direct].view(np.float32).astype(np.float64)
+    assert np.all(np.abs(got - want) <= 4e-6 * np.maximum(1.0, np.abs(want))), np.max(np.abs(got - want))
 
 
 def test_batch_graph_replay_order_and_autotune_keep_pixels(package, product):
