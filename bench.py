@@ -334,11 +334,15 @@ def run_gpu_arm(args) -> int:
     plain_ms = timed(0, max(1, args.steps // 2), 1) if forms["chosen"] != 0 else ms
     plain_value = plain_work * max(1, args.steps // 2) / (plain_ms * 1e-3) / 1e9 if forms["chosen"] != 0 else value
 
-    # Each queue timed alone (same launches, one part of the batch).
+    # Each queue timed alone with the step's own launch shapes (same
+    # launches, one part of the batch).
+    pinned = (ctypes.c_int * 4)(*shapes)
+    library.fractal_gb300_set_queue_shapes(pinned, 4)
     direct_ms = timed(forms["chosen"], 2, 1, subset=direct_levels) / 2
     steps_done = ctypes.c_ulonglong(0)
     library.fractal_gb300_last_direct_steps(ctypes.byref(steps_done))
     deep_ms = timed(forms["chosen"], 2, 1, subset=deep_levels[::-1], schedule=chosen_schedule) / 2
+    library.fractal_gb300_set_queue_shapes(None, 0)
     fp64 = ctypes.c_double(0.0)
     library.fractal_gb300_fma_peak(64, ctypes.byref(fp64))
     fp32 = ctypes.c_double(0.0)
@@ -453,6 +457,80 @@ def run_gpu_arm(args) -> int:
     return 0
 
 
+def run_case(name: str) -> int:
+    """One small, fixed piece of the workload for profiler captures (no
+    timing output): the commands in profiles/ run these."""
+    import torch
+
+    package = __graft_entry__._package()
+    library = package.load_library()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    if name == "costnet_predict_20992":
+        net = package.costnet.load_default(library)
+        rows = 20992
+        x = torch.zeros((rows, 320), dtype=torch.int16, device="cuda")
+        out = torch.empty(rows, dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            assert library.fractal_gb300_costnet_predict(net.handle, x.data_ptr(), rows, out.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        net.close()
+        print("ok", name)
+        return 0
+    if name in ("kfp_colour_3840x2160", "aurora_colour_3840x2160"):
+        # A 4K field from the stack's level 30 view, then the colour pass
+        # twice (device buffers in and out).
+        width, height = 3840, 2160
+        levels, step = workload_levels()
+        x, y = centre()
+        stack = package.atlas.KeyframeStack(library, x, y, [levels[30]], step=step)
+        keyframe = stack.keyframes[0]
+        field = torch.empty(width * height, dtype=torch.float32, device="cuda")
+        counts = torch.empty(width * height, dtype=torch.int32, device="cuda")
+        stack.render_device(keyframe, field.data_ptr(), counts.data_ptr(), width, height, form=1,
+                            stream=stream.cuda_stream)
+        rgb = torch.empty(width * height * 3, dtype=torch.uint8, device="cuda")
+        kfp = package.kfp
+        profile = kfp.recipe("seeded16")
+        lut = torch.from_numpy(kfp.palette_lut(profile)).cuda()
+        options = kfp.options(profile)
+        for _ in range(2):
+            if name.startswith("kfp"):
+                status = library.fractal_gb300_colourise_kfp_device(
+                    ctypes.c_void_p(field.data_ptr()), ctypes.c_void_p(rgb.data_ptr()), width, height,
+                    keyframe.max_iter, ctypes.byref(options), ctypes.c_void_p(lut.data_ptr()), lut.shape[0],
+                    ctypes.c_void_p(stream.cuda_stream))
+            else:
+                status = library.fractal_gb300_colourise_device(
+                    ctypes.c_void_p(field.data_ptr()), ctypes.c_void_p(rgb.data_ptr()), width, height,
+                    keyframe.max_iter, 0.3, 0.4, 0.7, 0.5, ctypes.c_void_p(stream.cuda_stream))
+            assert status == 0, package.native.last_error(library)
+        torch.cuda.synchronize()
+        stack.close()
+        print("ok", name)
+        return 0
+    width, height = (960, 540) if name.endswith("960x540") else (WIDTH, HEIGHT)
+    levels, step = workload_levels()
+    x, y = centre()
+    stack = package.atlas.KeyframeStack(library, x, y, levels, step=step)
+    n = len(stack.keyframes)
+    fields = torch.empty((n, width * height), dtype=torch.float32, device="cuda")
+    counts = torch.empty((n, width * height), dtype=torch.int32, device="cuda")
+    targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(n)]
+    direct = [i for i, k in enumerate(stack.keyframes) if k.reference is None]
+    deep = [i for i, k in enumerate(stack.keyframes) if k.reference is not None][::-1]
+    subsets = {"direct_levels_4_13_960x540": direct[4:], "direct_levels_0_3_960x540": direct[:4],
+               "deep_levels_12_960x540": deep[:12], "stack_step_fhd": direct + deep}
+    repeats = 2 if name == "stack_step_fhd" else 1
+    for _ in range(repeats):
+        stack.render_batch_device(targets, width, height, form=1, stream=stream.cuda_stream, order=subsets[name],
+                                  graph=name == "stack_step_fhd")
+    torch.cuda.synchronize()
+    stack.close()
+    print("ok", name)
+    return 0
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     parser.add_argument("--gpus", type=int, default=1)
@@ -461,7 +539,14 @@ def main() -> int:
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--form", choices=["chosen", "plain"], default="chosen")
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--case", default=None,
+                        choices=["direct_levels_4_13_960x540", "direct_levels_0_3_960x540", "deep_levels_12_960x540",
+                                 "stack_step_fhd", "costnet_predict_20992", "kfp_colour_3840x2160",
+                                 "aurora_colour_3840x2160"],
+                        help="run one fixed piece of the workload for a profiler capture and exit")
     args = parser.parse_args()
+    if args.case:
+        return run_case(args.case)
     if args.impl == "reference":
         return run_reference_arm(args)
     return run_gpu_arm(args)

@@ -94,6 +94,9 @@ void* scratch(ThreadRuntime& rt, ScratchSlot slot, std::size_t bytes) {
         rt.scratch[slot] = nullptr;
         rt.capacity[slot] = 0;
         check_cuda(cudaMalloc(&rt.scratch[slot], bytes), "cudaMalloc (scratch)");
+        // Zeroed once: the direct queue's spill entries carry a generation
+        // mark that must not match by accident.
+        check_cuda(cudaMemset(rt.scratch[slot], 0, bytes), "cudaMemset (scratch)");
         rt.capacity[slot] = bytes;
     }
     return rt.scratch[slot];
@@ -1118,6 +1121,12 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
                     s.direct.chunk = chunk;
                     c.push_back(s);
                 }
+                for (int steps : {1, 2, 4}) {
+                    if (steps == (best.direct.steps > 0 ? best.direct.steps : 2)) continue;
+                    BatchShapes s = best;
+                    s.direct.steps = steps;
+                    c.push_back(s);
+                }
             }
             if (both) {
                 for (int d = 1; d < capacity; ++d) {
@@ -1797,8 +1806,12 @@ int fractal_gb300_last_direct_steps(unsigned long long* steps) {
         check_cuda(cudaStreamSynchronize(rt.batch_stream ? rt.batch_stream : rt.stream), "keyframe batch");
         check_cuda(cudaStreamSynchronize(rt.side), "keyframe batch");
         const auto* counters = static_cast<const unsigned long long*>(rt.scratch[kScratchDirect]);
-        check_cuda(cudaMemcpy(steps, counters + 2 * kDirectPhases, sizeof(unsigned long long),
+        check_cuda(cudaMemcpy(steps, counters + kStepsExecuted, sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost), "direct step count");
+        unsigned long long error = 0;
+        check_cuda(cudaMemcpy(&error, counters + kQueueError, sizeof error, cudaMemcpyDeviceToHost),
+                   "direct queue status");
+        if (error) throw Failure{"direct queue: a spilled pixel was never published (render incomplete)"};
     });
 }
 

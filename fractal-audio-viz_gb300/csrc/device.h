@@ -276,6 +276,7 @@ cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stre
 struct QueueShape {
     int chunk = 0;
     int blocks_per_sm = 0;
+    int steps = 0;  // direct queue: steps between refills in its first phase (0 = 2)
 };
 
 constexpr int kMaxFxFields = 64;
@@ -341,14 +342,24 @@ cudaError_t launch_plain_alternate(const AltParams& params, bool planes, bool st
 // A batch of direct fields (one kernel over all of them); the batch struct
 // travels as a __grid_constant__ kernel parameter.
 constexpr int kMaxDirectFields = 64;
-// A pixel that ran past its phase's iteration budget, parked with its whole
-// state so a later phase resumes it bit for bit.
-struct DirectSpill {
+// A pixel that ran past its iteration budget, parked with its whole state
+// so that another warp resumes it bit for bit; `ready` carries the batch's
+// generation once the entry is written.
+struct alignas(128) DirectSpill {
     double zr, zi, dr, di, test1, test2;
     unsigned long long saved_r, saved_i, mark_r, mark_i;
     int it, check_at, field, local;
+    unsigned long long ready;
 };
-constexpr int kDirectPhases = 4;
+// Device counters of a direct batch (at the start of its scratch).
+enum DirectCounter {
+    kClaimFresh = 0,   // pixels claimed
+    kSpillReserved,    // spill slots taken by producers
+    kSpillClaimed,     // spill slots taken by consumers
+    kStepsExecuted,    // iterations computed
+    kQueueError,       // a wait on a spill entry gave up
+    kGeneration,       // batch generation (not reset; bumped per launch)
+};
 struct DirectBatch {
     DirectParams field[kMaxDirectFields];
     long long first[kMaxDirectFields + 1];  // pixel prefix over the batch
@@ -357,21 +368,19 @@ struct DirectBatch {
     int count;
     int chunk;                              // pixels per warp claim
     double* coords;
-    unsigned long long* counter;            // kDirectPhases claim counters, then kDirectPhases spill counts
-    // Phase p claims fresh pixels (p = 0) or the spills of phase p-1, runs
-    // each for at most `budget` more steps (0 = to the cap) and spills the
-    // rest into `spill_out` (capacity entries; when full the lane goes on).
-    int phase;
+    unsigned long long* counter;            // DirectCounter slots
+    // A fresh pixel still running after `budget` steps is spilled (when the
+    // list has room) and resumed, to its end, by whichever warp refills
+    // first: long orbits end up 32 to a warp and start early.
     int budget;
-    int steps;                              // steps between refills
+    int steps;                              // steps between refills (fresh pixels in the warp)
+    int long_steps;                         // steps between refills (only resumed pixels)
     int fast_smooth;                        // smooth value in FP32 (floatexp form's direct levels)
-    const DirectSpill* spill_in;
-    long long spill_in_capacity;
-    DirectSpill* spill_out;
+    DirectSpill* spill;
     long long spill_capacity;
 };
-// Device scratch for one batch: counters, coordinate tables and two spill
-// lists of `spill_entries` each (0: one phase, no spilling).
+// Device scratch for one batch: counters, coordinate tables and a spill list
+// of `spill_entries` (0: no spilling).
 std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries);
 cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
                                 long long spill_entries, cudaStream_t stream, bool fast_smooth = false);

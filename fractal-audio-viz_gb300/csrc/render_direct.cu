@@ -93,6 +93,53 @@ __device__ __forceinline__ unsigned long long dbits(double v) {
     return static_cast<unsigned long long>(__double_as_longlong(v));
 }
 
+// The reference's escape test m2 > R^2 with m2 = RN(a + b), a = zr*zr and
+// b = zi*zi (so a, b >= +0), decided on the bit patterns without an FP64
+// instruction: a lone term above R^2 (or infinite / NaN) escapes, two terms
+// at most R^2/2 cannot, and in between the exact sum is compared with the
+// rounding midpoint above R^2 in integer units of half an ulp of R^2 (ties
+// to even, as the FP64 add rounds).  R^2 is a normal double above 2.
+__device__ __forceinline__ bool sum_exceeds(unsigned long long a, unsigned long long b, unsigned long long r2) {
+    constexpr unsigned long long kMant = (1ull << 52) - 1;
+    constexpr unsigned long long kMag = 0x7fffffffffffffffull;
+    a &= kMag;
+    b &= kMag;
+    if (a < b) {
+        const unsigned long long t = a;
+        a = b;
+        b = t;
+    }
+    if (a > r2) return true;
+    if (a <= r2 - (1ull << 52)) return false;
+    const int er = static_cast<int>(r2 >> 52);
+    const unsigned long long mr = (r2 & kMant) | (1ull << 52);
+    const int ea = static_cast<int>(a >> 52);
+    const unsigned long long big = ((a & kMant) | (1ull << 52)) << (ea - er + 1);
+    int eb = static_cast<int>(b >> 52);
+    unsigned long long mb = b & kMant;
+    if (eb == 0) {
+        eb = 1;
+    } else {
+        mb |= 1ull << 52;
+    }
+    const int shift = eb - er + 1;
+    unsigned long long small;
+    bool below = false;  // bits of b under the unit
+    if (shift >= 0) {
+        small = mb << shift;
+    } else if (shift > -64) {
+        small = mb >> -shift;
+        below = (mb & ((1ull << -shift) - 1)) != 0;
+    } else {
+        small = 0;
+        below = mb != 0;
+    }
+    const unsigned long long sum = big + small;
+    const unsigned long long midpoint = 2 * mr + 1;
+    if (sum != midpoint) return sum > midpoint;
+    return below || (mr & 1) != 0;
+}
+
 // Per-lane state of one pixel in flight.
 struct Lane {
     double zr, zi;      // z_n
@@ -111,10 +158,10 @@ struct Lane {
     int local;          // pixel index inside the field
 };
 
-__device__ __forceinline__ int phase_stop(const DirectBatch& b, int it, int max_iter) {
+// Step at which a fresh pixel is spilled (the cap when spilling is off).
+__device__ __forceinline__ int budget_stop(const DirectBatch& b, int max_iter) {
     if (b.budget <= 0 || b.spill_capacity <= 0) return max_iter;
-    const long long stop = static_cast<long long>(it) + b.budget;
-    return stop < max_iter ? static_cast<int>(stop) : max_iter;
+    return b.budget < max_iter ? b.budget : max_iter;
 }
 
 template <bool Planes>
@@ -176,7 +223,7 @@ struct StartSlot {
     int field, local;
 };
 struct ParkSlot {
-    double m2;
+    double rs, is;  // the escaping step's squares (|z|^2 = rs + is)
     int it, field, local, pad;
 };
 constexpr int kStage = 64;
@@ -278,43 +325,47 @@ __device__ void begin_pixel(const DirectBatch& b, const StartSlot& slot, Lane& l
     l.it = 0;
     l.check_at = 1;
     l.max_iter = p.max_iter;
-    l.stop_at = phase_stop(b, 0, p.max_iter);
+    l.stop_at = budget_stop(b, p.max_iter);
 }
 
-// Resume a spilled pixel of an earlier phase.
+// Resume a spilled pixel (it then runs to its end).  The entry was written
+// by another SM during this launch: read it from L2 (ld.global.cg), never
+// from a possibly stale L1 line.
 template <int Formula>
 __device__ void resume_pixel(const DirectBatch& b, const DirectSpill& e, Lane& l) {
     constexpr bool julia = Formula == kFormulaJulia;
-    const DirectParams& p = b.field[e.field];
-    l.field = e.field;
-    l.local = e.local;
-    l.zr = e.zr;
-    l.zi = e.zi;
+    const int field = __ldcg(&e.field);
+    const int local = __ldcg(&e.local);
+    const DirectParams& p = b.field[field];
+    l.field = field;
+    l.local = local;
+    l.zr = __ldcg(&e.zr);
+    l.zi = __ldcg(&e.zi);
     l.rs = l.zr * l.zr;
     l.is = l.zi * l.zi;
     if (julia) {
         l.pr = p.julia_re;
         l.pi = p.julia_im;
     } else {
-        const int py = e.local / p.width;
-        const int px = e.local - py * p.width;
-        const double* coords = b.coords + b.coord_offset[e.field];
+        const int py = local / p.width;
+        const int px = local - py * p.width;
+        const double* coords = b.coords + b.coord_offset[field];
         l.pr = coords[px];
         l.pi = coords[p.width + py];
     }
-    l.dr = e.dr;
-    l.di = e.di;
-    l.test1 = e.test1;
-    l.test2 = e.test2;
+    l.dr = __ldcg(&e.dr);
+    l.di = __ldcg(&e.di);
+    l.test1 = __ldcg(&e.test1);
+    l.test2 = __ldcg(&e.test2);
     l.escape2 = escape_r2_d(p.escape_mode);
-    l.saved_r = e.saved_r;
-    l.saved_i = e.saved_i;
-    l.mark_r = e.mark_r;
-    l.mark_i = e.mark_i;
-    l.it = e.it;
-    l.check_at = e.check_at;
+    l.saved_r = __ldcg(&e.saved_r);
+    l.saved_i = __ldcg(&e.saved_i);
+    l.mark_r = __ldcg(&e.mark_r);
+    l.mark_i = __ldcg(&e.mark_i);
+    l.it = __ldcg(&e.it);
+    l.check_at = __ldcg(&e.check_at);
     l.max_iter = p.max_iter;
-    l.stop_at = phase_stop(b, e.it, p.max_iter);
+    l.stop_at = p.max_iter;  // resumed pixels run to their end
 }
 
 // The smooth value with the logarithms in FP32 (the floatexp form's direct
@@ -330,7 +381,8 @@ __device__ float smooth_value_fast(const DirectParams& p, int iteration, double 
 
 __device__ void finish_parked(const DirectBatch& b, const ParkSlot& e) {
     const DirectParams& p = b.field[e.field];
-    p.out[e.local] = b.fast_smooth ? smooth_value_fast(p, e.it, e.m2) : smooth_value(p, e.it, e.m2);
+    const double m2 = e.rs + e.is;
+    p.out[e.local] = b.fast_smooth ? smooth_value_fast(p, e.it, m2) : smooth_value(p, e.it, m2);
     if (p.counts) p.counts[e.local] = static_cast<std::uint32_t>(e.it + 1);
 }
 
@@ -361,14 +413,14 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
     WarpStage& st = stages[threadIdx.x >> 5];
     const unsigned lane_id = threadIdx.x & 31u;
     const unsigned below = (1u << lane_id) - 1u;
-    const bool fresh = b.phase == 0;
-    unsigned long long* claim = b.counter + b.phase;
-    unsigned long long* spill_count = b.counter + kDirectPhases + b.phase;
-    const long long total = fresh ? b.first[b.count]
-                                  : static_cast<long long>(*(b.counter + kDirectPhases + b.phase - 1));
-    const long long spilled_in = fresh ? 0 : (total < b.spill_in_capacity ? total : b.spill_in_capacity);
+    unsigned long long* claim = b.counter + kClaimFresh;
+    unsigned long long* reserved = b.counter + kSpillReserved;
+    unsigned long long* taken = b.counter + kSpillClaimed;
+    const unsigned long long generation = *(b.counter + kGeneration);
+    const long long total = b.first[b.count];
     WarpQueue q{0, 0, 0, 0, 0, false};
     bool active = false;
+    bool resumed = false;  // the lane's pixel came from the spill list
     unsigned long long executed = 0;  // steps this lane computed for a pixel
     Lane l;
     l.field = 0;
@@ -382,50 +434,94 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
     l.stop_at = 0;
     l.local = 0;
 
+    unsigned rounds = 0;
     while (true) {
         unsigned idle = __ballot_sync(kFull, !active);
-        if (idle != 0u && fresh) {
+        bool pending = false;  // spilled pixels exist that nobody has taken yet
+        // The spill counters live in L2: look at them every 32nd refill round
+        // (a long pixel waits a few dozen steps at most) or once the fresh
+        // queue is drained, not on every step.
+        const bool poll = (++rounds & 31u) == 0u || q.drained;
+        if (idle != 0u && b.spill_capacity > 0 && poll) {
+            // Spilled (long) pixels first: claim up to one per idle lane.
+            unsigned long long base = 0, got = 0;
+            if (lane_id == 0) {
+                unsigned long long seen = *const_cast<volatile unsigned long long*>(taken);
+                for (int attempt = 0; attempt < 64; ++attempt) {
+                    unsigned long long made = *const_cast<volatile unsigned long long*>(reserved);
+                    if (made > static_cast<unsigned long long>(b.spill_capacity)) {
+                        made = static_cast<unsigned long long>(b.spill_capacity);
+                    }
+                    if (seen >= made) break;
+                    const unsigned long long want = made - seen < static_cast<unsigned long long>(__popc(idle))
+                                                        ? made - seen
+                                                        : static_cast<unsigned long long>(__popc(idle));
+                    const unsigned long long old = atomicCAS(taken, seen, seen + want);
+                    if (old == seen) {
+                        base = seen;
+                        got = want;
+                        break;
+                    }
+                    seen = old;
+                }
+            }
+            base = __shfl_sync(kFull, base, 0);
+            got = __shfl_sync(kFull, got, 0);
+            const int rank = __popc(idle & below);
+            const bool mine = ((idle >> lane_id) & 1u) != 0u && static_cast<unsigned long long>(rank) < got;
+            if (mine) {
+                // The producer reserved this slot before writing it; wait
+                // (bounded) for its generation mark.
+                const DirectSpill& e = b.spill[base + rank];
+                bool ready = false;
+                for (int spin = 0; spin < (1 << 22); ++spin) {
+                    if (*reinterpret_cast<const volatile unsigned long long*>(&e.ready) == generation) {
+                        ready = true;
+                        break;
+                    }
+                }
+                __threadfence();
+                if (ready) {
+                    resume_pixel<Formula>(b, e, l);
+                    active = true;
+                    resumed = true;
+                } else {
+                    atomicExch(b.counter + kQueueError, 1ull);
+                }
+            }
+            idle &= ~__ballot_sync(kFull, mine);
+            pending = got != 0;
+        }
+        if (idle != 0u) {
             const int need = __popc(idle);
             while (q.starts < need && !q.drained) classify<Formula, Planes>(b, q, st, claim, lane_id, below, total);
             const int rank = __popc(idle & below);
-            if (!active && rank < q.starts) {
+            if (((idle >> lane_id) & 1u) != 0u && rank < q.starts) {
                 begin_pixel<Formula>(b, st.start[q.starts - 1 - rank], l);
                 active = true;
+                resumed = false;
             }
             q.starts -= need < q.starts ? need : q.starts;
             __syncwarp();
-        } else if (idle != 0u) {
-            // Resume phase: idle lanes take spilled pixels of the last phase.
-            while (idle != 0u && !q.drained) {
-                if (q.next >= q.end) {
-                    unsigned long long base = 0;
-                    if (lane_id == 0) base = atomicAdd(claim, static_cast<unsigned long long>(b.chunk));
-                    base = __shfl_sync(kFull, base, 0);
-                    if (static_cast<long long>(base) >= spilled_in) {
-                        q.drained = true;
-                        break;
-                    }
-                    q.next = static_cast<long long>(base);
-                    q.end = q.next + b.chunk < spilled_in ? q.next + b.chunk : spilled_in;
-                }
-                const int rank = __popc(idle & below);
-                const bool mine = ((idle >> lane_id) & 1u) != 0u && rank < q.end - q.next;
-                if (mine) {
-                    resume_pixel<Formula>(b, b.spill_in[q.next + rank], l);
-                    active = true;
-                }
-                const unsigned took = __ballot_sync(kFull, mine);
-                q.next += __popc(took);
-                idle &= ~took;
-            }
         }
         if (__ballot_sync(kFull, active) == 0u) {
+            if (pending) continue;
+            // No work in hand: stop unless spilled pixels are waiting.
+            bool waiting = false;
+            if (b.spill_capacity > 0 && lane_id == 0) {
+                unsigned long long made = *const_cast<volatile unsigned long long*>(reserved);
+                if (made > static_cast<unsigned long long>(b.spill_capacity)) {
+                    made = static_cast<unsigned long long>(b.spill_capacity);
+                }
+                waiting = *const_cast<volatile unsigned long long*>(taken) < made;
+            }
+            if (__shfl_sync(kFull, waiting, 0)) continue;
             // Drained: finish what is parked (fewer than 32) and stop.
             if constexpr (!Planes) {
                 if (static_cast<int>(lane_id) < q.parked) finish_parked(b, st.park[lane_id]);
             }
             for (int o = 16; o > 0; o >>= 1) executed += __shfl_xor_sync(kFull, executed, o);
-            if (lane_id == 0) atomicAdd(b.counter + 2 * kDirectPhases, executed);
+            if (lane_id == 0) atomicAdd(b.counter + kStepsExecuted, executed);
             break;
         }
 
@@ -436,8 +532,9 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
         constexpr bool has_de = Formula == kFormulaMandelbrot || Formula == kFormulaJulia;
         bool running = active;
         bool escaped = false, inside = false, spill = false;
-        double m2_at_escape = 0.0;
-        for (int s = 0; s < b.steps; ++s) {
+        double rs_at_escape = 0.0, is_at_escape = 0.0;
+        const int steps = __all_sync(kFull, !active || resumed) ? b.long_steps : b.steps;
+        for (int s = 0; s < steps; ++s) {
             if (!__any_sync(kFull, running)) break;
             executed += running ? 1u : 0u;
             if constexpr (Planes && has_de) {
@@ -465,7 +562,6 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
             const double ni = cross + l.pi;
             const double rs = nr * nr;
             const double is = ni * ni;
-            const double m2 = rs + is;
             if (!running) continue;
             l.zr = nr;
             l.zi = ni;
@@ -473,14 +569,12 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
             l.is = is;
             if constexpr (Planes) {
                 l.test2 = l.test1;
-                l.test1 = m2;
+                l.test1 = rs + is;
             }
-            // m2 > R^2 or not finite.  m2 is a sum of squares (sign bit
-            // clear), so the IEEE order equals the integer order of the bit
-            // patterns, and NaN and infinity compare above every finite R^2.
-            if ((dbits(m2) & 0x7fffffffffffffffull) > dbits(l.escape2)) {
+            if (sum_exceeds(dbits(rs), dbits(is), dbits(l.escape2))) {
                 escaped = true;
-                m2_at_escape = m2;
+                rs_at_escape = rs;
+                is_at_escape = is;
                 running = false;
                 continue;
             }
@@ -505,24 +599,25 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                 running = false;
             }
         }
-        const double m2 = m2_at_escape;
         if (inside) {
             write_inside<Planes>(b.field[l.field], l.local);
             active = false;
         }
         const unsigned spilling = __ballot_sync(kFull, spill);
         if (spilling != 0u) {
-            // Park lanes past the phase budget in the next phase's list (one
-            // atomic per warp); a full list lets them run on here.
+            // Hand lanes past the budget to the spill list (one reservation
+            // per warp, the entry's generation mark written last); a full
+            // list lets them run on here.
+            const int leader = __ffs(spilling) - 1;
             unsigned long long base = 0;
-            if (lane_id == static_cast<unsigned>(__ffs(spilling) - 1)) {
-                base = atomicAdd(spill_count, static_cast<unsigned long long>(__popc(spilling)));
+            if (static_cast<int>(lane_id) == leader) {
+                base = atomicAdd(reserved, static_cast<unsigned long long>(__popc(spilling)));
             }
-            base = __shfl_sync(kFull, base, __ffs(spilling) - 1);
+            base = __shfl_sync(kFull, base, leader);
             if (spill) {
                 const long long slot = static_cast<long long>(base) + __popc(spilling & below);
                 if (slot < b.spill_capacity) {
-                    DirectSpill& e = b.spill_out[slot];
+                    DirectSpill& e = b.spill[slot];
                     e.zr = l.zr;
                     e.zi = l.zi;
                     e.dr = l.dr;
@@ -537,6 +632,8 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                     e.check_at = l.check_at;
                     e.field = l.field;
                     e.local = l.local;
+                    __threadfence();
+                    *reinterpret_cast<volatile unsigned long long*>(&e.ready) = generation;
                     active = false;
                 } else {
                     l.stop_at = l.max_iter;
@@ -545,7 +642,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
         }
         if constexpr (Planes) {
             if (escaped) {
-                write_escape_planes<Formula>(b.field[l.field], l, m2);
+                write_escape_planes<Formula>(b.field[l.field], l, rs_at_escape + is_at_escape);
                 active = false;
             }
         } else {
@@ -553,7 +650,8 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
             if (esc != 0u) {
                 if (escaped) {
                     ParkSlot& slot = st.park[q.parked + __popc(esc & below)];
-                    slot.m2 = m2;
+                    slot.rs = rs_at_escape;
+                    slot.is = is_at_escape;
                     slot.it = l.it;
                     slot.field = l.field;
                     slot.local = l.local;
@@ -576,7 +674,8 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
 // batch's claim counter.
 __global__ void direct_coords_kernel(const __grid_constant__ DirectBatch b) {
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i <= 2 * kDirectPhases) b.counter[i] = 0ull;  // claims, spill counts, executed steps
+    if (i < kGeneration) b.counter[i] = 0ull;
+    if (i == kGeneration) b.counter[i] += 1ull;  // a new mark for this batch's spill entries
     for (int f = 0; f < b.count; ++f) {
         const DirectParams& p = b.field[f];
         const long long span = static_cast<long long>(p.width) + p.height;
@@ -709,7 +808,7 @@ std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long lon
     std::size_t bytes = 256 + doubles * sizeof(double);
     if (spill_entries > 0) {
         bytes = (bytes + 255) / 256 * 256;
-        bytes += 2 * static_cast<std::size_t>(spill_entries) * sizeof(DirectSpill);
+        bytes += static_cast<std::size_t>(spill_entries) * sizeof(DirectSpill);
     }
     return bytes;
 }
@@ -747,37 +846,22 @@ cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scr
         coords += static_cast<long long>(fields[f].width) + fields[f].height;
     }
     b.first[count] = pixels;
-    DirectSpill* lists[2] = {nullptr, nullptr};
     if (spill_entries > 0) {
         const std::size_t head = (256 + static_cast<std::size_t>(coords) * sizeof(double) + 255) / 256 * 256;
-        lists[0] = reinterpret_cast<DirectSpill*>(static_cast<char*>(scratch) + head);
-        lists[1] = lists[0] + spill_entries;
+        b.spill = reinterpret_cast<DirectSpill*>(static_cast<char*>(scratch) + head);
+        b.spill_capacity = spill_entries;
+        b.budget = 256;
     }
+    b.steps = shape.steps > 0 ? shape.steps : 2;
+    b.long_steps = 16;
     int device = 0, sms = 152;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     direct_coords_kernel<<<static_cast<unsigned>((coords + 255) / 256), 256, 0, stream>>>(b);
     cudaError_t status = cudaGetLastError();
     if (status != cudaSuccess) return status;
-    // Iteration budgets of the phases: short pixels finish in phase 0; the
-    // long ones (interior pixels the cycle probe has not settled yet, slow
-    // escapes) are repacked 32 to a warp in the later phases instead of
-    // holding a warp each at the end of the queue.
-    static const int budgets[kDirectPhases] = {256, 1024, 4096, 0};
-    const int phases = spill_entries > 0 ? kDirectPhases : 1;
-    for (int phase = 0; phase < phases; ++phase) {
-        b.phase = phase;
-        b.budget = phase + 1 < phases ? budgets[phase] : 0;
-        b.steps = phase == 0 ? 2 : 16;
-        b.spill_capacity = phase + 1 < phases ? spill_entries : 0;
-        b.spill_in = phase > 0 ? lists[(phase - 1) % 2] : nullptr;
-        b.spill_in_capacity = phase > 0 ? spill_entries : 0;
-        b.spill_out = phase + 1 < phases ? lists[phase % 2] : nullptr;
-        status = planes ? launch_formula<true>(b, formula, sms, shape.blocks_per_sm, stream)
-                        : launch_formula<false>(b, formula, sms, shape.blocks_per_sm, stream);
-        if (status != cudaSuccess) return status;
-    }
-    return cudaSuccess;
+    return planes ? launch_formula<true>(b, formula, sms, shape.blocks_per_sm, stream)
+                  : launch_formula<false>(b, formula, sms, shape.blocks_per_sm, stream);
 }
 
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels, const std::uint8_t* lut,
