@@ -45,6 +45,7 @@ WIDTH, HEIGHT = 1920, 1080
 FACTOR = 8.0
 LEVELS = 55
 SAMPLE_DIVISOR = 4  # CPU sample: every keyframe at 480x270 (1/16 of the pixels)
+E2E_THREADS = 4     # host threads calling the renderer.h ABI in the end-to-end leg
 METRIC = "Gpixel-iter/s on 1e100 FHD atlas, chosen vs plain GPU at ≤1e-4 pixel mismatch"
 
 
@@ -122,6 +123,20 @@ def algorithmic_flops(stats: dict, series_order: int) -> float:
     cubic BLA 60, image series 8 per term per pixel."""
     return (22.0 * stats["exact_steps"] + 14.0 * stats["linear_blocks"] + 60.0 * stats["cubic_blocks"]
             + 8.0 * series_order * stats["series_pixels"])
+
+
+def max_over_ranks(value: float) -> float:
+    """The largest of every rank's value (the job's time is its slowest
+    replica's); the value itself when no process group is running."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def run_reference_arm(args) -> int:
@@ -279,12 +294,7 @@ def run_gpu_arm(args) -> int:
             step_device(form, subset, schedule=schedule)
         stop.record(stream)
         torch.cuda.synchronize()
-        ms = start.elapsed_time(stop)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(start.elapsed_time(stop))
 
     # Launch shapes tuned once per schedule on this batch (graph replay; the
     # shapes change the schedule only, never a pixel).
@@ -382,15 +392,25 @@ def run_gpu_arm(args) -> int:
     # copied back every keyframe.
     # Backend 4 selects the same floatexp form through the ABI; backend 0 is
     # the plain form.
+    # The calls come from E2E_THREADS host threads at once, as the reference
+    # pipeline's prefetch executor makes them (visualizer.py:11541); each
+    # thread has its own stream and scratch in the library, so one thread's
+    # copy-back overlaps another's render.
+    from concurrent.futures import ThreadPoolExecutor
+
     e2e_options = native.RenderOptions(backend=4 if forms["chosen"] == 1 else 0)
     e2e_steps = max(1, args.steps // 2)
-    for keyframe in stack.keyframes[:2]:
+    e2e_order = [stack.keyframes[i] for i in order]
+
+    def render_one(keyframe):
         stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for keyframe in stack.keyframes:
-            stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
-    e2e_s = time.perf_counter() - t0
+
+    with ThreadPoolExecutor(E2E_THREADS) as pool:
+        list(pool.map(render_one, e2e_order[:2 * E2E_THREADS]))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            list(pool.map(render_one, e2e_order))
+        e2e_s = time.perf_counter() - t0
     e2e_value = world * work * e2e_steps / e2e_s / 1e9
 
     cpu = None
@@ -442,7 +462,7 @@ def run_gpu_arm(args) -> int:
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": n_levels * pixels * 4,
-                    "path": "fractal_render_reference_ex / render_fractal_ex into host memory"},
+                    "path": f"fractal_render_reference_ex / render_fractal_ex into host memory, {E2E_THREADS} host threads"},
             # Per step: direct coordinates + 4 queue phases; series prologue +
             # the floatexp queue (learned adds probe, features, 2 GEMMs,
             # output layer, order); the plain form launches per deep field.

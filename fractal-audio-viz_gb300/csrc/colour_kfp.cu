@@ -16,6 +16,9 @@
 // the reference to +-1 LSB per channel.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <limits>
+
 #include <cstdint>
 
 #include "device.h"
@@ -40,6 +43,11 @@ struct KfpDevice {
     float slope_cos, slope_sin, slope_power, slope_ratio;
     int interior[3];
     int lut_size;
+    // FP32 shortcuts of exact double tests (set on the host):
+    float sample_hi;     // smallest float >= max_iter - field_bias
+    int sample_fast;     // field_bias >= 0 and smooth_offset >= 0
+    double inv_iter_div; // 1 / iter_div
+    int lut_shift;       // log2(lut_size) when a power of two, else -1
 };
 
 // A stencil sample is kept as its raw field value sv with the sample equal to
@@ -50,6 +58,11 @@ struct KfpDevice {
 // shifted into the same frame.
 __device__ __forceinline__ float sample(const float* __restrict__ field, const KfpDevice& k, int x, int y) {
     const float v = __ldg(field + static_cast<long long>(y) * k.width + x);
+    // Common case without FP64: a finite value in [0, max_iter - bias) with a
+    // non-negative bias and offset passes through unchanged (v >= 0 makes both
+    // shifted values non-negative; v < sample_hi is the double comparison
+    // against max_iter - bias, exactly, for a float v).
+    if (k.sample_fast && v >= 0.0f && v < k.sample_hi) return v;
     const double shift = k.field_bias_d + k.smooth_offset_d;
     if (!isfinite(v)) return static_cast<float>(fmax(0.0, k.smooth_offset_d) - shift);
     const double biased = static_cast<double>(v) + k.field_bias_d;
@@ -159,7 +172,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     const long long index = static_cast<long long>(y) * k.width + x;
     unsigned char* out = rgb + 3 * index;
     const float raw = __ldg(field + index);
-    if (isfinite(raw) && static_cast<double>(raw) >= static_cast<double>(k.max_iter) - k.field_bias_d) {
+    if (isfinite(raw) && raw >= k.sample_hi) {  // the double test raw >= max_iter - bias, exactly
         out[0] = static_cast<unsigned char>(k.interior[0]);
         out[1] = static_cast<unsigned char>(k.interior[1]);
         out[2] = static_cast<unsigned char>(k.interior[2]);
@@ -237,13 +250,22 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     double palette_value = exact_transfer ? transfer_d : static_cast<double>(transfer);
     if (isnan(palette_value) || palette_value < 0.0) palette_value = 0.0;
     if (k.color_method == 5 || k.color_method == 7 || k.color_method == 8) palette_value = fmin(palette_value, 1024.0);
-    if (k.iter_div != 1.0) palette_value /= k.iter_div;
+    if (k.iter_div != 1.0) palette_value *= k.inv_iter_div;  // within an ulp of the quotient
     const double base = palette_value + k.color_offset;
     float red, green, blue;
     auto palette_rgb = [&](double input, float& o_r, float& o_g, float& o_b) {
         const double size = static_cast<double>(k.lut_size);
-        double position = fmod(input, size);
-        if (position < 0.0) position += size;
+        double position;
+        if (k.lut_shift >= 0) {
+            // Power-of-two palettes: the cyclic position input - size *
+            // floor(input / size) takes only exact operations (scaling by a
+            // power of two, floor, an exact subtraction) and equals fmod's
+            // result shifted into [0, size).
+            position = input - size * floor(ldexp(input, -k.lut_shift));
+        } else {
+            position = fmod(input, size);
+            if (position < 0.0) position += size;
+        }
         const double lower_position = floor(position);
         int lower = static_cast<int>(lower_position);
         lower = lower < 0 ? 0 : (lower > k.lut_size - 1 ? k.lut_size - 1 : lower);
@@ -394,6 +416,18 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
     k.slope_ratio = static_cast<float>(launch.slope_ratio);
     for (int c = 0; c < 3; ++c) k.interior[c] = launch.interior[c];
     k.lut_size = launch.lut_size;
+    {
+        const double threshold = static_cast<double>(launch.max_iter) - launch.field_bias;
+        float hi = static_cast<float>(threshold);
+        if (static_cast<double>(hi) < threshold) hi = std::nextafter(hi, std::numeric_limits<float>::infinity());
+        k.sample_hi = hi;
+    }
+    k.sample_fast = launch.field_bias >= 0.0 && launch.smooth_offset >= 0.0 ? 1 : 0;
+    k.inv_iter_div = 1.0 / launch.iter_div;
+    k.lut_shift = -1;
+    for (int shift = 0; shift < 31; ++shift) {
+        if ((1 << shift) == launch.lut_size) k.lut_shift = shift;
+    }
     const dim3 block(32, 8);
     const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
     const std::size_t shared = static_cast<std::size_t>(launch.lut_size) * 3;

@@ -732,7 +732,7 @@ cudaError_t launch_formula(const DirectBatch& b, int formula, int sms, int block
 // palette index is smooth * ((size-1)/max_iter) formed in double from a
 // float32 scale, truncated and clamped; interior and non-finite pixels are
 // black.  Four pixels per thread: 16 B of field in, 12 B of RGB out.
-__global__ void __launch_bounds__(256) aurora_kernel(const float* __restrict__ field,
+__global__ void __launch_bounds__(1024) aurora_kernel(const float* __restrict__ field,
                                                      std::uint8_t* __restrict__ rgb, long long pixels,
                                                      const std::uint8_t* __restrict__ lut, int lut_size,
                                                      float index_scale, int max_iter, int vector_ok) {
@@ -869,20 +869,24 @@ cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixel
     int device = 0, sms = 152;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const std::size_t shared = static_cast<std::size_t>(lut_size) * 3;
     const long long quads = (pixels + 3) / 4;
-    long long blocks = (quads + 255) / 256;
-    const long long cap = static_cast<long long>(sms) * 8;
+    // The palette is copied into shared memory by every block: with a large
+    // palette (up to 192 KiB) run one 1024-thread block per SM so the copy is
+    // made once per SM, not once per 256 pixels.
+    const int threads = shared > 48 * 1024 ? 1024 : 256;
+    long long blocks = (quads + threads - 1) / threads;
+    const long long cap = static_cast<long long>(sms) * (shared > 48 * 1024 ? 1 : 8);
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    const std::size_t shared = static_cast<std::size_t>(lut_size) * 3;
     if (shared > 48 * 1024) {
         cudaFuncSetAttribute(aurora_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(shared));
     }
     const int vector_ok = (reinterpret_cast<std::uintptr_t>(field) % 16 == 0)
         && (reinterpret_cast<std::uintptr_t>(rgb) % 4 == 0);
-    aurora_kernel<<<static_cast<unsigned>(blocks), 256, shared, stream>>>(field, rgb, pixels, lut, lut_size,
-                                                                          index_scale, max_iter, vector_ok);
+    aurora_kernel<<<static_cast<unsigned>(blocks), threads, shared, stream>>>(field, rgb, pixels, lut, lut_size,
+                                                                              index_scale, max_iter, vector_ok);
     return cudaGetLastError();
 }
 
