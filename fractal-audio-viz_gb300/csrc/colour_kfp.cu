@@ -43,6 +43,14 @@ struct KfpDevice {
     float slope_cos, slope_sin, slope_power, slope_ratio;
     int interior[3];
     int lut_size;
+    // Double-float (hi + lo FP32 pair) copies of the double constants of the
+    // palette position (set on the host).
+    float shift_hi, shift_lo;          // field_bias + smooth_offset
+    float inv_div_hi, inv_div_lo;      // 1 / iter_div
+    float offset_hi, offset_lo;        // color_offset
+    float tmin_hi, tmin_lo;            // transfer_min (ColorMethod 4)
+    float tscale_hi, tscale_lo;        // 1024 / max(transfer_max - transfer_min, 1e-12)
+    int has_div;                       // iter_div != 1
     // FP32 shortcuts of exact double tests (set on the host):
     float sample_hi;     // smallest float >= max_iter - field_bias
     int sample_fast;     // field_bias >= 0 and smooth_offset >= 0
@@ -158,6 +166,54 @@ __device__ __forceinline__ unsigned char dither_byte(float value, int x, int y, 
     return static_cast<unsigned char>(q < 0 ? 0 : (q > 255 ? 255 : q));
 }
 
+// Double-float arithmetic (unevaluated sum hi + lo of two floats, about 48
+// significant bits): Knuth's two-sum and the FMA two-product, after Dekker's
+// double-length arithmetic.  The palette position runs in it on the FP32
+// pipe instead of in FP64 (1/64 of the FP32 rate on this GPU); it is within
+// ~2^-44 relative of the double value, far inside the +-1 LSB colour budget.
+struct Df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ Df two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return Df{s, err};
+}
+
+__device__ __forceinline__ Df df_norm(float hi, float lo) {
+    const float s = __fadd_rn(hi, lo);
+    return Df{s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+
+__device__ __forceinline__ Df df_add(Df x, Df y) {
+    const Df s = two_sum(x.hi, y.hi);
+    return df_norm(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+__device__ __forceinline__ Df df_neg(Df x) { return Df{-x.hi, -x.lo}; }
+
+__device__ __forceinline__ Df df_mul(Df x, Df y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    const float e = fmaf(x.hi, y.hi, -p);
+    return df_norm(p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e)));
+}
+
+__device__ __forceinline__ Df df_scale(Df x, float power_of_two) { return Df{x.hi * power_of_two, x.lo * power_of_two}; }
+
+// floor(hi + lo): a non-integral hi is at least an ulp from the next
+// integer, farther than |lo|; an integral hi adds floor(lo).
+__device__ __forceinline__ Df df_floor(Df x) {
+    const float f = floorf(x.hi);
+    if (f != x.hi) return Df{f, 0.0f};
+    return two_sum(f, floorf(x.lo));
+}
+
+__device__ __forceinline__ float df_value(Df x) { return __fadd_rn(x.hi, x.lo); }
+
+__device__ __forceinline__ bool df_negative(Df x) { return x.hi < 0.0f || (x.hi == 0.0f && x.lo < 0.0f); }
+
 __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
                                                   const KfpDevice k, const unsigned char* __restrict__ lut_global,
                                                   const double* __restrict__ mc_period, const int* __restrict__ mc_type) {
@@ -179,9 +235,9 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         return;
     }
     const float centre = sample(field, k, x, y);
-    const double centre_value = static_cast<double>(centre) + k.field_bias_d + k.smooth_offset_d;
-    const double colour_iter_d = k.flat ? floor(centre_value) : centre_value;
-    const float colour_iter = static_cast<float>(colour_iter_d);
+    const Df centre_value = df_add(Df{centre, 0.0f}, Df{k.shift_hi, k.shift_lo});
+    const Df colour_iter_df = k.flat ? df_floor(centre_value) : centre_value;
+    const float colour_iter = df_value(colour_iter_df);
     float l = centre, r = centre, u = centre, d = centre, tl = centre, tr = centre, bl = centre, br = centre;
     if (k.needs_difference || k.needs_slopes) {
         l = reflected(field, k, x, y, -1, 0, centre);
@@ -217,7 +273,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     float gradient = k.needs_difference ? difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br) : 0.0f;
     float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.width) / 640.0f;
     if (distance < 0.0f) distance = 0.0f;
-    double transfer_d = colour_iter_d;  // kept exact for methods 0, 4 and 6's iteration branch
+    Df transfer_df = colour_iter_df;  // kept in double-float for methods 0, 4 and 6's iteration branch
     bool exact_transfer = k.color_method == 0 || k.color_method == 4;
     float transfer = colour_iter;
     switch (k.color_method) {
@@ -225,15 +281,16 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         case 2: transfer = powf(fmaxf(0.0f, colour_iter), 1.0f / 3.0f); break;
         case 3: transfer = logf(fmaxf(1.0f, colour_iter)); break;
         case 4:
-            transfer_d = 1024.0 * (colour_iter_d - k.transfer_min) / fmax(k.transfer_max - k.transfer_min, 1.0e-12);
-            transfer = static_cast<float>(transfer_d);
+            transfer_df = df_mul(df_add(colour_iter_df, df_neg(Df{k.tmin_hi, k.tmin_lo})),
+                                 Df{k.tscale_hi, k.tscale_lo});
+            transfer = df_value(transfer_df);
             break;
         case 5: transfer = fminf(distance, 1024.0f); break;
         case 6: {
             const float dt = fminf(sqrtf(fmaxf(0.0f, distance)), 1024.0f);
             if (static_cast<double>(dt) > k.iter_div) {
-                transfer_d = centre_value;
-                transfer = static_cast<float>(centre_value);
+                transfer_df = centre_value;
+                transfer = df_value(centre_value);
                 exact_transfer = true;
             } else {
                 transfer = dt;
@@ -247,30 +304,34 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         case 11: transfer = sqrtf(sqrtf(fmaxf(0.0f, colour_iter))); break;
         default: break;
     }
-    double palette_value = exact_transfer ? transfer_d : static_cast<double>(transfer);
-    if (isnan(palette_value) || palette_value < 0.0) palette_value = 0.0;
-    if (k.color_method == 5 || k.color_method == 7 || k.color_method == 8) palette_value = fmin(palette_value, 1024.0);
-    if (k.iter_div != 1.0) palette_value *= k.inv_iter_div;  // within an ulp of the quotient
-    const double base = palette_value + k.color_offset;
+    Df palette_value = exact_transfer ? transfer_df : Df{transfer, 0.0f};
+    if (isnan(palette_value.hi) || isnan(palette_value.lo) || df_negative(palette_value)) palette_value = Df{0.0f, 0.0f};
+    if ((k.color_method == 5 || k.color_method == 7 || k.color_method == 8) && palette_value.hi > 1024.0f) {
+        palette_value = Df{1024.0f, 0.0f};
+    }
+    if (k.has_div) palette_value = df_mul(palette_value, Df{k.inv_div_hi, k.inv_div_lo});
+    const Df base = df_add(palette_value, Df{k.offset_hi, k.offset_lo});
     float red, green, blue;
-    auto palette_rgb = [&](double input, float& o_r, float& o_g, float& o_b) {
-        const double size = static_cast<double>(k.lut_size);
-        double position;
+    auto palette_rgb = [&](Df input, float& o_r, float& o_g, float& o_b) {
+        Df position;
         if (k.lut_shift >= 0) {
-            // Power-of-two palettes: the cyclic position input - size *
-            // floor(input / size) takes only exact operations (scaling by a
-            // power of two, floor, an exact subtraction) and equals fmod's
-            // result shifted into [0, size).
-            position = input - size * floor(ldexp(input, -k.lut_shift));
+            // input - size * floor(input / size): power-of-two scalings are
+            // exact, so this is the cyclic position in [0, size).
+            const float size = static_cast<float>(k.lut_size);
+            const Df turns = df_floor(df_scale(input, 1.0f / size));
+            position = df_add(input, df_neg(df_scale(turns, size)));
         } else {
-            position = fmod(input, size);
-            if (position < 0.0) position += size;
+            const double size = static_cast<double>(k.lut_size);
+            double p = fmod(static_cast<double>(input.hi) + static_cast<double>(input.lo), size);
+            if (p < 0.0) p += size;
+            const float hi = static_cast<float>(p);
+            position = Df{hi, static_cast<float>(p - static_cast<double>(hi))};
         }
-        const double lower_position = floor(position);
-        int lower = static_cast<int>(lower_position);
+        const Df lower_position = df_floor(position);
+        int lower = static_cast<int>(lower_position.hi) + static_cast<int>(lower_position.lo);
         lower = lower < 0 ? 0 : (lower > k.lut_size - 1 ? k.lut_size - 1 : lower);
         if (k.smooth) {
-            float f = static_cast<float>(position - lower_position);
+            float f = df_value(df_add(position, df_neg(lower_position)));
             if (k.inverse_transition) f = 1.0f - f;
             const int upper = (lower + 1) % k.lut_size;
             const float g = 1.0f - f;
@@ -284,7 +345,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         }
     };
     if (k.multi_color) {
-        const double wave_input = k.smooth ? base : floor(base);
+        const double wave_input = static_cast<double>(df_value(k.smooth ? base : df_floor(base)));
         float hs = 0.0f, ss = 0.0f, vs = 0.0f;
         int hc = 0, sc = 0, vc = 0;
         for (int i = 0; i < k.multi_count; ++i) {
@@ -423,6 +484,16 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
         k.sample_hi = hi;
     }
     k.sample_fast = launch.field_bias >= 0.0 && launch.smooth_offset >= 0.0 ? 1 : 0;
+    auto split = [](double v, float& hi, float& lo) {
+        hi = static_cast<float>(v);
+        lo = static_cast<float>(v - static_cast<double>(hi));
+    };
+    split(launch.field_bias + launch.smooth_offset, k.shift_hi, k.shift_lo);
+    split(1.0 / launch.iter_div, k.inv_div_hi, k.inv_div_lo);
+    k.has_div = launch.iter_div != 1.0 ? 1 : 0;
+    split(launch.color_offset, k.offset_hi, k.offset_lo);
+    split(launch.transfer_min, k.tmin_hi, k.tmin_lo);
+    split(1024.0 / std::fmax(launch.transfer_max - launch.transfer_min, 1.0e-12), k.tscale_hi, k.tscale_lo);
     k.inv_iter_div = 1.0 / launch.iter_div;
     k.lut_shift = -1;
     for (int shift = 0; shift < 31; ++shift) {

@@ -178,3 +178,91 @@ def test_tile_queue_static_and_learned_orders_keep_pixels(package, product):
     for field, counts in (static, learned, learned_graph):
         np.testing.assert_array_equal(counts, want_counts)
         np.testing.assert_array_equal(field, want_field)
+
+
+def test_mixed_formula_batch_matches_fixtures_and_singles(package, product):
+    """A batch of uneven fields: Julia, burning ship and tricorn deep views
+    (plain form launches), a Mandelbrot deep view (floatexp queue in form 1)
+    and shallow alternate views (direct queue grouped by formula).  Every
+    frame equals its single-call render; the alternate ones also equal the
+    reference's own fixtures."""
+    import ctypes
+
+    from .conftest import golden_arrays
+
+    native = package.native
+    wanted = ["julia_fixed_1_e9_96x54", "julia_fixed_2_e15_64x36", "burning-ship_e7_96x54", "tricorn_e12_64x36"]
+    cases = [c for c in case_defs.alternate_cases() if c["name"] in wanted]
+    e30 = case_defs.centres()["field_640x360_e30"]
+    cases.append(case_defs._m("mandel_e30", kind="reference", centre=e30, log10_zoom=30.0, width=80, height=45,
+                              max_iter=50_000))
+    handles, frames_meta = [], []
+    try:
+        for case in cases:
+            bits = case_defs.precision_bits(case["centre"]["re"], case["centre"]["im"], case["log10_zoom"])
+            handle = native.create_reference(product, case["centre"]["re"], case["centre"]["im"],
+                                             case_defs.zoom_text(case["log10_zoom"]).encode(), case["max_iter"],
+                                             bits, case["image_series_order"], formula=case["formula"],
+                                             julia=case.get("julia", ("0", "0")))
+            assert handle, native.last_error(product)
+            handles.append(handle)
+            frames_meta.append((case, handle, case_defs.zoom_text(case["log10_zoom"]).encode()))
+        # Shallow views of two alternate references (direct path, by formula).
+        for case, handle, _ in frames_meta[:1] + frames_meta[2:3]:
+            frames_meta.append((dict(case, name=case["name"] + "_shallow", log10_zoom=3.0), handle, b"1000"))
+        for form in (0, 1):
+            bufs = []
+            frames = (native.Keyframe * len(frames_meta))()
+            for i, (case, handle, zoom) in enumerate(frames_meta):
+                w, h = case["width"], case["height"]
+                field = torch.full((w * h,), -1.0, dtype=torch.float32, device="cuda")
+                counts = torch.zeros((w * h,), dtype=torch.int32, device="cuda")
+                bufs.append((field, counts))
+                frames[i].field = field.data_ptr()
+                frames[i].counts = counts.data_ptr()
+                frames[i].zoom_text = zoom
+                frames[i].reference = handle
+                frames[i].max_iter = case["max_iter"]
+            # One size per batch call: group by size.
+            sizes = sorted({(c["width"], c["height"]) for c, _, _ in frames_meta})
+            for w, h in sizes:
+                idx = [i for i, (c, _, _) in enumerate(frames_meta) if (c["width"], c["height"]) == (w, h)]
+                sub = (native.Keyframe * len(idx))(*[frames[i] for i in idx])
+                options = native.RenderOptions()
+                status = product.fractal_gb300_render_keyframes_device(sub, len(idx), w, h, None, None, 3, 256,
+                                                                       ctypes.byref(options), form, 1, None)
+                assert status == 0, native.last_error(product)
+            torch.cuda.synchronize()
+            for (case, handle, zoom), (field, counts) in zip(frames_meta, bufs):
+                w, h = case["width"], case["height"]
+                single_f = torch.full((w * h,), -1.0, dtype=torch.float32, device="cuda")
+                single_c = torch.zeros((w * h,), dtype=torch.int32, device="cuda")
+                options = native.RenderOptions()
+                status = product.fractal_gb300_render_reference_device(
+                    ctypes.c_void_p(single_f.data_ptr()), ctypes.c_void_p(single_c.data_ptr()), w, h, zoom,
+                    ctypes.c_void_p(handle), case["max_iter"], 3, 256, ctypes.byref(options), form, None)
+                assert status == 0, native.last_error(product)
+                torch.cuda.synchronize()
+                np.testing.assert_array_equal(counts.cpu().numpy(), single_c.cpu().numpy(), err_msg=case["name"])
+                if form == 1 and case["name"].endswith("_shallow"):
+                    # The floatexp form's batch takes direct frames' smooth
+                    # logarithms in FP32 (a few float ulps).
+                    got, want = field.cpu().numpy(), single_f.cpu().numpy()
+                    assert np.all(np.abs(got - want) <= 4e-6 * np.maximum(1.0, np.abs(want))), case["name"]
+                else:
+                    np.testing.assert_array_equal(_bits(field), _bits(single_f), err_msg=case["name"])
+                stored = golden_arrays(case["name"]) if case["formula"] != "mandelbrot" else None
+                if stored is not None and not case["name"].endswith("_shallow"):
+                    got = counts.cpu().numpy().view(np.uint32)
+                    want = stored["counts"].copy()
+                    if case["formula"] == "julia":
+                        # Fixture counts are orbit_iteration + 1, and the
+                        # reference's Julia orbit_iteration is the escape
+                        # index itself (not index - 1 as for the parameter
+                        # plane): the escape index is one less.
+                        escaped = (want > 0) & (want < case["max_iter"])
+                        want[escaped] -= 1
+                    np.testing.assert_array_equal(got, want, err_msg=case["name"])
+    finally:
+        for handle in handles:
+            product.fractal_destroy_reference(handle)
