@@ -497,6 +497,29 @@ def run_case(name: str) -> int:
         net.close()
         print("ok", name)
         return 0
+    if name == "atlas_colour_3840x2160":
+        # Two 4K keyframes (levels 30 and 31), then the atlas frame twice.
+        width, height = 3840, 2160
+        levels, step = workload_levels()
+        x, y = centre()
+        stack = package.atlas.KeyframeStack(library, x, y, [levels[30], levels[31]], step=step)
+        fields = torch.empty((2, width * height), dtype=torch.float32, device="cuda")
+        counts = torch.empty((2, width * height), dtype=torch.int32, device="cuda")
+        for i, keyframe in enumerate(stack.keyframes):
+            stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), width, height, form=1,
+                                stream=stream.cuda_stream)
+        caps = [k.max_iter for k in stack.keyframes]
+        rgb = torch.empty(width * height * 3, dtype=torch.uint8, device="cuda")
+        for _ in range(2):
+            status = library.fractal_gb300_atlas_colourise_device(
+                fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
+                rgb.data_ptr(), width, height, 2.0, 0.5, 0, 0.3, 0.4, 0.7, 0.5, None, None,
+                ctypes.c_void_p(stream.cuda_stream))
+            assert status == 0, package.native.last_error(library)
+        torch.cuda.synchronize()
+        stack.close()
+        print("ok", name)
+        return 0
     if name in ("kfp_colour_3840x2160", "aurora_colour_3840x2160"):
         # A 4K field from the stack's level 30 view, then the colour pass
         # twice (device buffers in and out).
@@ -551,6 +574,108 @@ def run_case(name: str) -> int:
     return 0
 
 
+def run_frame_passes(args) -> int:
+    """Per-video-frame passes at 3840x2160 (the song path: atlas keyframes at
+    4K, factor 4): the atlas compositor (aurora RGB8, scalar frame, and the
+    raw KFP frame: composed surface + KFP pass) from two 4K keyframe fields
+    at parent zoom z / child fraction z/4 (the factor-4 ladder; z =
+    --frame-zoom, default 1.7), and the aurora and KFP colour passes of one
+    4K field.  Each pass: 3 warm-up runs,
+    then `--steps` runs timed with CUDA events on the launching stream, an
+    L2 flush (256 MiB write, untimed) before each.  Algorithmic bytes: the
+    source samples the frame needs once (parent crop + child, 4 B each) plus
+    the output (3 B RGB or 4 B float per pixel).  The oracle port times the
+    same atlas frame on the host cores."""
+    import torch
+
+    package = __graft_entry__._package()
+    library = package.load_library()
+    native = package.native
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    width, height = 3840, 2160
+    pixels = width * height
+    levels, step = workload_levels()
+    x, y = centre()
+    pair = [levels[30], levels[31]]
+    stack = package.atlas.KeyframeStack(library, x, y, pair, step=step)
+    fields = torch.empty((2, pixels), dtype=torch.float32, device="cuda")
+    counts = torch.empty((2, pixels), dtype=torch.int32, device="cuda")
+    for i, keyframe in enumerate(stack.keyframes):
+        stack.render_device(keyframe, fields[i].data_ptr(), counts[i].data_ptr(), width, height, form=1,
+                            stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    caps = [k.max_iter for k in stack.keyframes]
+    rgb = torch.empty(pixels * 3, dtype=torch.uint8, device="cuda")
+    frame = torch.empty(pixels, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    interior = (ctypes.c_int * 3)(0, 0, 0)
+    zoom, fraction = args.frame_zoom, args.frame_zoom / 4.0
+    kfp = package.kfp
+    profile = kfp.recipe("seeded16")
+    lut = torch.from_numpy(kfp.palette_lut(profile)).cuda()
+    options = kfp.options(profile)
+    h = ctypes.c_void_p(stream.cuda_stream)
+    passes = {
+        "atlas_colourise": (lambda: library.fractal_gb300_atlas_colourise_device(
+            fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
+            rgb.data_ptr(), width, height, zoom, fraction, 0, 0.3, 0.4, 0.7, 0.5, interior, None, h),
+            pixels * 4 / zoom ** 2 + pixels * 4 + pixels * 3),
+        "atlas_field": (lambda: library.fractal_gb300_atlas_field_device(
+            fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
+            frame.data_ptr(), width, height, zoom, fraction, 1.0, 0.0, 0.0, 0.0, caps[1], 48, h),
+            pixels * 4 / zoom ** 2 + pixels * 4 + pixels * 4),
+        "atlas_kfp_raw": (lambda: library.fractal_gb300_atlas_colourise_kfp_raw_device(
+            fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
+            rgb.data_ptr(), width, height, zoom, fraction, 1.0, caps[1], ctypes.byref(options),
+            ctypes.c_void_p(lut.data_ptr()), lut.shape[0], h),
+            pixels * 4 / zoom ** 2 + pixels * 4 + pixels * 3),
+        "aurora_colour": (lambda: library.fractal_gb300_colourise_device(
+            ctypes.c_void_p(fields[0].data_ptr()), ctypes.c_void_p(rgb.data_ptr()), width, height, caps[0], 0.3,
+            0.4, 0.7, 0.5, h), pixels * 7),
+        "kfp_colour": (lambda: library.fractal_gb300_colourise_kfp_device(
+            ctypes.c_void_p(fields[0].data_ptr()), ctypes.c_void_p(rgb.data_ptr()), width, height, caps[0],
+            ctypes.byref(options), ctypes.c_void_p(lut.data_ptr()), lut.shape[0], h), pixels * 7),
+    }
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"), encoding="ascii"))["hbm_gbs"]
+    results = []
+    with torch.cuda.stream(stream):
+        for name, (call, algorithmic) in passes.items():
+            times = []
+            for i in range(3 + args.steps):
+                flush.fill_(i & 0xFF)
+                start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                start.record(stream)
+                status = call()
+                stop.record(stream)
+                assert status == 0, native.last_error(library)
+                stream.synchronize()
+                if i >= 3:
+                    times.append(start.elapsed_time(stop))
+            ms = statistics.median(times)
+            achieved = algorithmic / (ms * 1e-3) / 1e9
+            results.append({"pass": f"{name}_3840x2160", "ms": round(ms, 4), "algorithmic_bytes": int(algorithmic),
+                            "achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / peak, 4)})
+    # The same atlas frame on the host cores through the oracle port.
+    port = native.load(os.path.join(ROOT, "oracle", "_ref", "liboracle.so"))
+    host = [fields[i].cpu().numpy() for i in range(2)]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    native.atlas_colourise(port, host[0], (width, height), caps[0], host[1], (width, height), caps[1],
+                           (width, height), zoom, fraction, 0, 0.3, 0.4, 0.7, 0.5, interior=(0, 0, 0))
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    native.atlas_colourise(library, host[0], (width, height), caps[0], host[1], (width, height), caps[1],
+                           (width, height), zoom, fraction, 0, 0.3, 0.4, 0.7, 0.5, interior=(0, 0, 0))
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    stack.close()
+    print(json.dumps({"frame_passes": results, "parent_zoom": zoom, "child_fraction": fraction,
+                      "atlas_colourise_cpu_port_ms": round(cpu_ms, 2),
+                      "cpu_cores": cores, "atlas_colourise_e2e_host_buffers_ms": round(e2e_ms, 2),
+                      "levels": [pair[0][0], pair[1][0]], "caps": caps}))
+    return 0
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     parser.add_argument("--gpus", type=int, default=1)
@@ -559,14 +684,20 @@ def main() -> int:
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--form", choices=["chosen", "plain"], default="chosen")
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--frame-passes", action="store_true",
+                        help="time the per-frame 4K passes (atlas compositor, colour) and exit")
+    parser.add_argument("--frame-zoom", type=float, default=1.7,
+                        help="parent zoom of the timed atlas frame (child fraction = zoom / 4)")
     parser.add_argument("--case", default=None,
                         choices=["direct_levels_4_13_960x540", "direct_levels_0_3_960x540", "deep_levels_12_960x540",
                                  "stack_step_fhd", "costnet_predict_20992", "kfp_colour_3840x2160",
-                                 "aurora_colour_3840x2160"],
+                                 "aurora_colour_3840x2160", "atlas_colour_3840x2160"],
                         help="run one fixed piece of the workload for a profiler capture and exit")
     args = parser.parse_args()
     if args.case:
         return run_case(args.case)
+    if args.frame_passes:
+        return run_frame_passes(args)
     if args.impl == "reference":
         return run_reference_arm(args)
     return run_gpu_arm(args)

@@ -631,6 +631,8 @@ namespace {
 struct AuroraCache {
     int max_iter = -1;
     double phase = 0, vocal = 0, pitch = 0;
+    bool accented = false;
+    std::array<std::uint8_t, 9> accents{};
     std::vector<std::uint8_t> rgb;
     int device = -1;
     std::uint8_t* device_lut = nullptr;
@@ -639,7 +641,11 @@ struct AuroraCache {
 
 std::uint8_t colour_byte(double value) { return static_cast<std::uint8_t>(std::clamp(value, 0.0, 255.0)); }
 
-void build_aurora(AuroraCache& cache, int max_iter, double phase, double vocal, double pitch) {
+// aurora_palette_for (renderer.cpp:4841-4923); with `accents` (three RGB
+// triples) the three waves are projected through the accents before the hue
+// rotation.
+void build_aurora(AuroraCache& cache, int max_iter, double phase, double vocal, double pitch,
+                  const std::uint8_t* accents) {
     const int size = std::min(65536, std::max(4096, max_iter * 4));
     std::vector<float> cosine(static_cast<std::size_t>(size)), sine(static_cast<std::size_t>(size));
     const double denominator = std::max(1, size - 1);
@@ -666,6 +672,20 @@ void build_aurora(AuroraCache& cache, int max_iter, double phase, double vocal, 
         double r = (0.5 - 0.5 * (c * rc + s * rs)) * 140.0;
         double g = (0.5 - 0.5 * (c * gc + s * gs)) * 140.0;
         double b = (0.5 - 0.5 * (c * bc + s * bs)) * 140.0;
+        if (accents != nullptr) {
+            const double wr = std::clamp(static_cast<double>(colour_byte(r)) / 140.0, 0.0, 1.0);
+            const double wg = std::clamp(static_cast<double>(colour_byte(g)) / 140.0, 0.0, 1.0);
+            const double wb = std::clamp(static_cast<double>(colour_byte(b)) / 140.0, 0.0, 1.0);
+            const double ar = (wr * static_cast<double>(accents[0]) + wg * static_cast<double>(accents[3])
+                               + wb * static_cast<double>(accents[6])) / 1.8;
+            const double ag = (wr * static_cast<double>(accents[1]) + wg * static_cast<double>(accents[4])
+                               + wb * static_cast<double>(accents[7])) / 1.8;
+            const double ab = (wr * static_cast<double>(accents[2]) + wg * static_cast<double>(accents[5])
+                               + wb * static_cast<double>(accents[8])) / 1.8;
+            r = ar;
+            g = ag;
+            b = ab;
+        }
         if (rotate) {
             // Chroma rotation in YIQ (renderer.cpp:4815-4833).
             const double y = 0.299 * r + 0.587 * g + 0.114 * b;
@@ -688,15 +708,18 @@ void build_aurora(AuroraCache& cache, int max_iter, double phase, double vocal, 
     cache.phase = phase;
     cache.vocal = vocal;
     cache.pitch = pitch;
+    cache.accented = accents != nullptr;
+    if (accents != nullptr) std::copy(accents, accents + 9, cache.accents.begin());
 }
 
 // Returns the device LUT for the parameters; uploads when they change.
 const std::uint8_t* aurora_lut(ThreadRuntime& rt, int max_iter, double phase, double vocal, double pitch,
-                               int& size) {
+                               int& size, const std::uint8_t* accents = nullptr) {
     thread_local AuroraCache cache;
     const bool same = cache.max_iter == max_iter && cache.phase == phase && cache.vocal == vocal
-        && cache.pitch == pitch && !cache.rgb.empty();
-    if (!same) build_aurora(cache, max_iter, phase, vocal, pitch);
+        && cache.pitch == pitch && !cache.rgb.empty() && cache.accented == (accents != nullptr)
+        && (accents == nullptr || std::equal(accents, accents + 9, cache.accents.begin()));
+    if (!same) build_aurora(cache, max_iter, phase, vocal, pitch, accents);
     size = static_cast<int>(cache.rgb.size() / 3);
     if (!same || cache.device != rt.device || cache.device_lut == nullptr) {
         std::uint8_t* lut = static_cast<std::uint8_t*>(scratch(rt, kScratchLut, cache.rgb.size()));
@@ -899,6 +922,230 @@ int kfp_host(const float* field, uint8_t* output, int width, int height, int max
 
 using namespace fgb;
 
+
+// ------------------------------------------------------------ atlas frames
+namespace {
+
+// Validated arguments of one atlas frame: geometry and numbers for
+// launch_atlas, sources and outputs left to the caller.
+struct AtlasRequest {
+    int parent_width, parent_height, parent_max_iter;
+    int child_width, child_height, child_max_iter;
+    bool has_child;
+    int out_width, out_height;
+    double parent_zoom, child_fraction;
+    int palette_max_iter;
+};
+
+AtlasLaunch atlas_geometry(const AtlasRequest& r) {
+    AtlasLaunch a{};
+    a.parent_width = r.parent_width;
+    a.parent_height = r.parent_height;
+    a.parent_max_iter = r.parent_max_iter;
+    a.parent_zoom = r.parent_zoom;
+    a.child_width = r.child_width;
+    a.child_height = r.child_height;
+    a.child_max_iter = r.child_max_iter;
+    a.child_zoom = 1.0;
+    a.out_width = r.out_width;
+    a.out_height = r.out_height;
+    const bool use_child = r.has_child && r.child_fraction > 0.0;
+    a.use_child = use_child;
+    a.full_child = use_child && r.child_fraction >= 0.999999;
+    if (use_child) {
+        a.child_visible_width = std::max(1, static_cast<int>(std::lround(static_cast<double>(r.out_width)
+                                                                         * r.child_fraction)));
+        a.child_visible_height = std::max(1, static_cast<int>(std::lround(static_cast<double>(r.out_height)
+                                                                          * r.child_fraction)));
+    }
+    a.child_left = (r.out_width - a.child_visible_width) / 2;
+    a.child_top = (r.out_height - a.child_visible_height) / 2;
+    return a;
+}
+
+void check_atlas_common(const AtlasRequest& r) {
+    if (!valid_dims(r.parent_width, r.parent_height) || !valid_dims(r.out_width, r.out_height)
+        || !valid_iterations(r.parent_max_iter) || !std::isfinite(r.parent_zoom) || r.parent_zoom <= 0.0
+        || !std::isfinite(r.child_fraction) || r.child_fraction < 0.0 || r.child_fraction > 1.0) {
+        throw Failure{""};
+    }
+}
+
+// fractal_atlas_field_ex's checks and frame constants (renderer.cpp:
+// 18720-18770).
+AtlasLaunch atlas_field_launch(const AtlasRequest& r, double child_zoom, double parent_bias, double child_bias,
+                               double output_bias, int feather) {
+    const char* invalid = "invalid native scalar atlas dimensions";
+    try {
+        check_atlas_common(r);
+    } catch (const Failure&) {
+        throw Failure{invalid};
+    }
+    if (!std::isfinite(child_zoom) || child_zoom <= 0.0 || !std::isfinite(parent_bias) || parent_bias < 0.0
+        || parent_bias > static_cast<double>(r.parent_max_iter) || !std::isfinite(child_bias) || child_bias < 0.0
+        || !std::isfinite(output_bias) || output_bias < 0.0 || feather < 0 || !valid_iterations(r.palette_max_iter)) {
+        throw Failure{invalid};
+    }
+    AtlasLaunch a = atlas_geometry(r);
+    a.mode = kAtlasField;
+    if (a.use_child && (!valid_dims(r.child_width, r.child_height) || !valid_iterations(r.child_max_iter)
+                        || child_bias > static_cast<double>(r.child_max_iter))) {
+        throw Failure{"invalid native scalar atlas child tile"};
+    }
+    const int effective = std::max(r.palette_max_iter, std::max(r.parent_max_iter, a.use_child ? r.child_max_iter : 0));
+    if (!valid_iterations(effective) || output_bias > static_cast<double>(effective)) {
+        throw Failure{"invalid native scalar atlas iteration cap"};
+    }
+    a.parent_bias = parent_bias;
+    a.child_bias = child_bias;
+    a.child_zoom = std::max(child_zoom, 1.0);
+    a.output_bias = output_bias;
+    a.effective_iter = effective;
+    a.feather = a.use_child && !a.full_child
+        ? std::min(feather, std::min(a.child_visible_width / 2, a.child_visible_height / 2)) : 0;
+    return a;
+}
+
+// atlas_colourise_impl's checks and frame constants (renderer.cpp:
+// 19162-19215); the aurora table is uploaded by the caller.
+AtlasLaunch atlas_colour_launch(const AtlasRequest& r, double phase, double vocal, double instrumental, double pitch,
+                                const int* interior_color) {
+    const char* invalid = "invalid native atlas dimensions or controls";
+    try {
+        check_atlas_common(r);
+    } catch (const Failure&) {
+        throw Failure{invalid};
+    }
+    if (r.palette_max_iter < 0 || r.palette_max_iter > kMaxIterations
+        || !valid_colour_controls(phase, vocal, instrumental, pitch)
+        || (interior_color != nullptr
+            && (interior_color[0] < 0 || interior_color[0] > 255 || interior_color[1] < 0 || interior_color[1] > 255
+                || interior_color[2] < 0 || interior_color[2] > 255))) {
+        throw Failure{invalid};
+    }
+    AtlasLaunch a = atlas_geometry(r);
+    a.mode = kAtlasAurora;
+    if (a.use_child && (!valid_dims(r.child_width, r.child_height) || !valid_iterations(r.child_max_iter))) {
+        throw Failure{"invalid native atlas child tile"};
+    }
+    a.palette_iter = std::max(1, std::max(r.palette_max_iter,
+                                          std::max(r.parent_max_iter, a.use_child ? r.child_max_iter : 0)));
+    a.feather = a.use_child && !a.full_child
+        ? std::min(48, std::min(a.child_visible_width / 8, a.child_visible_height / 8)) : 0;
+    for (int c = 0; c < 3; ++c) a.interior[c] = interior_color ? interior_color[c] : 0;
+    return a;
+}
+
+void attach_aurora(ThreadRuntime& rt, AtlasLaunch& a, double phase, double vocal, double pitch,
+                   const std::uint8_t* accents) {
+    int lut_size = 0;
+    a.lut = aurora_lut(rt, a.palette_iter, phase, vocal, pitch, lut_size, accents);
+    a.lut_size = lut_size;
+    a.index_scale = static_cast<float>(lut_size - 1) / static_cast<float>(a.palette_iter);
+}
+
+// Copies host sources (float fields, or RGB8 for kAtlasRgb) into the atlas
+// scratch and points `a` at them; returns the table space that follows.
+void* stage_atlas_sources(ThreadRuntime& rt, AtlasLaunch& a, const void* parent, const void* child) {
+    auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
+    const std::size_t unit = a.mode == kAtlasRgb ? 3 : 4;
+    const std::size_t parent_bytes = a.full_child ? 0 : static_cast<std::size_t>(a.parent_width) * a.parent_height * unit;
+    const std::size_t child_bytes = a.use_child ? static_cast<std::size_t>(a.child_width) * a.child_height * unit : 0;
+    char* base = static_cast<char*>(scratch(rt, kScratchAtlas, up(parent_bytes) + up(child_bytes)
+                                                                   + atlas_table_bytes(a)));
+    if (parent_bytes) {
+        check_cuda(cudaMemcpyAsync(base, parent, parent_bytes, cudaMemcpyHostToDevice, rt.stream), "atlas parent");
+    }
+    if (child_bytes) {
+        check_cuda(cudaMemcpyAsync(base + up(parent_bytes), child, child_bytes, cudaMemcpyHostToDevice, rt.stream),
+                   "atlas child");
+    }
+    if (a.mode == kAtlasRgb) {
+        a.parent_rgb = reinterpret_cast<const std::uint8_t*>(base);
+        a.child_rgb = reinterpret_cast<const std::uint8_t*>(base + up(parent_bytes));
+    } else {
+        a.parent = reinterpret_cast<const float*>(base);
+        a.child = reinterpret_cast<const float*>(base + up(parent_bytes));
+    }
+    return base + up(parent_bytes) + up(child_bytes);
+}
+
+// Copies host sources into the atlas scratch, composes, copies the frame
+// back; `output` is float[W*H] (field) or uint8[W*H*3] (aurora).
+void atlas_from_host(ThreadRuntime& rt, AtlasLaunch& a, const void* parent, const void* child, void* output,
+                     bool field) {
+    void* tables = stage_atlas_sources(rt, a, parent, child);
+    const std::size_t pixels = static_cast<std::size_t>(a.out_width) * a.out_height;
+    const std::size_t out_bytes = field ? pixels * sizeof(float) : pixels * 3;
+    void* device_out = scratch(rt, field ? kScratchField : kScratchRgb, out_bytes);
+    if (field) {
+        a.field_out = static_cast<float*>(device_out);
+    } else {
+        a.rgb = static_cast<std::uint8_t*>(device_out);
+    }
+    check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+    check_cuda(launch_atlas(a, tables, rt.stream), "atlas kernel launch");
+    check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+    check_cuda(cudaMemcpyAsync(output, device_out, out_bytes, cudaMemcpyDeviceToHost, rt.stream),
+               "copy atlas frame to host");
+    check_cuda(cudaStreamSynchronize(rt.stream), "atlas frame");
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+}
+
+// kfp_atlas_seam_feather (renderer.cpp:99-112).
+int kfp_seam_feather(int width, int height) {
+    const int minimum = std::min(width, height);
+    if (minimum <= 0) return 0;
+    const int requested = std::max(2, std::min(64, minimum / 2));
+    return std::min(requested, std::max(0, (minimum - 1) / 2));
+}
+
+// fractal_atlas_colourise_kfp_raw's child checks and surface constants
+// (renderer.cpp:18010-18068); `field_bias` is the KFP field bias.
+AtlasLaunch kfp_surface_launch(const AtlasRequest& r, double child_zoom, int max_iter, double field_bias) {
+    const bool use_child = r.has_child && r.child_fraction > 0.0;
+    if (use_child && (!valid_dims(r.child_width, r.child_height) || !valid_iterations(r.child_max_iter))) {
+        throw Failure{"invalid native raw KFP atlas child tile"};
+    }
+    if (!use_child && r.has_child) throw Failure{"raw KFP atlas child needs a positive visible fraction"};
+    if (!use_child && (r.child_width != 0 || r.child_height != 0 || r.child_max_iter != 0)) {
+        throw Failure{"invalid native raw KFP atlas child absence"};
+    }
+    if (field_bias > static_cast<double>(max_iter)) throw Failure{"native KFP field bias exceeds iteration cap"};
+    AtlasLaunch a = atlas_geometry(r);
+    a.mode = kAtlasKfpSurface;
+    a.full_child = 0;  // the parent is sampled everywhere; the seam runs to the frame edge
+    a.parent_zoom = std::max(r.parent_zoom, 1.0);
+    a.child_zoom = std::max(child_zoom, 1.0);
+    const bool centred = field_bias > 0.0;
+    a.parent_bias = centred ? static_cast<double>(r.parent_max_iter) : 0.0;
+    a.child_bias = centred ? static_cast<double>(r.child_max_iter) : 0.0;
+    a.output_bias = field_bias;
+    a.effective_iter = max_iter;
+    a.feather = use_child ? kfp_seam_feather(a.child_visible_width, a.child_visible_height) : 0;
+    return a;
+}
+
+// The argument checks of fractal_atlas_colourise_kfp_raw (renderer.cpp:
+// 17994-18009), then the surface constants.
+AtlasLaunch kfp_raw_launch(const AtlasRequest& r, double child_zoom, int max_iter, double phase, double vocal,
+                           double instrumental, double pitch, const FractalKfpOptions* options, const uint8_t* lut,
+                           int lut_size) {
+    const char* invalid = "invalid native raw KFP atlas dimensions or controls";
+    try {
+        check_atlas_common(r);
+    } catch (const Failure&) {
+        throw Failure{invalid};
+    }
+    if (!valid_iterations(max_iter) || !std::isfinite(child_zoom) || child_zoom <= 0.0
+        || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut || !valid_kfp(options, lut_size)) {
+        throw Failure{invalid};
+    }
+    return kfp_surface_launch(r, child_zoom, max_iter, options->field_bias);
+}
+
+}  // namespace
 
 // ------------------------------------------------------- keyframe batches
 namespace {
@@ -1414,18 +1661,32 @@ int render_mandelbrot(float* output, int width, int height, const char* zoom_tex
                                 use_perturbation, threads, nullptr);
 }
 
-int fractal_colourise(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
-                      double vocal, double instrumental, double pitch, int threads) {
+}  // extern "C"
+
+namespace {
+
+// colourise_field_impl (renderer.cpp:13771-13826): aurora palette, optional
+// interior colour and accents.
+int colourise_field(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
+                    double vocal, double instrumental, double pitch, int threads, const int* interior_color,
+                    const std::uint8_t* accents) {
     return guarded("native colouriser failed with an unknown exception", [&] {
         if (!field || !output || !valid_dims(width, height) || !valid_iterations(max_iter) || !valid_threads(threads)
-            || !valid_colour_controls(phase, vocal, instrumental, pitch)) {
+            || !valid_colour_controls(phase, vocal, instrumental, pitch)
+            || (interior_color != nullptr
+                && (interior_color[0] < 0 || interior_color[0] > 255 || interior_color[1] < 0
+                    || interior_color[1] > 255 || interior_color[2] < 0 || interior_color[2] > 255))) {
             throw Failure{"invalid native colour dimensions or palette"};
         }
+        const std::uint32_t interior = interior_color == nullptr
+            ? 0u
+            : static_cast<std::uint32_t>(interior_color[0]) | (static_cast<std::uint32_t>(interior_color[1]) << 8)
+                | (static_cast<std::uint32_t>(interior_color[2]) << 16);
         ThreadRuntime& rt = thread_runtime();
         wait_scratch(rt, rt.stream);
         const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
         int lut_size = 0;
-        const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size);
+        const std::uint8_t* lut = aurora_lut(rt, max_iter, phase, vocal, pitch, lut_size, accents);
         float* d_field = static_cast<float*>(scratch(rt, kScratchField, pixels * sizeof(float)));
         std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
         check_cuda(cudaMemcpyAsync(d_field, field, pixels * sizeof(float), cudaMemcpyHostToDevice, rt.stream),
@@ -1433,13 +1694,38 @@ int fractal_colourise(const float* field, uint8_t* output, int width, int height
         const float scale = static_cast<float>(lut_size - 1) / static_cast<float>(max_iter);
         check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
         check_cuda(launch_aurora(d_field, d_rgb, static_cast<long long>(pixels), lut, lut_size, scale, max_iter,
-                                 rt.stream), "aurora kernel launch");
+                                 rt.stream, interior), "aurora kernel launch");
         check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
         check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream), "copy RGB to host");
         check_cuda(cudaStreamSynchronize(rt.stream), "aurora colour");
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
     });
+}
+
+}  // namespace
+
+extern "C" {
+
+int fractal_colourise(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
+                      double vocal, double instrumental, double pitch, int threads) {
+    return colourise_field(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, threads,
+                           nullptr, nullptr);
+}
+
+// fractal_colourise_accents (renderer.cpp:16210-16248): accent palette with
+// an interior colour.
+int fractal_colourise_accents(const float* field, uint8_t* output, int width, int height, int max_iter,
+                              double phase, double vocal, double instrumental, double pitch,
+                              const uint8_t* accents, int interior_red, int interior_green, int interior_blue,
+                              int threads) {
+    if (accents == nullptr) {
+        set_error("ordinary palette accents are required");
+        return 1;
+    }
+    const int interior[3] = {interior_red, interior_green, interior_blue};
+    return colourise_field(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, threads,
+                           interior, accents);
 }
 
 int fractal_colourise_kfp(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
@@ -1933,6 +2219,504 @@ int fractal_gb300_gemm_bf16(const void* a, const void* b, float* c, int m, int n
         check_cuda(cudaMemcpyAsync(&flag, error, sizeof flag, cudaMemcpyDeviceToHost, stream), "GEMM status");
         check_cuda(cudaStreamSynchronize(stream), "GEMM");
         if (flag) throw Failure{"tensor-core GEMM gave up waiting on its barrier"};
+    });
+}
+
+// fractal_atlas_field_ex (renderer.h:815-836, renderer.cpp:18697-18888).
+int fractal_atlas_field_ex(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                           const float* child, int child_width, int child_height, int child_max_iter, float* output,
+                           int output_width, int output_height, double parent_zoom, double child_fraction,
+                           double child_zoom, double parent_field_bias, double child_field_bias,
+                           double output_field_bias, int palette_max_iter, int feather, int threads) {
+    return guarded("native scalar atlas compositor failed with an unknown exception", [&] {
+        if (!parent || !output || !valid_threads(threads)) throw Failure{"invalid native scalar atlas dimensions"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction,
+                             palette_max_iter};
+        AtlasLaunch a = atlas_field_launch(r, child_zoom, parent_field_bias, child_field_bias, output_field_bias,
+                                           feather);
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        atlas_from_host(rt, a, parent, child, output, true);
+    });
+}
+
+// fractal_atlas_field (renderer.h:797-813): the extended call with no
+// biases, child zoom 1 and a 48-pixel seam.
+int fractal_atlas_field(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                        const float* child, int child_width, int child_height, int child_max_iter, float* output,
+                        int output_width, int output_height, double parent_zoom, double child_fraction,
+                        int palette_max_iter, int threads) {
+    return fractal_atlas_field_ex(parent, parent_width, parent_height, parent_max_iter, child, child_width,
+                                  child_height, child_max_iter, output, output_width, output_height, parent_zoom,
+                                  child_fraction, 1.0, 0.0, 0.0, 0.0, palette_max_iter, 48, threads);
+}
+
+}  // extern "C"
+
+namespace {
+
+int atlas_colourise_common(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                           const float* child, int child_width, int child_height, int child_max_iter,
+                           uint8_t* output, int output_width, int output_height, double parent_zoom,
+                           double child_fraction, int palette_max_iter, double phase, double vocal,
+                           double instrumental, double pitch, int threads, const int* interior_color,
+                           const std::uint8_t* accents) {
+    return guarded("native atlas colouriser failed with an unknown exception", [&] {
+        if (!parent || !output || !valid_threads(threads)) throw Failure{"invalid native atlas dimensions or controls"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction,
+                             palette_max_iter};
+        AtlasLaunch a = atlas_colour_launch(r, phase, vocal, instrumental, pitch, interior_color);
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        attach_aurora(rt, a, phase, vocal, pitch, accents);
+        atlas_from_host(rt, a, parent, child, output, false);
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+// fractal_atlas_colourise (renderer.h:997-1017, renderer.cpp:19138-19455).
+int fractal_atlas_colourise(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                            const float* child, int child_width, int child_height, int child_max_iter,
+                            uint8_t* output, int output_width, int output_height, double parent_zoom,
+                            double child_fraction, int palette_max_iter, double phase, double vocal,
+                            double instrumental, double pitch, int threads) {
+    return atlas_colourise_common(parent, parent_width, parent_height, parent_max_iter, child, child_width,
+                                  child_height, child_max_iter, output, output_width, output_height, parent_zoom,
+                                  child_fraction, palette_max_iter, phase, vocal, instrumental, pitch, threads,
+                                  nullptr, nullptr);
+}
+
+// fractal_atlas_colourise_interior (renderer.h:1018-1042): the same with an
+// explicit interior colour.
+int fractal_atlas_colourise_interior(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                                     const float* child, int child_width, int child_height, int child_max_iter,
+                                     uint8_t* output, int output_width, int output_height, double parent_zoom,
+                                     double child_fraction, int palette_max_iter, double phase, double vocal,
+                                     double instrumental, double pitch, int interior_red, int interior_green,
+                                     int interior_blue, int threads) {
+    const int interior[3] = {interior_red, interior_green, interior_blue};
+    return atlas_colourise_common(parent, parent_width, parent_height, parent_max_iter, child, child_width,
+                                  child_height, child_max_iter, output, output_width, output_height, parent_zoom,
+                                  child_fraction, palette_max_iter, phase, vocal, instrumental, pitch, threads,
+                                  interior, nullptr);
+}
+
+// fractal_atlas_colourise_accents (renderer.h:1043-1067): the aurora waves
+// projected through three RGB accents, with an interior colour.
+int fractal_atlas_colourise_accents(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                                    const float* child, int child_width, int child_height, int child_max_iter,
+                                    uint8_t* output, int output_width, int output_height, double parent_zoom,
+                                    double child_fraction, int palette_max_iter, double phase, double vocal,
+                                    double instrumental, double pitch, const uint8_t* accents, int interior_red,
+                                    int interior_green, int interior_blue, int threads) {
+    if (accents == nullptr) {
+        set_error("ordinary palette accents are required");
+        return 1;
+    }
+    const int interior[3] = {interior_red, interior_green, interior_blue};
+    return atlas_colourise_common(parent, parent_width, parent_height, parent_max_iter, child, child_width,
+                                  child_height, child_max_iter, output, output_width, output_height, parent_zoom,
+                                  child_fraction, palette_max_iter, phase, vocal, instrumental, pitch, threads,
+                                  interior, accents);
+}
+
+// fractal_atlas_colourise_kfp_raw (renderer.h:663-687, renderer.cpp:
+// 17969-18304): the parent and child composed into one scalar surface
+// (device, L2-resident at 4K), then one KFP colour pass over it.
+int fractal_atlas_colourise_kfp_raw(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                                    const float* child, int child_width, int child_height, int child_max_iter,
+                                    uint8_t* output, int output_width, int output_height, double parent_zoom,
+                                    double child_fraction, double child_zoom, int max_iter, double phase,
+                                    double vocal, double instrumental, double pitch,
+                                    const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                    int threads) {
+    return guarded("native raw KFP atlas colourizer failed with an unknown exception", [&] {
+        if (!parent || !output || !valid_threads(threads)) {
+            throw Failure{"invalid native raw KFP atlas dimensions or controls"};
+        }
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction, 0};
+        AtlasLaunch a = kfp_raw_launch(r, child_zoom, max_iter, phase, vocal, instrumental, pitch, options, lut,
+                                       lut_size);
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        void* tables = stage_atlas_sources(rt, a, parent, child);
+        const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
+        a.field_out = static_cast<float*>(scratch(rt, kScratchSurface, pixels * sizeof(float)));
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, false);
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        check_cuda(launch_atlas(a, tables, rt.stream), "atlas surface launch");
+        kfp_colour(a.field_out, d_rgb, output_width, output_height, max_iter, *options, in, lut_size, rt, rt.stream);
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
+                   "copy atlas RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "raw KFP atlas");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+// fractal_atlas_colourise_kfp_raw_precise (renderer.h:688-711): the same
+// transfer under its compatibility name.
+int fractal_atlas_colourise_kfp_raw_precise(const float* parent, int parent_width, int parent_height,
+                                            int parent_max_iter, const float* child, int child_width,
+                                            int child_height, int child_max_iter, uint8_t* output, int output_width,
+                                            int output_height, double parent_zoom, double child_fraction,
+                                            double child_zoom, int max_iter, double phase, double vocal,
+                                            double instrumental, double pitch, const FractalKfpOptions* options,
+                                            const uint8_t* lut, int lut_size, int threads) {
+    return fractal_atlas_colourise_kfp_raw(parent, parent_width, parent_height, parent_max_iter, child, child_width,
+                                           child_height, child_max_iter, output, output_width, output_height,
+                                           parent_zoom, child_fraction, child_zoom, max_iter, phase, vocal,
+                                           instrumental, pitch, options, lut, lut_size, threads);
+}
+
+// Device-pointer raw KFP atlas frame (no reference counterpart): device
+// parent, child, LUT and RGB8 output; the surface lives in the thread's
+// scratch.
+int fractal_gb300_atlas_colourise_kfp_raw_device(const float* parent, int parent_width, int parent_height,
+                                                 int parent_max_iter, const float* child, int child_width,
+                                                 int child_height, int child_max_iter, uint8_t* output,
+                                                 int output_width, int output_height, double parent_zoom,
+                                                 double child_fraction, double child_zoom, int max_iter,
+                                                 const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                                 void* stream_handle) {
+    return guarded("device raw KFP atlas failed with an unknown exception", [&] {
+        if (!parent || !output) throw Failure{"invalid native raw KFP atlas dimensions or controls"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction, 0};
+        AtlasLaunch a = kfp_raw_launch(r, child_zoom, max_iter, 0.0, 0.0, 0.0, 0.0, options, lut, lut_size);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        wait_scratch(rt, rt.stream);
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true);
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
+        wait_scratch(rt, stream);
+        a.parent = parent;
+        a.child = child;
+        const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
+        a.field_out = static_cast<float*>(scratch(rt, kScratchSurface, pixels * sizeof(float)));
+        void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
+        check_cuda(launch_atlas(a, tables, stream), "atlas surface launch");
+        kfp_colour(a.field_out, output, output_width, output_height, max_iter, *options, in, lut_size, rt, stream);
+        release_scratch(rt, stream);
+    });
+}
+
+// The raw KFP atlas surface alone (no reference counterpart): the scalar
+// frame fractal_atlas_colourise_kfp_raw colours, into device `surface`, for
+// callers that colour it later or differently.  `field_bias` is the KFP
+// field bias (a positive bias means centred sources).
+int fractal_gb300_atlas_kfp_surface_device(const float* parent, int parent_width, int parent_height,
+                                           int parent_max_iter, const float* child, int child_width,
+                                           int child_height, int child_max_iter, float* surface, int output_width,
+                                           int output_height, double parent_zoom, double child_fraction,
+                                           double child_zoom, int max_iter, double field_bias, void* stream_handle) {
+    return guarded("device raw KFP atlas failed with an unknown exception", [&] {
+        if (!parent || !surface || !std::isfinite(field_bias) || field_bias < 0.0) {
+            throw Failure{"invalid native raw KFP atlas dimensions or controls"};
+        }
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction, 0};
+        try {
+            check_atlas_common(r);
+        } catch (const Failure&) {
+            throw Failure{"invalid native raw KFP atlas dimensions or controls"};
+        }
+        if (!valid_iterations(max_iter) || !std::isfinite(child_zoom) || child_zoom <= 0.0) {
+            throw Failure{"invalid native raw KFP atlas dimensions or controls"};
+        }
+        AtlasLaunch a = kfp_surface_launch(r, child_zoom, max_iter, field_bias);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        wait_scratch(rt, stream);
+        a.parent = parent;
+        a.child = child;
+        a.field_out = surface;
+        void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
+        check_cuda(launch_atlas(a, tables, stream), "atlas surface launch");
+        release_scratch(rt, stream);
+    });
+}
+
+// fractal_crop_field (renderer.h:786-795, renderer.cpp:18631-18696): plain
+// bilinear crop of one field by `zoom_factor` (at least 1) about its centre.
+int fractal_crop_field(const float* source, int source_width, int source_height, float* output, int output_width,
+                       int output_height, double zoom_factor, int threads) {
+    return guarded("native raw-field crop failed with an unknown exception", [&] {
+        if (!source || !output || !valid_dims(source_width, source_height) || !valid_dims(output_width, output_height)
+            || !valid_threads(threads) || !std::isfinite(zoom_factor) || zoom_factor <= 0.0) {
+            throw Failure{"invalid native raw-field crop dimensions"};
+        }
+        AtlasLaunch a{};
+        a.mode = kAtlasCropField;
+        a.parent_width = source_width;
+        a.parent_height = source_height;
+        a.parent_zoom = std::max(zoom_factor, 1.0);
+        a.out_width = output_width;
+        a.out_height = output_height;
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        atlas_from_host(rt, a, source, nullptr, output, true);
+    });
+}
+
+// fractal_crop_rgb (renderer.h:716-725, renderer.cpp:18399-18465): bilinear
+// crop of an RGB8 image.
+int fractal_crop_rgb(const uint8_t* source, int source_width, int source_height, uint8_t* output, int output_width,
+                     int output_height, double zoom_factor, int threads) {
+    return guarded("native RGB crop failed with an unknown exception", [&] {
+        if (!source || !output || !valid_dims(source_width, source_height) || !valid_dims(output_width, output_height)
+            || !valid_threads(threads) || !std::isfinite(zoom_factor) || zoom_factor <= 0.0) {
+            throw Failure{"invalid native RGB crop dimensions"};
+        }
+        zoom_factor = std::max(zoom_factor, 1.0);
+        if (source_width == output_width && source_height == output_height && zoom_factor == 1.0) {
+            // The identity crop (renderer.cpp:18418-18427).
+            std::memcpy(output, source, static_cast<std::size_t>(output_width) * output_height * 3);
+            return;
+        }
+        AtlasLaunch a{};
+        a.mode = kAtlasRgb;
+        a.parent_width = source_width;
+        a.parent_height = source_height;
+        a.parent_zoom = zoom_factor;
+        a.out_width = output_width;
+        a.out_height = output_height;
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        atlas_from_host(rt, a, source, nullptr, output, false);
+    });
+}
+
+// fractal_atlas_composite_rgb (renderer.h:726-741, renderer.cpp:18467-18629):
+// already-coloured parent and child tiles composed with a double smoothstep
+// seam of `feather` pixels.
+int fractal_atlas_composite_rgb(const uint8_t* parent, int parent_width, int parent_height, const uint8_t* child,
+                                int child_width, int child_height, uint8_t* output, int output_width,
+                                int output_height, double parent_zoom, double child_fraction, double child_zoom,
+                                int feather, int threads) {
+    return guarded("native RGB atlas compositor failed with an unknown exception", [&] {
+        if (!parent || !output || !valid_dims(parent_width, parent_height) || !valid_dims(output_width, output_height)
+            || !valid_threads(threads) || !std::isfinite(parent_zoom) || parent_zoom <= 0.0
+            || !std::isfinite(child_fraction) || child_fraction < 0.0 || child_fraction > 1.0
+            || !std::isfinite(child_zoom) || child_zoom <= 0.0 || feather < 0) {
+            throw Failure{"invalid native RGB atlas dimensions or controls"};
+        }
+        const bool use_child = child != nullptr && child_fraction > 0.0;
+        if (!use_child && child_fraction > 0.0) throw Failure{"RGB atlas child data is missing for a positive fraction"};
+        if (!use_child && child != nullptr) throw Failure{"RGB atlas child needs a positive visible fraction"};
+        if (!use_child && (child_width != 0 || child_height != 0)) throw Failure{"invalid native RGB atlas child absence"};
+        if (use_child && (!valid_dims(child_width, child_height) || feather > std::min(output_width, output_height))) {
+            throw Failure{"invalid native RGB atlas child tile"};
+        }
+        const AtlasRequest r{parent_width, parent_height, 1, child_width, child_height, 1, use_child, output_width,
+                             output_height, parent_zoom, child_fraction, 0};
+        AtlasLaunch a = atlas_geometry(r);
+        a.mode = kAtlasRgb;
+        a.full_child = 0;
+        a.parent_zoom = std::max(parent_zoom, 1.0);
+        a.child_zoom = std::max(child_zoom, 1.0);
+        a.feather = use_child ? std::min(feather, std::min(a.child_visible_width, a.child_visible_height)) : 0;
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        atlas_from_host(rt, a, parent, use_child ? child : nullptr, output, false);
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+// crop_colourise_impl (renderer.cpp:18977-19020).
+int crop_colourise_common(const float* source, int source_width, int source_height, uint8_t* output,
+                          int output_width, int output_height, double zoom_factor, int max_iter, double phase,
+                          double vocal, double instrumental, double pitch, int threads, const int* interior_color,
+                          const std::uint8_t* accents) {
+    return guarded("native crop colouriser failed with an unknown exception", [&] {
+        if (!source || !output || !valid_dims(source_width, source_height) || !valid_dims(output_width, output_height)
+            || !valid_iterations(max_iter) || !valid_threads(threads) || !std::isfinite(zoom_factor)
+            || zoom_factor <= 0.0 || !valid_colour_controls(phase, vocal, instrumental, pitch)
+            || (interior_color != nullptr
+                && (interior_color[0] < 0 || interior_color[0] > 255 || interior_color[1] < 0
+                    || interior_color[1] > 255 || interior_color[2] < 0 || interior_color[2] > 255))) {
+            throw Failure{"invalid native crop/colour dimensions or palette"};
+        }
+        AtlasLaunch a{};
+        a.mode = kAtlasCropAurora;
+        a.parent_width = source_width;
+        a.parent_height = source_height;
+        a.parent_max_iter = max_iter;
+        a.parent_zoom = std::max(zoom_factor, 1.0);
+        a.out_width = output_width;
+        a.out_height = output_height;
+        a.palette_iter = max_iter;
+        for (int c = 0; c < 3; ++c) a.interior[c] = interior_color ? interior_color[c] : 0;
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        attach_aurora(rt, a, phase, vocal, pitch, accents);
+        atlas_from_host(rt, a, source, nullptr, output, false);
+    });
+}
+
+// fractal_crop_colourise_kfp's crop, then the KFP pass (renderer.cpp:
+// 17803-17967): the interior-preserving crop biased and encoded by the KFP
+// field bias.
+int crop_colourise_kfp_common(const float* source, int source_width, int source_height, uint8_t* output,
+                              int output_width, int output_height, double zoom_factor, int max_iter, double phase,
+                              double vocal, double instrumental, double pitch, const FractalKfpOptions* options,
+                              const uint8_t* lut, int lut_size, int threads) {
+    return guarded("native KFP crop colourizer failed with an unknown exception", [&] {
+        if (!source || !output || !valid_dims(source_width, source_height) || !valid_dims(output_width, output_height)
+            || !valid_iterations(max_iter) || !valid_threads(threads) || !std::isfinite(zoom_factor)
+            || zoom_factor <= 0.0 || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut
+            || !valid_kfp(options, lut_size)) {
+            throw Failure{"invalid native KFP crop dimensions or controls"};
+        }
+        if (options->field_bias > static_cast<double>(max_iter)) {
+            throw Failure{"native KFP field bias exceeds iteration cap"};
+        }
+        AtlasLaunch a{};
+        a.mode = kAtlasKfpSurface;
+        a.parent_width = source_width;
+        a.parent_height = source_height;
+        a.parent_max_iter = max_iter;
+        a.parent_bias = options->field_bias;
+        a.parent_zoom = std::max(zoom_factor, 1.0);
+        a.out_width = output_width;
+        a.out_height = output_height;
+        a.output_bias = options->field_bias;
+        a.effective_iter = max_iter;
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        void* tables = stage_atlas_sources(rt, a, source, nullptr);
+        const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
+        a.field_out = static_cast<float*>(scratch(rt, kScratchSurface, pixels * sizeof(float)));
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, false);
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        check_cuda(launch_atlas(a, tables, rt.stream), "crop surface launch");
+        kfp_colour(a.field_out, d_rgb, output_width, output_height, max_iter, *options, in, lut_size, rt, rt.stream);
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
+                   "copy crop RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP crop");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+// fractal_crop_colourise (renderer.h:943-956).
+int fractal_crop_colourise(const float* source, int source_width, int source_height, uint8_t* output,
+                           int output_width, int output_height, double zoom_factor, int max_iter, double phase,
+                           double vocal, double instrumental, double pitch, int threads) {
+    return crop_colourise_common(source, source_width, source_height, output, output_width, output_height,
+                                 zoom_factor, max_iter, phase, vocal, instrumental, pitch, threads, nullptr, nullptr);
+}
+
+// fractal_crop_colourise_interior (renderer.h:957-975).
+int fractal_crop_colourise_interior(const float* source, int source_width, int source_height, uint8_t* output,
+                                    int output_width, int output_height, double zoom_factor, int max_iter,
+                                    double phase, double vocal, double instrumental, double pitch, int interior_red,
+                                    int interior_green, int interior_blue, int threads) {
+    const int interior[3] = {interior_red, interior_green, interior_blue};
+    return crop_colourise_common(source, source_width, source_height, output, output_width, output_height,
+                                 zoom_factor, max_iter, phase, vocal, instrumental, pitch, threads, interior, nullptr);
+}
+
+// fractal_crop_colourise_accents (renderer.h:976-996); NULL accents give the
+// plain aurora palette, as in the reference.
+int fractal_crop_colourise_accents(const float* source, int source_width, int source_height, uint8_t* output,
+                                   int output_width, int output_height, double zoom_factor, int max_iter,
+                                   double phase, double vocal, double instrumental, double pitch,
+                                   const uint8_t* accents, int interior_red, int interior_green, int interior_blue,
+                                   int threads) {
+    const int interior[3] = {interior_red, interior_green, interior_blue};
+    return crop_colourise_common(source, source_width, source_height, output, output_width, output_height,
+                                 zoom_factor, max_iter, phase, vocal, instrumental, pitch, threads, interior, accents);
+}
+
+// fractal_crop_colourise_kfp (renderer.h:518-535) and its compatibility name
+// (renderer.h:536-553).
+int fractal_crop_colourise_kfp(const float* source, int source_width, int source_height, uint8_t* output,
+                               int output_width, int output_height, double zoom_factor, int max_iter, double phase,
+                               double vocal, double instrumental, double pitch, const FractalKfpOptions* options,
+                               const uint8_t* lut, int lut_size, int threads) {
+    return crop_colourise_kfp_common(source, source_width, source_height, output, output_width, output_height,
+                                     zoom_factor, max_iter, phase, vocal, instrumental, pitch, options, lut, lut_size,
+                                     threads);
+}
+
+int fractal_crop_colourise_kfp_precise(const float* source, int source_width, int source_height, uint8_t* output,
+                                       int output_width, int output_height, double zoom_factor, int max_iter,
+                                       double phase, double vocal, double instrumental, double pitch,
+                                       const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                       int threads) {
+    return crop_colourise_kfp_common(source, source_width, source_height, output, output_width, output_height,
+                                     zoom_factor, max_iter, phase, vocal, instrumental, pitch, options, lut, lut_size,
+                                     threads);
+}
+
+// Device-pointer atlas frames (no reference counterpart): sources and output
+// in device memory, enqueued on `stream` without synchronising.
+int fractal_gb300_atlas_field_device(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                                     const float* child, int child_width, int child_height, int child_max_iter,
+                                     float* output, int output_width, int output_height, double parent_zoom,
+                                     double child_fraction, double child_zoom, double parent_field_bias,
+                                     double child_field_bias, double output_field_bias, int palette_max_iter,
+                                     int feather, void* stream_handle) {
+    return guarded("device atlas compositor failed with an unknown exception", [&] {
+        if (!parent || !output) throw Failure{"invalid native scalar atlas dimensions"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction,
+                             palette_max_iter};
+        AtlasLaunch a = atlas_field_launch(r, child_zoom, parent_field_bias, child_field_bias, output_field_bias,
+                                           feather);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        wait_scratch(rt, stream);
+        a.parent = parent;
+        a.child = child;
+        a.field_out = output;
+        void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
+        check_cuda(launch_atlas(a, tables, stream), "atlas kernel launch");
+        release_scratch(rt, stream);
+    });
+}
+
+int fractal_gb300_atlas_colourise_device(const float* parent, int parent_width, int parent_height,
+                                         int parent_max_iter, const float* child, int child_width, int child_height,
+                                         int child_max_iter, uint8_t* output, int output_width, int output_height,
+                                         double parent_zoom, double child_fraction, int palette_max_iter,
+                                         double phase, double vocal, double instrumental, double pitch,
+                                         const int* interior_rgb, const uint8_t* accents, void* stream_handle) {
+    return guarded("device atlas colouriser failed with an unknown exception", [&] {
+        if (!parent || !output) throw Failure{"invalid native atlas dimensions or controls"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction,
+                             palette_max_iter};
+        AtlasLaunch a = atlas_colour_launch(r, phase, vocal, instrumental, pitch, interior_rgb);
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        wait_scratch(rt, rt.stream);
+        attach_aurora(rt, a, phase, vocal, pitch, accents);
+        wait_scratch(rt, stream);
+        a.parent = parent;
+        a.child = child;
+        a.rgb = output;
+        void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
+        check_cuda(launch_atlas(a, tables, stream), "atlas kernel launch");
+        release_scratch(rt, stream);
     });
 }
 

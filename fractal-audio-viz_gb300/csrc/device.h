@@ -388,10 +388,82 @@ cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scr
 // the library (render_noalloc.cu): no device allocation at all.
 bool launch_direct_noalloc(const DirectParams& params, cudaStream_t stream, std::string& why);
 std::size_t noalloc_scratch_limit();
+// Atlas compositor (compose.cu): one output frame from a parent and a child
+// keyframe.  Axes map output columns/rows to source indices and weights; the
+// launcher builds them (and the child's edge ramps) on the device.
+struct AtlasAxis {
+    const int* index0;
+    const int* index1;
+    const float* weight;
+};
+struct AtlasTables {
+    struct Axis {
+        int* i0;
+        int* i1;
+        float* w;
+    };
+    Axis parent_x, parent_y, child_x, child_y;
+    float* edge_x;
+    float* edge_y;
+    double* alpha;
+    int parent_x_size, parent_y_size, child_x_size, child_y_size, edge_x_size, edge_y_size, alpha_size;
+};
+enum AtlasMode {
+    kAtlasField = 0,        // fractal_atlas_field_ex: interior-preserving scalar frame
+    kAtlasAurora = 1,       // atlas_colourise_impl: aurora RGB8 frame
+    kAtlasKfpSurface = 2,   // fractal_atlas_colourise_kfp_raw / fractal_crop_colourise_kfp surface
+    kAtlasCropField = 3,    // fractal_crop_field: plain bilinear scalar crop
+    kAtlasRgb = 4,          // fractal_crop_rgb / fractal_atlas_composite_rgb: RGB8 sources
+    kAtlasCropAurora = 5,   // crop_colourise_impl: aurora crop of one field
+};
+struct AtlasLaunch {
+    int mode;  // AtlasMode: field_out (field, KFP surface) or rgb (aurora)
+    const float* parent;
+    int parent_width, parent_height, parent_max_iter;
+    double parent_bias, parent_zoom;
+    const float* child;
+    int child_width, child_height, child_max_iter;
+    double child_bias, child_zoom;
+    const std::uint8_t* parent_rgb;  // kAtlasRgb sources (3 bytes per pixel)
+    const std::uint8_t* child_rgb;
+    int out_width, out_height;
+    int use_child, full_child;
+    int feather;  // edge-ramp width; < 2 = no ramp
+    int child_left, child_top, child_visible_width, child_visible_height;
+    // Filled by launch_atlas.
+    AtlasAxis parent_x, parent_y, child_x, child_y;
+    const float* edge_x;
+    const float* edge_y;
+    const double* alpha;                    // kAtlasRgb: seam alpha by edge distance, feather entries
+    float parent_limit, child_limit;        // smallest float >= cap - bias
+    float parent_bias_hi, parent_bias_lo;   // biases as double-float
+    float child_bias_hi, child_bias_lo;
+    float output_bias_f;
+    int output_bias_exact;                  // output_bias is a float
+    float interior_value;                   // the output value of an interior sample
+    // Scalar output (fractal_atlas_field_ex; the KFP surface, where
+    // output_bias is the KFP field bias and effective_iter the cap) ...
+    float* field_out;
+    double output_bias;
+    int effective_iter;
+    // ... or aurora RGB8 (atlas_colourise_impl) when field_out is null.
+    std::uint8_t* rgb;
+    const std::uint8_t* lut;
+    int lut_size;
+    float index_scale;
+    int palette_iter;
+    int interior[3];
+};
+// Device bytes of the per-frame tables of `launch` (axes and ramps).
+std::size_t atlas_table_bytes(const AtlasLaunch& launch);
+// Builds the tables in `tables` (atlas_table_bytes, 256-byte aligned), then
+// composes the frame: two kernels on `stream`.
+cudaError_t launch_atlas(AtlasLaunch& launch, void* tables, cudaStream_t stream);
+
 // Records %globaltimer into *slot (the time-budget origin of the next kernel).
 cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream);
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels,
                           const std::uint8_t* lut, int lut_size, float index_scale, int max_iter,
-                          cudaStream_t stream);
+                          cudaStream_t stream, std::uint32_t interior = 0);  // interior RGB as 0xBBGGRR
 
 }  // namespace fgb

@@ -735,7 +735,8 @@ cudaError_t launch_formula(const DirectBatch& b, int formula, int sms, int block
 __global__ void __launch_bounds__(1024) aurora_kernel(const float* __restrict__ field,
                                                      std::uint8_t* __restrict__ rgb, long long pixels,
                                                      const std::uint8_t* __restrict__ lut, int lut_size,
-                                                     float index_scale, int max_iter, int vector_ok) {
+                                                     float index_scale, int max_iter, int vector_ok,
+                                                     std::uint32_t interior) {
     extern __shared__ std::uint8_t palette[];
     for (int i = threadIdx.x; i < lut_size * 3; i += blockDim.x) palette[i] = lut[i];
     __syncthreads();
@@ -744,9 +745,9 @@ __global__ void __launch_bounds__(1024) aurora_kernel(const float* __restrict__ 
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
     auto colour = [&](float smooth, std::uint8_t* dst) {
         if (!isfinite(smooth) || smooth >= limit) {
-            dst[0] = 0;
-            dst[1] = 0;
-            dst[2] = 0;
+            dst[0] = static_cast<std::uint8_t>(interior);
+            dst[1] = static_cast<std::uint8_t>(interior >> 8);
+            dst[2] = static_cast<std::uint8_t>(interior >> 16);
             return;
         }
         const double scaled = static_cast<double>(smooth) * static_cast<double>(index_scale);
@@ -865,7 +866,8 @@ cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scr
 }
 
 cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixels, const std::uint8_t* lut,
-                          int lut_size, float index_scale, int max_iter, cudaStream_t stream) {
+                          int lut_size, float index_scale, int max_iter, cudaStream_t stream,
+                          std::uint32_t interior) {
     int device = 0, sms = 152;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -886,7 +888,8 @@ cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixel
     const int vector_ok = (reinterpret_cast<std::uintptr_t>(field) % 16 == 0)
         && (reinterpret_cast<std::uintptr_t>(rgb) % 4 == 0);
     aurora_kernel<<<static_cast<unsigned>(blocks), threads, shared, stream>>>(field, rgb, pixels, lut, lut_size,
-                                                                              index_scale, max_iter, vector_ok);
+                                                                              index_scale, max_iter, vector_ok,
+                                                                              interior);
     return cudaGetLastError();
 }
 

@@ -40,6 +40,8 @@ enum ScratchSlot {
     kScratchQueue,
     kScratchTiles,
     kScratchSeries,
+    kScratchAtlas,
+    kScratchSurface,
     kScratchCount
 };
 

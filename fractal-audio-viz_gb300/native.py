@@ -254,6 +254,71 @@ _ABI = (
      (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
       _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_colourise_accents", ctypes.c_int,
+     (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, _c_u8_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int)),
+    ("fractal_atlas_colourise_kfp_raw", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.POINTER(KfpOptions), _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_atlas_colourise_kfp_raw_precise", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.POINTER(KfpOptions), _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_crop_field", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+      ctypes.c_int)),
+    ("fractal_crop_rgb", ctypes.c_int,
+     (_c_u8_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int)),
+    ("fractal_atlas_composite_rgb", ctypes.c_int,
+     (_c_u8_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int,
+      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int)),
+    ("fractal_crop_colourise", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int)),
+    ("fractal_crop_colourise_interior", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int)),
+    ("fractal_crop_colourise_accents", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _c_u8_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int)),
+    ("fractal_crop_colourise_kfp", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions), _c_u8_p,
+      ctypes.c_int, ctypes.c_int)),
+    ("fractal_crop_colourise_kfp_precise", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions), _c_u8_p,
+      ctypes.c_int, ctypes.c_int)),
+    # Atlas compositor (renderer.h:797-836, 997-1067).
+    ("fractal_atlas_field", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+      ctypes.c_int)),
+    ("fractal_atlas_field_ex", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int)),
+    ("fractal_atlas_colourise", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int)),
+    ("fractal_atlas_colourise_interior", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int)),
+    ("fractal_atlas_colourise_accents", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _c_u8_p, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int, ctypes.c_int)),
 )
 
 # GB300 extensions (include/fractal_gb300.h).  Absent from the CPU oracles.
@@ -296,6 +361,25 @@ _GB300_ABI = (
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
       ctypes.c_void_p)),
+    ("fractal_gb300_atlas_field_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+      ctypes.c_void_p)),
+    ("fractal_gb300_atlas_colourise_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+      _c_u8_p, ctypes.c_void_p)),
+    ("fractal_gb300_atlas_colourise_kfp_raw_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_int, ctypes.POINTER(KfpOptions), ctypes.c_void_p, ctypes.c_int,
+      ctypes.c_void_p)),
+    ("fractal_gb300_atlas_kfp_surface_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+      ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)),
     ("fractal_gb300_render_keyframes_device", ctypes.c_int,
      (ctypes.POINTER(Keyframe), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions), ctypes.c_int,
@@ -533,6 +617,172 @@ def colourise(
         field.ctypes.data_as(_c_float_p), output.ctypes.data_as(_c_u8_p), width, height,
         max_iter, phase, vocal, instrumental, pitch, threads)
     _check(library, status, "fractal_colourise")
+    return output
+
+
+def _float_in(array):
+    if array is None:
+        return None
+    return np.ascontiguousarray(array, dtype=np.float32)
+
+
+def atlas_field(library, parent, parent_shape, parent_max_iter, child, child_shape, child_max_iter,
+                output_shape, parent_zoom, child_fraction, palette_max_iter, *, child_zoom=None,
+                parent_bias=None, child_bias=None, output_bias=None, feather=None, threads=0) -> np.ndarray:
+    """Scalar atlas frame: ``fractal_atlas_field_ex`` (renderer.h:815-836)
+    when any extended argument is given, else ``fractal_atlas_field``.
+    Shapes are (width, height)."""
+    parent, child = _float_in(parent), _float_in(child)
+    width, height = output_shape
+    output = np.empty(width * height, dtype=np.float32)
+    child_ptr = child.ctypes.data_as(_c_float_p) if child is not None else None
+    cw, ch = child_shape if child_shape else (0, 0)
+    extended = any(v is not None for v in (child_zoom, parent_bias, child_bias, output_bias, feather))
+    if extended:
+        status = library.fractal_atlas_field_ex(
+            parent.ctypes.data_as(_c_float_p), parent_shape[0], parent_shape[1], parent_max_iter, child_ptr, cw,
+            ch, child_max_iter, output.ctypes.data_as(_c_float_p), width, height, parent_zoom, child_fraction,
+            1.0 if child_zoom is None else child_zoom, parent_bias or 0.0, child_bias or 0.0, output_bias or 0.0,
+            palette_max_iter, 48 if feather is None else feather, threads)
+    else:
+        status = library.fractal_atlas_field(
+            parent.ctypes.data_as(_c_float_p), parent_shape[0], parent_shape[1], parent_max_iter, child_ptr, cw,
+            ch, child_max_iter, output.ctypes.data_as(_c_float_p), width, height, parent_zoom, child_fraction,
+            palette_max_iter, threads)
+    _check(library, status, "fractal_atlas_field")
+    return output
+
+
+def atlas_colourise(library, parent, parent_shape, parent_max_iter, child, child_shape, child_max_iter,
+                    output_shape, parent_zoom, child_fraction, palette_max_iter, phase, vocal, instrumental,
+                    pitch, *, interior=None, accents=None, threads=0) -> np.ndarray:
+    """Aurora atlas frame (renderer.h:997-1067): ``fractal_atlas_colourise``,
+    ``_interior`` (interior RGB given) or ``_accents`` (accents given)."""
+    parent, child = _float_in(parent), _float_in(child)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    child_ptr = child.ctypes.data_as(_c_float_p) if child is not None else None
+    cw, ch = child_shape if child_shape else (0, 0)
+    common = (parent.ctypes.data_as(_c_float_p), parent_shape[0], parent_shape[1], parent_max_iter, child_ptr, cw,
+              ch, child_max_iter, output.ctypes.data_as(_c_u8_p), width, height, parent_zoom, child_fraction,
+              palette_max_iter, phase, vocal, instrumental, pitch)
+    if accents is not None:
+        accents = np.ascontiguousarray(accents, dtype=np.uint8).reshape(9)
+        red, green, blue = interior if interior is not None else (0, 0, 0)
+        status = library.fractal_atlas_colourise_accents(*common, accents.ctypes.data_as(_c_u8_p), red, green,
+                                                         blue, threads)
+    elif interior is not None:
+        status = library.fractal_atlas_colourise_interior(*common, *interior, threads)
+    else:
+        status = library.fractal_atlas_colourise(*common, threads)
+    _check(library, status, "fractal_atlas_colourise")
+    return output
+
+
+def atlas_colourise_kfp_raw(library, parent, parent_shape, parent_max_iter, child, child_shape, child_max_iter,
+                            output_shape, parent_zoom, child_fraction, child_zoom, max_iter, options, lut,
+                            colour=(0.0, 0.0, 0.0, 0.5), threads=0) -> np.ndarray:
+    """``fractal_atlas_colourise_kfp_raw`` (renderer.h:663-687): parent and
+    child composed into one scalar surface, then one KFP pass.  `options` is
+    a KfpOptions block, `lut` the N x 3 palette."""
+    parent, child = _float_in(parent), _float_in(child)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    child_ptr = child.ctypes.data_as(_c_float_p) if child is not None else None
+    cw, ch = child_shape if child_shape else (0, 0)
+    status = library.fractal_atlas_colourise_kfp_raw(
+        parent.ctypes.data_as(_c_float_p), parent_shape[0], parent_shape[1], parent_max_iter, child_ptr, cw, ch,
+        child_max_iter, output.ctypes.data_as(_c_u8_p), width, height, parent_zoom, child_fraction, child_zoom,
+        max_iter, *colour, ctypes.byref(options), lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
+    _check(library, status, "fractal_atlas_colourise_kfp_raw")
+    return output
+
+
+def crop_field(library, source, source_shape, output_shape, zoom, threads=0) -> np.ndarray:
+    """``fractal_crop_field`` (renderer.h:786-795): plain bilinear crop."""
+    source = np.ascontiguousarray(source, dtype=np.float32)
+    width, height = output_shape
+    output = np.empty(width * height, dtype=np.float32)
+    status = library.fractal_crop_field(source.ctypes.data_as(_c_float_p), source_shape[0], source_shape[1],
+                                        output.ctypes.data_as(_c_float_p), width, height, zoom, threads)
+    _check(library, status, "fractal_crop_field")
+    return output
+
+
+def crop_rgb(library, source, source_shape, output_shape, zoom, threads=0) -> np.ndarray:
+    """``fractal_crop_rgb`` (renderer.h:716-725)."""
+    source = np.ascontiguousarray(source, dtype=np.uint8)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_crop_rgb(source.ctypes.data_as(_c_u8_p), source_shape[0], source_shape[1],
+                                      output.ctypes.data_as(_c_u8_p), width, height, zoom, threads)
+    _check(library, status, "fractal_crop_rgb")
+    return output
+
+
+def atlas_composite_rgb(library, parent, parent_shape, child, child_shape, output_shape, parent_zoom,
+                        child_fraction, child_zoom, feather, threads=0) -> np.ndarray:
+    """``fractal_atlas_composite_rgb`` (renderer.h:726-741): coloured parent
+    and child tiles composed with a smoothstep seam."""
+    parent = np.ascontiguousarray(parent, dtype=np.uint8)
+    child = None if child is None else np.ascontiguousarray(child, dtype=np.uint8)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    cw, ch = child_shape if child is not None else (0, 0)
+    status = library.fractal_atlas_composite_rgb(
+        parent.ctypes.data_as(_c_u8_p), parent_shape[0], parent_shape[1],
+        child.ctypes.data_as(_c_u8_p) if child is not None else None, cw, ch, output.ctypes.data_as(_c_u8_p),
+        width, height, parent_zoom, child_fraction, child_zoom, feather, threads)
+    _check(library, status, "fractal_atlas_composite_rgb")
+    return output
+
+
+def crop_colourise(library, source, source_shape, output_shape, zoom, max_iter, phase, vocal, instrumental, pitch,
+                   *, interior=None, accents=None, threads=0) -> np.ndarray:
+    """Aurora crop (renderer.h:943-996): ``fractal_crop_colourise``,
+    ``_interior`` or ``_accents``."""
+    source = np.ascontiguousarray(source, dtype=np.float32)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    common = (source.ctypes.data_as(_c_float_p), source_shape[0], source_shape[1], output.ctypes.data_as(_c_u8_p),
+              width, height, zoom, max_iter, phase, vocal, instrumental, pitch)
+    if accents is not None:
+        accents = np.ascontiguousarray(accents, dtype=np.uint8).reshape(9)
+        status = library.fractal_crop_colourise_accents(*common, accents.ctypes.data_as(_c_u8_p),
+                                                        *(interior or (0, 0, 0)), threads)
+    elif interior is not None:
+        status = library.fractal_crop_colourise_interior(*common, *interior, threads)
+    else:
+        status = library.fractal_crop_colourise(*common, threads)
+    _check(library, status, "fractal_crop_colourise")
+    return output
+
+
+def crop_colourise_kfp(library, source, source_shape, output_shape, zoom, max_iter, options, lut,
+                       colour=(0.0, 0.0, 0.0, 0.5), threads=0) -> np.ndarray:
+    """``fractal_crop_colourise_kfp`` (renderer.h:518-535)."""
+    source = np.ascontiguousarray(source, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    width, height = output_shape
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_crop_colourise_kfp(
+        source.ctypes.data_as(_c_float_p), source_shape[0], source_shape[1], output.ctypes.data_as(_c_u8_p), width,
+        height, zoom, max_iter, *colour, ctypes.byref(options), lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
+    _check(library, status, "fractal_crop_colourise_kfp")
+    return output
+
+
+def colourise_accents(library, field, width, height, max_iter, phase, vocal, instrumental, pitch, accents,
+                      interior=(0, 0, 0), threads=0) -> np.ndarray:
+    """``fractal_colourise_accents`` (renderer.h:426-440)."""
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    accents = np.ascontiguousarray(accents, dtype=np.uint8).reshape(9)
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_colourise_accents(
+        field.ctypes.data_as(_c_float_p), output.ctypes.data_as(_c_u8_p), width, height, max_iter, phase, vocal,
+        instrumental, pitch, accents.ctypes.data_as(_c_u8_p), *interior, threads)
+    _check(library, status, "fractal_colourise_accents")
     return output
 
 

@@ -222,6 +222,133 @@ int fractal_colourise_kfp_precise(const float *field, uint8_t *output, int width
                                   int max_iter, double phase, double vocal, double instrumental,
                                   double pitch, const FractalKfpOptions *options,
                                   const uint8_t *lut, int lut_size, int threads);
+/* renderer.h:426-440: aurora palette projected through three RGB accents
+ * (9 bytes), with an interior colour.  NULL accents fail with "ordinary palette accents are required". */
+int fractal_colourise_accents(const float *field, uint8_t *output, int width, int height, int max_iter,
+                              double phase, double vocal, double instrumental, double pitch,
+                              const uint8_t *accents, int interior_red, int interior_green,
+                              int interior_blue, int threads);
+
+/* Atlas compositor: one output frame from a parent keyframe field and the
+ * next, deeper child field.  The parent is cropped by `parent_zoom` about its
+ * centre and resampled bilinearly; the child fills the centred rectangle of
+ * `child_fraction` of the frame, feathered by a smoothstep at its edges.
+ * Bilinear samples keep interior: an interior weight >= 1/2 gives interior,
+ * otherwise the exterior corners are renormalised.  Host buffers; the frame
+ * is composed on the GPU and copied back. */
+
+/* renderer.h:797-813: scalar frame (no biases, child zoom 1, 48-px seam). */
+int fractal_atlas_field(const float *parent, int parent_width, int parent_height, int parent_max_iter,
+                        const float *child, int child_width, int child_height, int child_max_iter,
+                        float *output, int output_width, int output_height, double parent_zoom,
+                        double child_fraction, int palette_max_iter, int threads);
+/* renderer.h:815-836: scalar frame with field biases (value + bias is the
+ * true smooth count), child crop zoom and seam width. */
+int fractal_atlas_field_ex(const float *parent, int parent_width, int parent_height, int parent_max_iter,
+                           const float *child, int child_width, int child_height, int child_max_iter,
+                           float *output, int output_width, int output_height, double parent_zoom,
+                           double child_fraction, double child_zoom, double parent_field_bias,
+                           double child_field_bias, double output_field_bias, int palette_max_iter,
+                           int feather, int threads);
+/* renderer.h:997-1017: the frame coloured with the aurora palette (seam
+ * min(48, visible/8), blended in RGB). */
+int fractal_atlas_colourise(const float *parent, int parent_width, int parent_height, int parent_max_iter,
+                            const float *child, int child_width, int child_height, int child_max_iter,
+                            uint8_t *output, int output_width, int output_height, double parent_zoom,
+                            double child_fraction, int palette_max_iter, double phase, double vocal,
+                            double instrumental, double pitch, int threads);
+/* renderer.h:1018-1042: the same with an explicit interior colour. */
+int fractal_atlas_colourise_interior(const float *parent, int parent_width, int parent_height,
+                                     int parent_max_iter, const float *child, int child_width,
+                                     int child_height, int child_max_iter, uint8_t *output,
+                                     int output_width, int output_height, double parent_zoom,
+                                     double child_fraction, int palette_max_iter, double phase,
+                                     double vocal, double instrumental, double pitch, int interior_red,
+                                     int interior_green, int interior_blue, int threads);
+/* renderer.h:1043-1067: accent palette and interior colour. */
+int fractal_atlas_colourise_accents(const float *parent, int parent_width, int parent_height,
+                                    int parent_max_iter, const float *child, int child_width,
+                                    int child_height, int child_max_iter, uint8_t *output,
+                                    int output_width, int output_height, double parent_zoom,
+                                    double child_fraction, int palette_max_iter, double phase,
+                                    double vocal, double instrumental, double pitch,
+                                    const uint8_t *accents, int interior_red, int interior_green,
+                                    int interior_blue, int threads);
+
+/* renderer.h:660-687: raw KFP atlas frame.  The parent (crop by
+ * parent_zoom) and the child (visible rectangle of child_fraction, crop by
+ * child_zoom) are composed into one scalar surface encoded relative to the
+ * options' field_bias (a positive bias means each source is stored relative
+ * to its own cap), with a smoothstep seam inside the child rectangle; one
+ * KFP pass then colours the surface, so differences and slopes stay
+ * continuous across the seam. */
+int fractal_atlas_colourise_kfp_raw(const float *parent, int parent_width, int parent_height,
+                                    int parent_max_iter, const float *child, int child_width,
+                                    int child_height, int child_max_iter, uint8_t *output,
+                                    int output_width, int output_height, double parent_zoom,
+                                    double child_fraction, double child_zoom, int max_iter,
+                                    double phase, double vocal, double instrumental, double pitch,
+                                    const FractalKfpOptions *options, const uint8_t *lut,
+                                    int lut_size, int threads);
+/* renderer.h:688-711: compatibility name of the same call. */
+int fractal_atlas_colourise_kfp_raw_precise(const float *parent, int parent_width, int parent_height,
+                                            int parent_max_iter, const float *child, int child_width,
+                                            int child_height, int child_max_iter, uint8_t *output,
+                                            int output_width, int output_height, double parent_zoom,
+                                            double child_fraction, double child_zoom, int max_iter,
+                                            double phase, double vocal, double instrumental,
+                                            double pitch, const FractalKfpOptions *options,
+                                            const uint8_t *lut, int lut_size, int threads);
+
+/* Crops of one source by a zoom factor (at least 1) about its centre,
+ * resampled bilinearly to the output size. */
+/* renderer.h:786-795: plain bilinear crop of a scalar field. */
+int fractal_crop_field(const float *source, int source_width, int source_height, float *output,
+                       int output_width, int output_height, double zoom_factor, int threads);
+/* renderer.h:716-725: bilinear crop of an RGB8 image. */
+int fractal_crop_rgb(const uint8_t *source, int source_width, int source_height, uint8_t *output,
+                     int output_width, int output_height, double zoom_factor, int threads);
+/* renderer.h:726-741: coloured parent and child tiles composed per frame
+ * (child crop by child_zoom in the centred rectangle of child_fraction, a
+ * smoothstep seam of `feather` pixels). */
+int fractal_atlas_composite_rgb(const uint8_t *parent, int parent_width, int parent_height,
+                                const uint8_t *child, int child_width, int child_height,
+                                uint8_t *output, int output_width, int output_height,
+                                double parent_zoom, double child_fraction, double child_zoom,
+                                int feather, int threads);
+/* renderer.h:943-956: interior-preserving crop coloured with the aurora
+ * palette. */
+int fractal_crop_colourise(const float *source, int source_width, int source_height, uint8_t *output,
+                           int output_width, int output_height, double zoom_factor, int max_iter,
+                           double phase, double vocal, double instrumental, double pitch, int threads);
+/* renderer.h:957-975: with an interior colour. */
+int fractal_crop_colourise_interior(const float *source, int source_width, int source_height,
+                                    uint8_t *output, int output_width, int output_height,
+                                    double zoom_factor, int max_iter, double phase, double vocal,
+                                    double instrumental, double pitch, int interior_red,
+                                    int interior_green, int interior_blue, int threads);
+/* renderer.h:976-996: with accents (NULL: the plain palette) and an
+ * interior colour. */
+int fractal_crop_colourise_accents(const float *source, int source_width, int source_height,
+                                   uint8_t *output, int output_width, int output_height,
+                                   double zoom_factor, int max_iter, double phase, double vocal,
+                                   double instrumental, double pitch, const uint8_t *accents,
+                                   int interior_red, int interior_green, int interior_blue,
+                                   int threads);
+/* renderer.h:518-535: interior-preserving crop encoded by the KFP field
+ * bias, then one KFP pass. */
+int fractal_crop_colourise_kfp(const float *source, int source_width, int source_height,
+                               uint8_t *output, int output_width, int output_height,
+                               double zoom_factor, int max_iter, double phase, double vocal,
+                               double instrumental, double pitch, const FractalKfpOptions *options,
+                               const uint8_t *lut, int lut_size, int threads);
+/* renderer.h:536-553: compatibility name of the same call. */
+int fractal_crop_colourise_kfp_precise(const float *source, int source_width, int source_height,
+                                       uint8_t *output, int output_width, int output_height,
+                                       double zoom_factor, int max_iter, double phase, double vocal,
+                                       double instrumental, double pitch,
+                                       const FractalKfpOptions *options, const uint8_t *lut,
+                                       int lut_size, int threads);
 
 /* ---------------------------------------------------------------------
  * Part 2: GB300 extensions (no counterpart in the reference)
@@ -277,6 +404,47 @@ int fractal_gb300_colourise_kfp_device(const float *field, uint8_t *rgb, int wid
 int fractal_gb300_colourise_device(const float *field, uint8_t *rgb, int width, int height,
                                    int max_iter, double phase, double vocal, double instrumental,
                                    double pitch, void *stream);
+
+/* Atlas frames (fractal_atlas_field_ex / fractal_atlas_colourise_*) from
+ * device parent and child fields into device output; `interior_rgb` (three
+ * ints, or NULL for black) and `accents` (9 bytes, or NULL for the plain
+ * aurora palette) are host memory. */
+int fractal_gb300_atlas_field_device(const float *parent, int parent_width, int parent_height,
+                                     int parent_max_iter, const float *child, int child_width,
+                                     int child_height, int child_max_iter, float *output,
+                                     int output_width, int output_height, double parent_zoom,
+                                     double child_fraction, double child_zoom,
+                                     double parent_field_bias, double child_field_bias,
+                                     double output_field_bias, int palette_max_iter, int feather,
+                                     void *stream);
+int fractal_gb300_atlas_colourise_device(const float *parent, int parent_width, int parent_height,
+                                         int parent_max_iter, const float *child, int child_width,
+                                         int child_height, int child_max_iter, uint8_t *output,
+                                         int output_width, int output_height, double parent_zoom,
+                                         double child_fraction, int palette_max_iter, double phase,
+                                         double vocal, double instrumental, double pitch,
+                                         const int *interior_rgb, const uint8_t *accents,
+                                         void *stream);
+
+/* Raw KFP atlas frame from device parent/child fields and a device LUT
+ * into device RGB8 (fractal_atlas_colourise_kfp_raw without the colour
+ * controls it ignores). */
+int fractal_gb300_atlas_colourise_kfp_raw_device(const float *parent, int parent_width,
+                                                 int parent_height, int parent_max_iter,
+                                                 const float *child, int child_width, int child_height,
+                                                 int child_max_iter, uint8_t *output, int output_width,
+                                                 int output_height, double parent_zoom,
+                                                 double child_fraction, double child_zoom, int max_iter,
+                                                 const FractalKfpOptions *options, const uint8_t *lut,
+                                                 int lut_size, void *stream);
+/* The scalar surface of the raw KFP atlas frame alone, into device
+ * `surface` (output_width x output_height floats), for `field_bias`. */
+int fractal_gb300_atlas_kfp_surface_device(const float *parent, int parent_width, int parent_height,
+                                           int parent_max_iter, const float *child, int child_width,
+                                           int child_height, int child_max_iter, float *surface,
+                                           int output_width, int output_height, double parent_zoom,
+                                           double child_fraction, double child_zoom, int max_iter,
+                                           double field_bias, void *stream);
 
 /* One keyframe of a batch: device outputs (`counts` may be NULL), its zoom,
  * the reference handle it renders from (NULL: the direct FP64 path at the

@@ -22,6 +22,8 @@
 //   deep Mandelbrot pixel loop  renderer.cpp:12451-13583
 //   direct renderer             renderer.cpp:10054-10135, 10281-10438
 //   aurora colour               renderer.cpp:4788-4923, 5210-5237, 13771-13826
+//   atlas compositor            renderer.cpp:4931-5003, 5141-5244, 17969-18304,
+//                               18697-18888, 19138-19430
 #include <omp.h>
 
 #include <algorithm>
@@ -1474,51 +1476,577 @@ int render_fractal_ex(float* out, int W, int H, const char* z, const char* x, co
     return render_fractal_ex_planes(out, W, H, z, x, y, m, b, u, t, f, jr, ji, o, nullptr);
 }
 
-// Aurora palette (renderer.cpp:4788-4923) and lookup (:5210-5237).
-int fractal_colourise(const float* field, uint8_t* rgb, int W, int H, int max_iter, double phase, double vocal,
-                      double instrumental, double pitch, int threads) {
-    return status_of([&] {
-        if (!field || !rgb || !dims_ok(W, H) || max_iter <= 0 || !std::isfinite(phase) || !std::isfinite(vocal) ||
-            !std::isfinite(instrumental) || !std::isfinite(pitch))
-            throw Oops("invalid native colour dimensions or palette");
-        const int n = std::min(65536, std::max(4096, max_iter * 4));
-        std::vector<uint8_t> lut(static_cast<std::size_t>(n) * 3);
-        const double v = std::clamp(vocal, 0.0, 1.0), split = 5.0 * v * v;
-        const double p[3] = {phase, phase + split * 0.4, phase + split};
-        const double sp = std::clamp(2.0 * (pitch - 0.5), -1.0, 1.0), hue = sp * 0.16 * TAU;
-        const bool rot = std::fabs(hue) > 1.0e-15;
-        const double hc = rot ? std::cos(hue) : 1.0, hs = rot ? std::sin(hue) : 0.0;
-        for (int k = 0; k < n; ++k) {
-            double angle = 0.15 * static_cast<double>(max_iter) * static_cast<double>(k) / std::max(1, n - 1);
-            double c = static_cast<float>(std::cos(angle)), s = static_cast<float>(std::sin(angle));
-            double col[3];
-            for (int j = 0; j < 3; ++j) col[j] = (0.5 - 0.5 * (c * std::cos(p[j]) + s * std::sin(p[j]))) * 140.0;
-            if (rot) {
-                double Y = 0.299 * col[0] + 0.587 * col[1] + 0.114 * col[2];
-                double I = 0.596 * col[0] - 0.275 * col[1] - 0.321 * col[2];
-                double Q = 0.212 * col[0] - 0.523 * col[1] + 0.311 * col[2];
-                double ri = I * hc - Q * hs, rq = I * hs + Q * hc;
-                col[0] = Y + 0.956 * ri + 0.621 * rq;
-                col[1] = Y - 0.272 * ri - 0.647 * rq;
-                col[2] = Y - 1.106 * ri + 1.703 * rq;
-            }
-            for (int j = 0; j < 3; ++j) lut[3 * static_cast<std::size_t>(k) + j] = static_cast<uint8_t>(std::clamp(col[j], 0.0, 255.0));
+}  // extern "C"
+
+namespace oracle {
+
+// aurora_palette_for (renderer.cpp:4841-4923), with the optional three-accent
+// projection (:4883-4911).
+std::vector<uint8_t> aurora_table(int max_iter, double phase, double vocal, double pitch, const uint8_t* accents) {
+    const int n = std::min(65536, std::max(4096, max_iter * 4));
+    std::vector<uint8_t> lut(static_cast<std::size_t>(n) * 3);
+    const double v = std::clamp(vocal, 0.0, 1.0), split = 5.0 * v * v;
+    const double p[3] = {phase, phase + split * 0.4, phase + split};
+    const double sp = std::clamp(2.0 * (pitch - 0.5), -1.0, 1.0), hue = sp * 0.16 * TAU;
+    const bool rot = std::fabs(hue) > 1.0e-15;
+    const double hc = rot ? std::cos(hue) : 1.0, hs = rot ? std::sin(hue) : 0.0;
+    auto byte = [](double x) { return static_cast<uint8_t>(std::clamp(x, 0.0, 255.0)); };
+    for (int k = 0; k < n; ++k) {
+        double angle = 0.15 * static_cast<double>(max_iter) * static_cast<double>(k) / std::max(1, n - 1);
+        double c = static_cast<float>(std::cos(angle)), s = static_cast<float>(std::sin(angle));
+        double col[3];
+        for (int j = 0; j < 3; ++j) col[j] = (0.5 - 0.5 * (c * std::cos(p[j]) + s * std::sin(p[j]))) * 140.0;
+        if (accents) {
+            double w[3];
+            for (int j = 0; j < 3; ++j) w[j] = std::clamp(static_cast<double>(byte(col[j])) / 140.0, 0.0, 1.0);
+            for (int j = 0; j < 3; ++j)
+                col[j] = (w[0] * accents[j] + w[1] * accents[3 + j] + w[2] * accents[6 + j]) / 1.8;
         }
-        const float scale = static_cast<float>(n - 1) / static_cast<float>(max_iter);
-        if (threads > 0) omp_set_num_threads(threads);
+        if (rot) {
+            double Y = 0.299 * col[0] + 0.587 * col[1] + 0.114 * col[2];
+            double I = 0.596 * col[0] - 0.275 * col[1] - 0.321 * col[2];
+            double Q = 0.212 * col[0] - 0.523 * col[1] + 0.311 * col[2];
+            double ri = I * hc - Q * hs, rq = I * hs + Q * hc;
+            col[0] = Y + 0.956 * ri + 0.621 * rq;
+            col[1] = Y - 0.272 * ri - 0.647 * rq;
+            col[2] = Y - 1.106 * ri + 1.703 * rq;
+        }
+        for (int j = 0; j < 3; ++j) lut[3 * static_cast<std::size_t>(k) + j] = byte(col[j]);
+    }
+    return lut;
+}
+
+// write_colour_pixel (renderer.cpp:5210-5237).
+void aurora_pixel(float f, int cap, const std::vector<uint8_t>& lut, float scale, const int* interior, uint8_t* d) {
+    const int n = static_cast<int>(lut.size() / 3);
+    if (!std::isfinite(f) || f >= static_cast<float>(cap)) {
+        for (int j = 0; j < 3; ++j) d[j] = interior ? static_cast<uint8_t>(interior[j]) : 0;
+        return;
+    }
+    double x = static_cast<double>(f) * static_cast<double>(scale);
+    int k = x >= static_cast<double>(n - 1) ? n - 1 : (!std::isfinite(x) || x <= 0.0 ? 0 : static_cast<int>(x));
+    std::memcpy(d, &lut[3 * static_cast<std::size_t>(k)], 3);
+}
+
+bool colour_controls_ok(double a, double b, double c, double d) {
+    return std::isfinite(a) && std::isfinite(b) && std::isfinite(c) && std::isfinite(d);
+}
+
+bool rgb_ok(const int* c) {
+    return !c || (c[0] >= 0 && c[0] <= 255 && c[1] >= 0 && c[1] <= 255 && c[2] >= 0 && c[2] <= 255);
+}
+
+void colourise(const float* field, uint8_t* rgb, int W, int H, int max_iter, double phase, double vocal,
+               double instrumental, double pitch, int threads, const int* interior, const uint8_t* accents) {
+    if (!field || !rgb || !dims_ok(W, H) || max_iter <= 0 || !colour_controls_ok(phase, vocal, instrumental, pitch)
+        || !rgb_ok(interior))
+        throw Oops("invalid native colour dimensions or palette");
+    const std::vector<uint8_t> lut = aurora_table(max_iter, phase, vocal, pitch, accents);
+    const int n = static_cast<int>(lut.size() / 3);
+    const float scale = static_cast<float>(n - 1) / static_cast<float>(max_iter);
+    if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(static)
-        for (long long i = 0; i < static_cast<long long>(W) * H; ++i) {
-            float f = field[i];
-            uint8_t* d = rgb + 3 * i;
-            if (!std::isfinite(f) || f >= static_cast<float>(max_iter)) {
-                d[0] = d[1] = d[2] = 0;
+    for (long long i = 0; i < static_cast<long long>(W) * H; ++i) aurora_pixel(field[i], max_iter, lut, scale, interior, rgb + 3 * i);
+}
+
+// ------------------------------------------------------------------ atlas
+// fill_bilinear_axis (renderer.cpp:4931-4961).
+struct Axis {
+    std::vector<int> i0, i1;
+    std::vector<float> w;
+};
+
+Axis axis_of(int src, int dst, double zoom) {
+    zoom = std::max(zoom, 1.0);
+    const double crop = static_cast<double>(src) * (1.0 / zoom);
+    const double left = (static_cast<double>(src) - crop) * 0.5, step = crop / static_cast<double>(dst);
+    Axis a;
+    for (int d = 0; d < dst; ++d) {
+        double x = std::clamp(left + (static_cast<double>(d) + 0.5) * step - 0.5, 0.0, static_cast<double>(src - 1));
+        int k = static_cast<int>(std::floor(x));
+        a.i0.push_back(k);
+        a.i1.push_back(std::min(k + 1, src - 1));
+        a.w.push_back(static_cast<float>(x - static_cast<double>(k)));
+    }
+    return a;
+}
+
+// sample_bilinear_mapped_preserving_interior (renderer.cpp:5141-5208).
+float sample(const float* f, int width, const Axis& ax, const Axis& ay, int x, int y, int cap, bool& inside,
+             double bias) {
+    const double xw = ax.w[x], yw = ay.w[y];
+    const float v[4] = {f[static_cast<std::size_t>(ay.i0[y]) * width + ax.i0[x]],
+                        f[static_cast<std::size_t>(ay.i0[y]) * width + ax.i1[x]],
+                        f[static_cast<std::size_t>(ay.i1[y]) * width + ax.i0[x]],
+                        f[static_cast<std::size_t>(ay.i1[y]) * width + ax.i1[x]]};
+    const double w[4] = {(1.0 - yw) * (1.0 - xw), (1.0 - yw) * xw, yw * (1.0 - xw), yw * xw};
+    double in = 0.0, out = 0.0, sum = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        if (!std::isfinite(v[k])) continue;
+        if (static_cast<double>(v[k]) >= static_cast<double>(cap) - bias) {
+            in += w[k];
+        } else {
+            out += w[k];
+            sum += (static_cast<double>(v[k]) + bias) * w[k];
+        }
+    }
+    inside = in >= 0.5;
+    if (inside) return static_cast<float>(cap);
+    return out <= 1.0e-12 ? 0.0F : static_cast<float>(sum / out);
+}
+
+std::vector<float> ramp(int size, int feather) {
+    std::vector<float> r(size);
+    for (int i = 0; i < size; ++i) {
+        float l = std::min(1.0F, static_cast<float>(std::min(i, size - 1 - i)) / static_cast<float>(feather));
+        r[i] = l * l * (3.0F - 2.0F * l);
+    }
+    return r;
+}
+
+struct Frame {
+    bool child = false, full = false;
+    int vw = 0, vh = 0, left = 0, top = 0;
+};
+
+Frame frame_of(bool child, double fraction, int W, int H) {
+    Frame f;
+    f.child = child;
+    f.full = child && fraction >= 0.999999;
+    if (child) {
+        f.vw = std::max(1, static_cast<int>(std::lround(static_cast<double>(W) * fraction)));
+        f.vh = std::max(1, static_cast<int>(std::lround(static_cast<double>(H) * fraction)));
+    }
+    f.left = (W - f.vw) / 2;
+    f.top = (H - f.vh) / 2;
+    return f;
+}
+
+// fractal_atlas_field_ex (renderer.cpp:18697-18888).
+void atlas_field(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap, float* out,
+                 int W, int H, double pzoom, double fraction, double czoom, double pbias, double cbias, double obias,
+                 int palette, int feather, int threads) {
+    if (!P || !out || !dims_ok(pw, ph) || !dims_ok(W, H) || pcap <= 0 || !std::isfinite(pzoom) || pzoom <= 0.0
+        || !std::isfinite(fraction) || fraction < 0.0 || fraction > 1.0 || !std::isfinite(czoom) || czoom <= 0.0
+        || !std::isfinite(pbias) || pbias < 0.0 || pbias > pcap || !std::isfinite(cbias) || cbias < 0.0
+        || !std::isfinite(obias) || obias < 0.0 || feather < 0 || palette <= 0)
+        throw Oops("invalid native scalar atlas dimensions");
+    const Frame f = frame_of(C != nullptr && fraction > 0.0, fraction, W, H);
+    if (f.child && (!dims_ok(cw, chh) || ccap <= 0 || cbias > ccap)) throw Oops("invalid native scalar atlas child tile");
+    const int cap = std::max(palette, std::max(pcap, f.child ? ccap : 0));
+    if (obias > cap) throw Oops("invalid native scalar atlas iteration cap");
+    const int seam = f.child && !f.full ? std::min(feather, std::min(f.vw / 2, f.vh / 2)) : 0;
+    Axis px, py, cx, cy;
+    if (!f.full) {
+        px = axis_of(pw, W, pzoom);
+        py = axis_of(ph, H, pzoom);
+    }
+    if (f.child) {
+        cx = axis_of(cw, f.full ? W : f.vw, std::max(czoom, 1.0));
+        cy = axis_of(chh, f.full ? H : f.vh, std::max(czoom, 1.0));
+    }
+    std::vector<float> ex, ey;
+    if (seam >= 2) {
+        ex = ramp(f.vw, seam);
+        ey = ramp(f.vh, seam);
+    }
+    const float interior = static_cast<float>(cap - obias);
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            bool in = false;
+            float v;
+            if (f.full) {
+                float s = sample(C, cw, cx, cy, x, y, ccap, in, cbias);
+                v = in ? interior : s - static_cast<float>(obias);
+            } else {
+                float s = sample(P, pw, px, py, x, y, pcap, in, pbias);
+                v = in ? interior : s - static_cast<float>(obias);
+                if (f.child && x >= f.left && x < f.left + f.vw && y >= f.top && y < f.top + f.vh) {
+                    bool cin = false;
+                    float cs = sample(C, cw, cx, cy, x - f.left, y - f.top, ccap, cin, cbias);
+                    float cv = cin ? interior : cs - static_cast<float>(obias);
+                    float alpha = seam >= 2 ? std::min(ex[x - f.left], ey[y - f.top]) : 1.0F;
+                    v = v * (1.0F - alpha) + cv * alpha;
+                }
+            }
+            out[static_cast<std::size_t>(y) * W + x] = v;
+        }
+    }
+}
+
+// atlas_colourise_impl (renderer.cpp:19138-19430).
+void atlas_colour(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap, uint8_t* out,
+                  int W, int H, double pzoom, double fraction, int palette, double phase, double vocal,
+                  double instrumental, double pitch, int threads, const int* interior, const uint8_t* accents) {
+    if (!P || !out || !dims_ok(pw, ph) || !dims_ok(W, H) || pcap <= 0 || !std::isfinite(pzoom) || pzoom <= 0.0
+        || !std::isfinite(fraction) || fraction < 0.0 || fraction > 1.0 || palette < 0
+        || !colour_controls_ok(phase, vocal, instrumental, pitch) || !rgb_ok(interior))
+        throw Oops("invalid native atlas dimensions or controls");
+    const Frame f = frame_of(C != nullptr && fraction > 0.0, fraction, W, H);
+    if (f.child && (!dims_ok(cw, chh) || ccap <= 0)) throw Oops("invalid native atlas child tile");
+    const int cap = std::max(1, std::max(palette, std::max(pcap, f.child ? ccap : 0)));
+    const std::vector<uint8_t> lut = aurora_table(cap, phase, vocal, pitch, accents);
+    const float scale = static_cast<float>(static_cast<int>(lut.size() / 3) - 1) / static_cast<float>(cap);
+    const int feather = f.child ? std::min(48, std::min(f.vw / 8, f.vh / 8)) : 0;
+    Axis px, py, cx, cy;
+    if (!f.full) {
+        px = axis_of(pw, W, pzoom);
+        py = axis_of(ph, H, pzoom);
+    }
+    if (f.child) {
+        cx = axis_of(cw, f.full ? W : f.vw, 1.0);
+        cy = axis_of(chh, f.full ? H : f.vh, 1.0);
+    }
+    std::vector<float> ex, ey;
+    if (f.child && !f.full && feather >= 2) {
+        ex = ramp(f.vw, feather);
+        ey = ramp(f.vh, feather);
+    }
+    const float icap = static_cast<float>(cap);
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            uint8_t* d = out + (static_cast<std::size_t>(y) * W + x) * 3;
+            bool in = false;
+            if (f.full) {
+                float s = sample(C, cw, cx, cy, x, y, ccap, in, 0.0);
+                aurora_pixel(in ? icap : s, cap, lut, scale, interior, d);
                 continue;
             }
-            double x = static_cast<double>(f) * static_cast<double>(scale);
-            int k = x >= static_cast<double>(n - 1) ? n - 1 : (!std::isfinite(x) || x <= 0.0 ? 0 : static_cast<int>(x));
+            const bool inside_child = f.child && x >= f.left && x < f.left + f.vw && y >= f.top && y < f.top + f.vh;
+            if (!inside_child) {
+                float s = sample(P, pw, px, py, x, y, pcap, in, 0.0);
+                aurora_pixel(in ? icap : s, cap, lut, scale, interior, d);
+                continue;
+            }
+            bool cin = false;
+            float cs = sample(C, cw, cx, cy, x - f.left, y - f.top, ccap, cin, 0.0);
+            float alpha = feather >= 2 ? std::min(ex[x - f.left], ey[y - f.top]) : 1.0F;
+            if (alpha >= 0.999999F) {
+                aurora_pixel(cin ? icap : cs, cap, lut, scale, interior, d);
+                continue;
+            }
+            float ps = sample(P, pw, px, py, x, y, pcap, in, 0.0);
+            uint8_t a[3], b[3];
+            aurora_pixel(in ? icap : ps, cap, lut, scale, interior, a);
+            aurora_pixel(cin ? icap : cs, cap, lut, scale, interior, b);
+            for (int j = 0; j < 3; ++j) {
+                double v = static_cast<double>(a[j]) * (1.0 - alpha) + static_cast<double>(b[j]) * alpha;
+                d[j] = static_cast<uint8_t>(std::clamp(static_cast<int>(std::nearbyint(std::clamp(v, 0.0, 255.0))), 0, 255));
+            }
+        }
+    }
+}
+
+// fill_bilinear_axis_window (renderer.cpp:4969-5003).
+Axis window_of(int src, int dst, double origin, double span, double zoom) {
+    zoom = std::max(zoom, 1.0);
+    const double crop = static_cast<double>(src) / zoom, left = (static_cast<double>(src) - crop) * 0.5;
+    Axis a;
+    for (int d = 0; d < dst; ++d) {
+        const double logical = origin + static_cast<double>(d) + 0.5;
+        double x = std::clamp(left + logical * crop / span - 0.5, 0.0, static_cast<double>(src - 1));
+        int k = static_cast<int>(std::floor(x));
+        a.i0.push_back(k);
+        a.i1.push_back(std::min(k + 1, src - 1));
+        a.w.push_back(static_cast<float>(x - static_cast<double>(k)));
+    }
+    return a;
+}
+
+// The scalar surface of fractal_atlas_colourise_kfp_raw (renderer.cpp:
+// 18010-18288): parent view, child view with its halo, ownership blend.
+void kfp_surface(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap, float* out,
+                 int W, int H, double pzoom, double fraction, double czoom, int max_iter, double field_bias) {
+    if (!P || !out || !dims_ok(pw, ph) || !dims_ok(W, H) || pcap <= 0 || max_iter <= 0 || !std::isfinite(pzoom)
+        || pzoom <= 0.0 || !std::isfinite(fraction) || fraction < 0.0 || fraction > 1.0 || !std::isfinite(czoom)
+        || czoom <= 0.0)
+        throw Oops("invalid native raw KFP atlas dimensions or controls");
+    pzoom = std::max(pzoom, 1.0);
+    czoom = std::max(czoom, 1.0);
+    const bool child = C != nullptr && fraction > 0.0;
+    if (child && (!dims_ok(cw, chh) || ccap <= 0)) throw Oops("invalid native raw KFP atlas child tile");
+    if (!child && C) throw Oops("raw KFP atlas child needs a positive visible fraction");
+    if (!child && (cw || chh || ccap)) throw Oops("invalid native raw KFP atlas child absence");
+    if (field_bias > max_iter) throw Oops("native KFP field bias exceeds iteration cap");
+    const bool centred = field_bias > 0.0;
+    const double pbias = centred ? pcap : 0.0, cbias = centred ? ccap : 0.0;
+    auto enc = [&](long double v) { return static_cast<float>(v - static_cast<long double>(field_bias)); };
+    const Frame f = frame_of(child, fraction, W, H);
+    const int halo = child ? std::min(2, std::min(std::min(f.left, W - f.left - f.vw), std::min(f.top, H - f.top - f.vh))) : 0;
+    int seam = 0;
+    if (child) {
+        const int m = std::min(f.vw, f.vh);
+        seam = m <= 0 ? 0 : std::min(std::max(2, std::min(64, m / 2)), std::max(0, (m - 1) / 2));
+    }
+    const Axis px = axis_of(pw, W, pzoom), py = axis_of(ph, H, pzoom);
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            bool in = false;
+            float s = sample(P, pw, px, py, x, y, pcap, in, pbias);
+            out[static_cast<std::size_t>(y) * W + x] = in ? enc(max_iter) : enc(s);
+        }
+    }
+    if (!child) return;
+    const int sw = f.vw + 2 * halo, sh = f.vh + 2 * halo;
+    const Axis cx = window_of(cw, sw, -halo, f.vw, czoom), cy = window_of(chh, sh, -halo, f.vh, czoom);
+    std::vector<float> view(static_cast<std::size_t>(sw) * sh);
+    for (int y = 0; y < sh; ++y) {
+        for (int x = 0; x < sw; ++x) {
+            bool in = false;
+            float s = sample(C, cw, cx, cy, x, y, ccap, in, cbias);
+            view[static_cast<std::size_t>(y) * sw + x] = in ? enc(max_iter) : enc(s);
+        }
+    }
+    for (int y = f.top; y < f.top + f.vh; ++y) {
+        for (int x = f.left; x < f.left + f.vw; ++x) {
+            const float cv = view[static_cast<std::size_t>(y - f.top + halo) * sw + (x - f.left + halo)];
+            float alpha = 1.0F;
+            if (seam >= 2) {
+                const int vx = x - f.left, vy = y - f.top;
+                const int edge = std::min(std::min(vx, f.vw - 1 - vx), std::min(vy, f.vh - 1 - vy));
+                const float l = std::clamp(static_cast<float>(edge) / static_cast<float>(seam), 0.0F, 1.0F);
+                alpha = l * l * (3.0F - 2.0F * l);
+            }
+            float& o = out[static_cast<std::size_t>(y) * W + x];
+            o = alpha >= 0.999999F ? cv : o * (1.0F - alpha) + cv * alpha;
+        }
+    }
+}
+
+// fractal_crop_colourise_kfp's scalar crop (renderer.cpp:17836-17868).
+void crop_kfp_surface(const float* S, int sw, int sh, float* out, int W, int H, double zoom, int max_iter,
+                      double field_bias) {
+    if (!S || !out || !dims_ok(sw, sh) || !dims_ok(W, H) || max_iter <= 0 || !std::isfinite(zoom) || zoom <= 0.0)
+        throw Oops("invalid native KFP crop dimensions or controls");
+    if (field_bias > max_iter) throw Oops("native KFP field bias exceeds iteration cap");
+    zoom = std::max(zoom, 1.0);
+    const Axis ax = axis_of(sw, W, zoom), ay = axis_of(sh, H, zoom);
+    auto enc = [&](long double v) { return static_cast<float>(v - static_cast<long double>(field_bias)); };
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            bool in = false;
+            float s = sample(S, sw, ax, ay, x, y, max_iter, in, field_bias);
+            out[static_cast<std::size_t>(y) * W + x] = in ? enc(max_iter) : enc(s);
+        }
+    }
+}
+
+// sample_bilinear_mapped (renderer.cpp:5053-5073) over a crop
+// (fractal_crop_field, renderer.cpp:18631-18696).
+void crop_field(const float* S, int sw, int sh, float* out, int W, int H, double zoom) {
+    if (!S || !out || !dims_ok(sw, sh) || !dims_ok(W, H) || !std::isfinite(zoom) || zoom <= 0.0)
+        throw Oops("invalid native raw-field crop dimensions");
+    zoom = std::max(zoom, 1.0);
+    const Axis ax = axis_of(sw, W, zoom), ay = axis_of(sh, H, zoom);
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            const float* t = S + static_cast<std::size_t>(ay.i0[y]) * sw;
+            const float* b = S + static_cast<std::size_t>(ay.i1[y]) * sw;
+            const float xw = ax.w[x], yw = ay.w[y];
+            const float tv = t[ax.i0[x]] * (1.0F - xw) + t[ax.i1[x]] * xw;
+            const float bv = b[ax.i0[x]] * (1.0F - xw) + b[ax.i1[x]] * xw;
+            out[static_cast<std::size_t>(y) * W + x] = tv * (1.0F - yw) + bv * yw;
+        }
+    }
+}
+
+uint8_t rounded_byte(double v) {
+    return static_cast<uint8_t>(std::clamp(static_cast<int>(std::nearbyint(std::clamp(v, 0.0, 255.0))), 0, 255));
+}
+
+// sample_rgb_bilinear_mapped (renderer.cpp:5262-5298).
+void rgb_sample(const uint8_t* S, int sw, const Axis& ax, const Axis& ay, int x, int y, uint8_t* d) {
+    const uint8_t* t0 = S + (static_cast<std::size_t>(ay.i0[y]) * sw + ax.i0[x]) * 3;
+    const uint8_t* t1 = S + (static_cast<std::size_t>(ay.i0[y]) * sw + ax.i1[x]) * 3;
+    const uint8_t* b0 = S + (static_cast<std::size_t>(ay.i1[y]) * sw + ax.i0[x]) * 3;
+    const uint8_t* b1 = S + (static_cast<std::size_t>(ay.i1[y]) * sw + ax.i1[x]) * 3;
+    const float xw = ax.w[x], yw = ay.w[y], ix = 1.0F - xw, iy = 1.0F - yw;
+    for (int c = 0; c < 3; ++c) {
+        const float tv = static_cast<float>(t0[c]) * ix + static_cast<float>(t1[c]) * xw;
+        const float bv = static_cast<float>(b0[c]) * ix + static_cast<float>(b1[c]) * xw;
+        d[c] = rounded_byte(static_cast<double>(tv * iy + bv * yw));
+    }
+}
+
+// fractal_atlas_composite_rgb (renderer.cpp:18467-18629); a null child with
+// zero fraction is fractal_crop_rgb (renderer.cpp:18399-18465).
+void composite_rgb(const uint8_t* P, int pw, int ph, const uint8_t* C, int cw, int chh, uint8_t* out, int W, int H,
+                   double pzoom, double fraction, double czoom, int feather) {
+    pzoom = std::max(pzoom, 1.0);
+    czoom = std::max(czoom, 1.0);
+    const bool child = C != nullptr && fraction > 0.0;
+    const Frame f = frame_of(child, fraction, W, H);
+    const int fe = child ? std::min(feather, std::min(f.vw, f.vh)) : 0;
+    const Axis px = axis_of(pw, W, pzoom), py = axis_of(ph, H, pzoom);
+    Axis cx, cy;
+    if (child) {
+        cx = axis_of(cw, f.vw, czoom);
+        cy = axis_of(chh, f.vh, czoom);
+    }
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            uint8_t* d = out + (static_cast<std::size_t>(y) * W + x) * 3;
+            rgb_sample(P, pw, px, py, x, y, d);
+            if (!child || x < f.left || x >= f.left + f.vw || y < f.top || y >= f.top + f.vh) continue;
+            uint8_t c[3];
+            rgb_sample(C, cw, cx, cy, x - f.left, y - f.top, c);
+            double alpha = 1.0;
+            if (fe >= 2) {
+                const int e = std::min(std::min(x - f.left, f.vw - 1 - (x - f.left)),
+                                       std::min(y - f.top, f.vh - 1 - (y - f.top)));
+                const double l = std::clamp(static_cast<double>(e) / static_cast<double>(fe), 0.0, 1.0);
+                alpha = l * l * (3.0 - 2.0 * l);
+            }
+            for (int k = 0; k < 3; ++k) d[k] = rounded_byte(static_cast<double>(d[k]) * (1.0 - alpha) + static_cast<double>(c[k]) * alpha);
+        }
+    }
+}
+
+// crop_colourise_impl (renderer.cpp:18977-19020).
+void crop_colour(const float* S, int sw, int sh, uint8_t* out, int W, int H, double zoom, int max_iter, double phase,
+                 double vocal, double instrumental, double pitch, const int* interior, const uint8_t* accents) {
+    if (!S || !out || !dims_ok(sw, sh) || !dims_ok(W, H) || max_iter <= 0 || !std::isfinite(zoom) || zoom <= 0.0
+        || !colour_controls_ok(phase, vocal, instrumental, pitch) || !rgb_ok(interior))
+        throw Oops("invalid native crop/colour dimensions or palette");
+    zoom = std::max(zoom, 1.0);
+    const std::vector<uint8_t> lut = aurora_table(max_iter, phase, vocal, pitch, accents);
+    const int n = static_cast<int>(lut.size() / 3);
+    const float scale = static_cast<float>(n - 1) / static_cast<float>(max_iter);
+    const Axis ax = axis_of(sw, W, zoom), ay = axis_of(sh, H, zoom);
+    for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+            uint8_t* d = out + (static_cast<std::size_t>(y) * W + x) * 3;
+            bool in = false;
+            const float s = sample(S, sw, ax, ay, x, y, max_iter, in, 0.0);
+            if (in) {
+                for (int j = 0; j < 3; ++j) d[j] = interior ? static_cast<uint8_t>(interior[j]) : 0;
+                continue;
+            }
+            const double v = static_cast<double>(s) * static_cast<double>(scale);
+            const int k = v >= static_cast<double>(n - 1) ? n - 1 : (!std::isfinite(v) || v <= 0.0 ? 0 : static_cast<int>(v));
             std::memcpy(d, &lut[3 * static_cast<std::size_t>(k)], 3);
         }
+    }
+}
+
+}  // namespace oracle
+
+extern "C" {
+int oracle_crop_kfp_surface(const float* S, int sw, int sh, float* out, int W, int H, double zoom, int max_iter,
+                            double field_bias) {
+    return status_of([&] { crop_kfp_surface(S, sw, sh, out, W, H, zoom, max_iter, field_bias); });
+}
+
+int fractal_crop_field(const float* S, int sw, int sh, float* out, int W, int H, double zoom, int) {
+    return status_of([&] { crop_field(S, sw, sh, out, W, H, zoom); });
+}
+
+int fractal_crop_rgb(const uint8_t* S, int sw, int sh, uint8_t* out, int W, int H, double zoom, int) {
+    return status_of([&] {
+        if (!S || !out || !dims_ok(sw, sh) || !dims_ok(W, H) || !std::isfinite(zoom) || zoom <= 0.0)
+            throw Oops("invalid native RGB crop dimensions");
+        composite_rgb(S, sw, sh, nullptr, 0, 0, out, W, H, zoom, 0.0, 1.0, 0);
     });
+}
+
+int fractal_atlas_composite_rgb(const uint8_t* P, int pw, int ph, const uint8_t* C, int cw, int chh, uint8_t* out,
+                                int W, int H, double pzoom, double fraction, double czoom, int feather, int) {
+    return status_of([&] {
+        if (!P || !out || !dims_ok(pw, ph) || !dims_ok(W, H) || !std::isfinite(pzoom) || pzoom <= 0.0
+            || !std::isfinite(fraction) || fraction < 0.0 || fraction > 1.0 || !std::isfinite(czoom) || czoom <= 0.0
+            || feather < 0)
+            throw Oops("invalid native RGB atlas dimensions or controls");
+        const bool child = C != nullptr && fraction > 0.0;
+        if (!child && fraction > 0.0) throw Oops("RGB atlas child data is missing for a positive fraction");
+        if (!child && C) throw Oops("RGB atlas child needs a positive visible fraction");
+        if (!child && (cw || chh)) throw Oops("invalid native RGB atlas child absence");
+        if (child && (!dims_ok(cw, chh) || feather > std::min(W, H))) throw Oops("invalid native RGB atlas child tile");
+        composite_rgb(P, pw, ph, C, cw, chh, out, W, H, pzoom, fraction, czoom, feather);
+    });
+}
+
+int fractal_crop_colourise(const float* S, int sw, int sh, uint8_t* out, int W, int H, double zoom, int max_iter,
+                           double phase, double vocal, double instrumental, double pitch, int) {
+    return status_of([&] { crop_colour(S, sw, sh, out, W, H, zoom, max_iter, phase, vocal, instrumental, pitch, nullptr, nullptr); });
+}
+
+int fractal_crop_colourise_interior(const float* S, int sw, int sh, uint8_t* out, int W, int H, double zoom,
+                                    int max_iter, double phase, double vocal, double instrumental, double pitch, int r,
+                                    int g, int b, int) {
+    const int interior[3] = {r, g, b};
+    return status_of([&] { crop_colour(S, sw, sh, out, W, H, zoom, max_iter, phase, vocal, instrumental, pitch, interior, nullptr); });
+}
+
+int fractal_crop_colourise_accents(const float* S, int sw, int sh, uint8_t* out, int W, int H, double zoom,
+                                   int max_iter, double phase, double vocal, double instrumental, double pitch,
+                                   const uint8_t* accents, int r, int g, int b, int) {
+    const int interior[3] = {r, g, b};
+    return status_of([&] { crop_colour(S, sw, sh, out, W, H, zoom, max_iter, phase, vocal, instrumental, pitch, interior, accents); });
+}
+
+// Test-only export: the raw KFP atlas surface (no reference symbol).
+int oracle_atlas_kfp_surface(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap,
+                             float* out, int W, int H, double pzoom, double fraction, double czoom, int max_iter,
+                             double field_bias) {
+    return status_of([&] { kfp_surface(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, czoom, max_iter, field_bias); });
+}
+
+int fractal_colourise(const float* field, uint8_t* rgb, int W, int H, int max_iter, double phase, double vocal,
+                      double instrumental, double pitch, int threads) {
+    return status_of([&] { colourise(field, rgb, W, H, max_iter, phase, vocal, instrumental, pitch, threads, nullptr, nullptr); });
+}
+
+int fractal_colourise_accents(const float* field, uint8_t* rgb, int W, int H, int max_iter, double phase,
+                              double vocal, double instrumental, double pitch, const uint8_t* accents, int r, int g,
+                              int b, int threads) {
+    if (!accents) {
+        error_text = "ordinary palette accents are required";
+        return 1;
+    }
+    const int interior[3] = {r, g, b};
+    return status_of([&] { colourise(field, rgb, W, H, max_iter, phase, vocal, instrumental, pitch, threads, interior, accents); });
+}
+
+int fractal_atlas_field_ex(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap,
+                           float* out, int W, int H, double pzoom, double fraction, double czoom, double pbias,
+                           double cbias, double obias, int palette, int feather, int threads) {
+    return status_of([&] { atlas_field(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, czoom, pbias, cbias, obias, palette, feather, threads); });
+}
+
+int fractal_atlas_field(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap,
+                        float* out, int W, int H, double pzoom, double fraction, int palette, int threads) {
+    return fractal_atlas_field_ex(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, 1.0, 0.0, 0.0, 0.0,
+                                  palette, 48, threads);
+}
+
+int fractal_atlas_colourise(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh, int ccap,
+                            uint8_t* out, int W, int H, double pzoom, double fraction, int palette, double phase,
+                            double vocal, double instrumental, double pitch, int threads) {
+    return status_of([&] { atlas_colour(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, palette, phase, vocal, instrumental, pitch, threads, nullptr, nullptr); });
+}
+
+int fractal_atlas_colourise_interior(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh,
+                                     int ccap, uint8_t* out, int W, int H, double pzoom, double fraction, int palette,
+                                     double phase, double vocal, double instrumental, double pitch, int r, int g,
+                                     int b, int threads) {
+    const int interior[3] = {r, g, b};
+    return status_of([&] { atlas_colour(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, palette, phase, vocal, instrumental, pitch, threads, interior, nullptr); });
+}
+
+int fractal_atlas_colourise_accents(const float* P, int pw, int ph, int pcap, const float* C, int cw, int chh,
+                                    int ccap, uint8_t* out, int W, int H, double pzoom, double fraction, int palette,
+                                    double phase, double vocal, double instrumental, double pitch,
+                                    const uint8_t* accents, int r, int g, int b, int threads) {
+    if (!accents) {
+        error_text = "ordinary palette accents are required";
+        return 1;
+    }
+    const int interior[3] = {r, g, b};
+    return status_of([&] { atlas_colour(P, pw, ph, pcap, C, cw, chh, ccap, out, W, H, pzoom, fraction, palette, phase, vocal, instrumental, pitch, threads, interior, accents); });
 }
 
 }  // extern "C"
