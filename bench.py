@@ -498,7 +498,8 @@ def run_case(name: str) -> int:
         print("ok", name)
         return 0
     if name == "atlas_colour_3840x2160":
-        # Two 4K keyframes (levels 30 and 31), then the atlas frame twice.
+        # Two 4K keyframes (levels 30 and 31), then the atlas frame twice
+        # (parent zoom 1.7, child fraction 1.7 / 4, as the frame-pass default).
         width, height = 3840, 2160
         levels, step = workload_levels()
         x, y = centre()
@@ -513,7 +514,7 @@ def run_case(name: str) -> int:
         for _ in range(2):
             status = library.fractal_gb300_atlas_colourise_device(
                 fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
-                rgb.data_ptr(), width, height, 2.0, 0.5, 0, 0.3, 0.4, 0.7, 0.5, None, None,
+                rgb.data_ptr(), width, height, 1.7, 0.425, 0, 0.3, 0.4, 0.7, 0.5, None, None,
                 ctypes.c_void_p(stream.cuda_stream))
             assert status == 0, package.native.last_error(library)
         torch.cuda.synchronize()
@@ -654,8 +655,11 @@ def run_frame_passes(args) -> int:
                     times.append(start.elapsed_time(stop))
             ms = statistics.median(times)
             achieved = algorithmic / (ms * 1e-3) / 1e9
-            results.append({"pass": f"{name}_3840x2160", "ms": round(ms, 4), "algorithmic_bytes": int(algorithmic),
-                            "achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / peak, 4)})
+            entry = {"pass": f"{name}_3840x2160", "ms": round(ms, 4), "algorithmic_bytes": int(algorithmic),
+                     "achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / peak, 4)}
+            if name.startswith("atlas"):
+                entry["exact_pass_pixels"] = int(library.fractal_gb300_atlas_last_exact_pixels())
+            results.append(entry)
     # The same atlas frame on the host cores through the oracle port.
     port = native.load(os.path.join(ROOT, "oracle", "_ref", "liboracle.so"))
     host = [fields[i].cpu().numpy() for i in range(2)]
@@ -676,6 +680,122 @@ def run_frame_passes(args) -> int:
     return 0
 
 
+SONG_FACTOR = 4.0      # atlas keyframe factor of the song workload
+SONG_OVERSCAN = 1.2    # KFP tiles are stored 1.2x wider than their view (ATLAS_TILE_OVERSCAN_FACTOR)
+SONG_MAX_LOG = 100.0   # the camera path ends at zoom 1e100
+
+
+def song_levels():
+    """The 4K song atlas: levels 0..167 of factor 4 up to 1e100 (the
+    reference's _atlas_geometry for a [0, 100] decade path), each tile stored
+    at its level zoom / 1.2, caps max_iterations(log, 384, 500, 100000)."""
+    step = math.log10(SONG_FACTOR)
+    count = int(math.ceil(SONG_MAX_LOG / step - 1.0e-12))
+    levels = []
+    for i in range(count + 1):
+        log_zoom = i * step - math.log10(SONG_OVERSCAN)
+        cap = min(100_000, max(64, int(384 + 500 * max(0.0, log_zoom))))
+        levels.append((i, log_zoom, cap))
+    return levels, step
+
+
+def song_frame(t: int, frames: int, step: float, last_level: int):
+    """Atlas parameters of frame t on a constant-rate path 1e0 -> 1e100:
+    (parent level, parent zoom, child fraction); child zoom is the
+    overscan (visualizer.py:11959-11975, 666-696)."""
+    log_zoom = SONG_MAX_LOG * t / max(1, frames - 1)
+    level = max(0, min(int(math.floor(log_zoom / step + 1.0e-9)), last_level))
+    parent_zoom = max(1.0, SONG_OVERSCAN * 10.0 ** (log_zoom - level * step))
+    fraction = min(1.0, max(0.0, parent_zoom / (SONG_FACTOR * SONG_OVERSCAN))) if level < last_level else 0.0
+    return level, parent_zoom, fraction
+
+
+def run_song(args) -> int:
+    """The song workload at 4K60: 180 s -> 10,800 frames over the 168-tile
+    factor-4 atlas to 1e100 (seeded Misiurewicz centre).  Every tile is
+    rendered once (batched keyframe call, chosen form), then every frame is
+    one raw KFP atlas frame (parent + child composed into a 4K surface, one
+    KFP pass: 16 seeded stops, ColorMethod 7, Differences 3, slopes, dither)
+    into device RGB8.  The zoom path is a constant rate (the audio-driven
+    zoom plan is outside the path).  Reports fps and the iteration / colour
+    time shares; the reference creation (MPFR orbit, host) is reported
+    apart."""
+    import torch
+
+    package = __graft_entry__._package()
+    library = package.load_library()
+    native = package.native
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    width, height = 3840, 2160
+    pixels = width * height
+    frames = int(round(args.song_seconds * 60))
+    levels, step = song_levels()
+    last = len(levels) - 1
+    x, y = centre()
+    t0 = time.perf_counter()
+    stack = package.atlas.KeyframeStack(library, x, y, levels, step=step)
+    reference_s = time.perf_counter() - t0
+    fields = torch.empty((len(levels), pixels), dtype=torch.float32, device="cuda")
+    counts = torch.empty((len(levels), pixels), dtype=torch.int32, device="cuda")
+    targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(len(levels))]
+    h = stream.cuda_stream
+    # Warm-up (tables upload, graph/autotune state), then the timed tile pass.
+    stack.render_batch_device(targets, width, height, form=1, stream=h)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    stack.render_batch_device(targets, width, height, form=1, stream=h)
+    stop.record(stream)
+    stop.synchronize()
+    fields_ms = start.elapsed_time(stop)
+    iterations = int(counts.to(torch.int64).sum().item())
+    caps = [cap for _, _, cap in levels]
+    kfp = package.kfp
+    profile = kfp.recipe("seeded16")
+    lut = torch.from_numpy(kfp.palette_lut(profile)).cuda()
+    options = kfp.options(profile)
+    rgb = torch.empty((2, pixels * 3), dtype=torch.uint8, device="cuda")
+
+    def frame(t):
+        level, parent_zoom, fraction = song_frame(t, frames, step, last)
+        child = level + 1 if fraction > 0.0 else None
+        status = library.fractal_gb300_atlas_colourise_kfp_raw_device(
+            fields[level].data_ptr(), width, height, caps[level],
+            fields[child].data_ptr() if child is not None else None, width if child is not None else 0,
+            height if child is not None else 0, caps[child] if child is not None else 0,
+            rgb[t & 1].data_ptr(), width, height, parent_zoom, fraction, SONG_OVERSCAN if child else 1.0,
+            max(caps[level], caps[child] if child is not None else 0), ctypes.byref(options),
+            ctypes.c_void_p(lut.data_ptr()), lut.shape[0], ctypes.c_void_p(h))
+        if status != 0:
+            raise RuntimeError(native.last_error(library))
+
+    for t in range(3):
+        frame(t)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    start.record(stream)
+    for t in range(frames):
+        frame(t)
+    stop.record(stream)
+    stop.synchronize()
+    frames_wall_ms = (time.perf_counter() - wall0) * 1e3
+    frames_ms = start.elapsed_time(stop)
+    total_ms = fields_ms + frames_ms
+    stack.close()
+    print(json.dumps({
+        "workload": f"song 4K60: {frames} frames, {len(levels)} atlas tiles (factor 4, to 1e100), KFP raw atlas frames",
+        "fps": round(frames / (total_ms / 1e3), 1),
+        "fields_ms": round(fields_ms, 2), "frames_ms": round(frames_ms, 2),
+        "frames_wall_ms": round(frames_wall_ms, 2),
+        "per_frame_ms": round(frames_ms / frames, 4),
+        "iteration_share": round(fields_ms / total_ms, 4), "colour_share": round(frames_ms / total_ms, 4),
+        "tile_gpixel_iter_per_s": round(iterations / (fields_ms * 1e-3) / 1e9, 1),
+        "tile_pixel_iterations": iterations, "reference_creation_s": round(reference_s, 2),
+        "readback": "none (RGB8 stays in device memory)"}))
+    return 0
+
+
 def main() -> int:
     parser = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     parser.add_argument("--gpus", type=int, default=1)
@@ -686,6 +806,9 @@ def main() -> int:
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--frame-passes", action="store_true",
                         help="time the per-frame 4K passes (atlas compositor, colour) and exit")
+    parser.add_argument("--song", action="store_true",
+                        help="run the 4K60 song workload (all atlas tiles, then every frame) and exit")
+    parser.add_argument("--song-seconds", type=float, default=180.0)
     parser.add_argument("--frame-zoom", type=float, default=1.7,
                         help="parent zoom of the timed atlas frame (child fraction = zoom / 4)")
     parser.add_argument("--case", default=None,
@@ -698,6 +821,8 @@ def main() -> int:
         return run_case(args.case)
     if args.frame_passes:
         return run_frame_passes(args)
+    if args.song:
+        return run_song(args)
     if args.impl == "reference":
         return run_reference_arm(args)
     return run_gpu_arm(args)

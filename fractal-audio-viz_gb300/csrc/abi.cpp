@@ -800,9 +800,20 @@ struct KfpDeviceInputs {
     const int* type = nullptr;
 };
 
-// Uploads the LUT and multi-colour waves into the thread's scratch.
+// Uploads the LUT and multi-colour waves into the thread's scratch.  The
+// upload is skipped when the same waves (and, for a host LUT, the same LUT
+// bytes) already sit in the same scratch buffer; `uploaded` reports whether
+// copies were enqueued on the thread stream.
 KfpDeviceInputs kfp_inputs(ThreadRuntime& rt, const FractalKfpOptions& o, const std::uint8_t* lut, int lut_size,
-                           bool lut_on_device) {
+                           bool lut_on_device, bool* uploaded = nullptr) {
+    struct Cached {
+        const void* base = nullptr;
+        std::vector<double> period;
+        std::vector<int> type;
+        std::vector<std::uint8_t> lut;
+        bool host_lut = false;
+    };
+    thread_local Cached cached;
     KfpDeviceInputs in;
     // Layout: [LUT padded to 16 B][256 wave periods][256 wave types].
     const std::size_t lut_bytes = static_cast<std::size_t>(lut_size) * 3;
@@ -813,20 +824,41 @@ KfpDeviceInputs kfp_inputs(ThreadRuntime& rt, const FractalKfpOptions& o, const 
     std::uint8_t* lut_copy = reinterpret_cast<std::uint8_t*>(base);
     double* period = reinterpret_cast<double*>(base + lut_padded);
     int* type = reinterpret_cast<int*>(base + lut_padded + FRACTAL_KFP_MAX_MULTI_COLORS * sizeof(double));
-    if (waves > 0) {
-        check_cuda(cudaMemcpyAsync(period, o.multi_color_period, waves * sizeof(double), cudaMemcpyHostToDevice,
-                                   rt.stream), "upload KFP waves");
-        check_cuda(cudaMemcpyAsync(type, o.multi_color_type, waves * sizeof(int), cudaMemcpyHostToDevice, rt.stream),
-                   "upload KFP waves");
+    const bool same_waves = cached.base == base && cached.period.size() == waves
+        && std::equal(o.multi_color_period, o.multi_color_period + waves, cached.period.begin())
+        && std::equal(o.multi_color_type, o.multi_color_type + waves, cached.type.begin());
+    const bool same_lut = lut_on_device
+        || (cached.base == base && cached.host_lut && cached.lut.size() == lut_bytes
+            && std::equal(lut, lut + lut_bytes, cached.lut.begin()));
+    bool copied = false;
+    if (!same_waves) {
+        if (waves > 0) {
+            check_cuda(cudaMemcpyAsync(period, o.multi_color_period, waves * sizeof(double), cudaMemcpyHostToDevice,
+                                       rt.stream), "upload KFP waves");
+            check_cuda(cudaMemcpyAsync(type, o.multi_color_type, waves * sizeof(int), cudaMemcpyHostToDevice,
+                                       rt.stream), "upload KFP waves");
+            copied = true;
+        }
+        cached.period.assign(o.multi_color_period, o.multi_color_period + waves);
+        cached.type.assign(o.multi_color_type, o.multi_color_type + waves);
     }
     if (lut_on_device) {
         in.lut = lut;
     } else {
-        check_cuda(cudaMemcpyAsync(lut_copy, lut, lut_bytes, cudaMemcpyHostToDevice, rt.stream), "upload KFP LUT");
+        if (!same_lut) {
+            check_cuda(cudaMemcpyAsync(lut_copy, lut, lut_bytes, cudaMemcpyHostToDevice, rt.stream),
+                       "upload KFP LUT");
+            cached.lut.assign(lut, lut + lut_bytes);
+            cached.host_lut = true;
+            copied = true;
+        }
         in.lut = lut_copy;
     }
+    if (lut_on_device) cached.host_lut = cached.host_lut && same_lut;
+    cached.base = base;
     in.period = period;
     in.type = type;
+    if (uploaded) *uploaded = copied;
     return in;
 }
 
@@ -925,6 +957,14 @@ using namespace fgb;
 
 // ------------------------------------------------------------ atlas frames
 namespace {
+
+// launch_atlas, remembering the frame's exact-pass counter for
+// fractal_gb300_atlas_last_exact_pixels.
+cudaError_t run_atlas(ThreadRuntime& rt, AtlasLaunch& a, void* tables, cudaStream_t stream) {
+    const cudaError_t status = launch_atlas(a, tables, stream);
+    rt.atlas_exact_count = a.exact_count;
+    return status;
+}
 
 // Validated arguments of one atlas frame: geometry and numbers for
 // launch_atlas, sources and outputs left to the caller.
@@ -1084,7 +1124,7 @@ void atlas_from_host(ThreadRuntime& rt, AtlasLaunch& a, const void* parent, cons
         a.rgb = static_cast<std::uint8_t*>(device_out);
     }
     check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
-    check_cuda(launch_atlas(a, tables, rt.stream), "atlas kernel launch");
+    check_cuda(run_atlas(rt, a, tables, rt.stream), "atlas kernel launch");
     check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
     check_cuda(cudaMemcpyAsync(output, device_out, out_bytes, cudaMemcpyDeviceToHost, rt.stream),
                "copy atlas frame to host");
@@ -1757,8 +1797,9 @@ int fractal_gb300_colourise_kfp_device(const float* field, uint8_t* rgb, int wid
         ThreadRuntime& rt = thread_runtime();
         cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
         wait_scratch(rt, rt.stream);
-        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true);
-        check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
+        bool uploaded = false;
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true, &uploaded);
+        if (uploaded) check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
         kfp_colour(field, rgb, width, height, max_iter, *options, in, lut_size, rt, stream);
         release_scratch(rt, stream);
     });
@@ -2351,7 +2392,7 @@ int fractal_atlas_colourise_kfp_raw(const float* parent, int parent_width, int p
         std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
         const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, false);
         check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
-        check_cuda(launch_atlas(a, tables, rt.stream), "atlas surface launch");
+        check_cuda(run_atlas(rt, a, tables, rt.stream), "atlas surface launch");
         kfp_colour(a.field_out, d_rgb, output_width, output_height, max_iter, *options, in, lut_size, rt, rt.stream);
         check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
         check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
@@ -2395,15 +2436,16 @@ int fractal_gb300_atlas_colourise_kfp_raw_device(const float* parent, int parent
         ThreadRuntime& rt = thread_runtime();
         cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
         wait_scratch(rt, rt.stream);
-        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true);
-        check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
+        bool uploaded = false;
+        const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, true, &uploaded);
+        if (uploaded) check_cuda(cudaStreamSynchronize(rt.stream), "KFP inputs");
         wait_scratch(rt, stream);
         a.parent = parent;
         a.child = child;
         const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
         a.field_out = static_cast<float*>(scratch(rt, kScratchSurface, pixels * sizeof(float)));
         void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
-        check_cuda(launch_atlas(a, tables, stream), "atlas surface launch");
+        check_cuda(run_atlas(rt, a, tables, stream), "atlas surface launch");
         kfp_colour(a.field_out, output, output_width, output_height, max_iter, *options, in, lut_size, rt, stream);
         release_scratch(rt, stream);
     });
@@ -2440,7 +2482,7 @@ int fractal_gb300_atlas_kfp_surface_device(const float* parent, int parent_width
         a.child = child;
         a.field_out = surface;
         void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
-        check_cuda(launch_atlas(a, tables, stream), "atlas surface launch");
+        check_cuda(run_atlas(rt, a, tables, stream), "atlas surface launch");
         release_scratch(rt, stream);
     });
 }
@@ -2601,7 +2643,7 @@ int crop_colourise_kfp_common(const float* source, int source_width, int source_
         std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
         const KfpDeviceInputs in = kfp_inputs(rt, *options, lut, lut_size, false);
         check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
-        check_cuda(launch_atlas(a, tables, rt.stream), "crop surface launch");
+        check_cuda(run_atlas(rt, a, tables, rt.stream), "crop surface launch");
         kfp_colour(a.field_out, d_rgb, output_width, output_height, max_iter, *options, in, lut_size, rt, rt.stream);
         check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
         check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
@@ -2667,6 +2709,21 @@ int fractal_crop_colourise_kfp_precise(const float* source, int source_width, in
                                      threads);
 }
 
+// Pixels of the last atlas frame on this thread that the fast pass left to
+// the exact FP64 pass (synchronises with the device); -1 before any frame.
+long long fractal_gb300_atlas_last_exact_pixels(void) {
+    try {
+        ThreadRuntime& rt = thread_runtime();
+        if (rt.atlas_exact_count == nullptr) return -1;
+        unsigned count = 0;
+        check_cuda(cudaDeviceSynchronize(), "atlas exact count");
+        check_cuda(cudaMemcpy(&count, rt.atlas_exact_count, sizeof count, cudaMemcpyDeviceToHost), "atlas exact count");
+        return static_cast<long long>(count);
+    } catch (...) {
+        return -1;
+    }
+}
+
 // Device-pointer atlas frames (no reference counterpart): sources and output
 // in device memory, enqueued on `stream` without synchronising.
 int fractal_gb300_atlas_field_device(const float* parent, int parent_width, int parent_height, int parent_max_iter,
@@ -2689,7 +2746,7 @@ int fractal_gb300_atlas_field_device(const float* parent, int parent_width, int 
         a.child = child;
         a.field_out = output;
         void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
-        check_cuda(launch_atlas(a, tables, stream), "atlas kernel launch");
+        check_cuda(run_atlas(rt, a, tables, stream), "atlas kernel launch");
         release_scratch(rt, stream);
     });
 }
@@ -2715,7 +2772,7 @@ int fractal_gb300_atlas_colourise_device(const float* parent, int parent_width, 
         a.child = child;
         a.rgb = output;
         void* tables = scratch(rt, kScratchAtlas, atlas_table_bytes(a));
-        check_cuda(launch_atlas(a, tables, stream), "atlas kernel launch");
+        check_cuda(run_atlas(rt, a, tables, stream), "atlas kernel launch");
         release_scratch(rt, stream);
     });
 }

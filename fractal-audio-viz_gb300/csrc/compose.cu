@@ -18,18 +18,21 @@
 // field bias, a 2-D smoothstep seam), which the KFP colour pass then reads
 // from L2.
 //
-// Two launches per frame:
-//   atlas_axes_kernel  the six per-frame tables (parent x/y and child x/y
-//                      bilinear axes: fill_bilinear_axis, renderer.cpp:
-//                      4931-4961; the child's two edge ramps), one thread
-//                      per entry (~12k entries at 4K);
-//   atlas_kernel       four output pixels per thread: 16-byte field stores
-//                      or 12-byte RGB stores.
+// Three launches per frame:
+//   atlas_axes_kernel   the per-frame tables (parent x/y and child x/y
+//                       bilinear axes: fill_bilinear_axis, renderer.cpp:
+//                       4931-4961; the child's edge ramps), one thread per
+//                       entry (~12k entries at 4K);
+//   atlas_kernel        four output pixels per thread, no FP64: 16-byte
+//                       field stores or 12-byte RGB stores; pixels it cannot
+//                       decide exactly are queued;
+//   atlas_exact_kernel  the queued pixels in the reference's FP64 form.
 // This unit is compiled without FMA contraction, so every double and float
 // operation rounds on its own exactly as in the reference: frames are
 // bit-identical, not merely close.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <limits>
@@ -86,7 +89,7 @@ __device__ __forceinline__ Df df_add(Df a, Df b) {
 
 // sample_bilinear_mapped_preserving_interior exactly as the reference forms
 // it, in FP64 (renderer.cpp:5141-5208).
-__device__ __noinline__ Sample sample_exact(const SourceView& src, const float values[4], double xw, double yw) {
+__device__ __forceinline__ Sample sample_exact(const SourceView& src, const float values[4], double xw, double yw) {
     const double weights[4] = {(1.0 - yw) * (1.0 - xw), (1.0 - yw) * xw, yw * (1.0 - xw), yw * xw};
     const double limit = static_cast<double>(src.max_iter) - src.bias;
     double interior = 0.0, exterior = 0.0, sum = 0.0;
@@ -102,7 +105,7 @@ __device__ __noinline__ Sample sample_exact(const SourceView& src, const float v
     }
     if (interior >= 0.5) return Sample{static_cast<float>(src.max_iter), true};
     if (exterior <= 1.0e-12) return Sample{0.0f, false};
-    return Sample{static_cast<float>(sum / exterior), false};
+    return Sample{static_cast<float>(exterior == 1.0 ? sum : sum / exterior), false};  // x / 1 = x
 }
 
 // Df quotient a / b (b > 0): one float quotient refined by the exact
@@ -119,10 +122,23 @@ __device__ __forceinline__ Df df_div(Df a, Df b) {
 // of v rounds to the same float; false when v is too close to a rounding
 // boundary to decide.
 __device__ __forceinline__ bool decided_float(Df v, float tolerance, float& out) {
-    const float up = (nextafterf(v.hi, INFINITY) - v.hi) * 0.5f;
-    const float down = (v.hi - nextafterf(v.hi, -INFINITY)) * 0.5f;
+    // Half the gaps to the neighbouring floats of v.hi from its exponent
+    // bits: 2^(e-24) on both sides, halved towards zero at a power of two.
+    const unsigned bits = __float_as_uint(v.hi) & 0x7fffffffu;
     out = v.hi;
+    if (bits < 0x0d800000u || bits >= 0x7f000000u) return false;  // tiny, huge or non-finite: undecided
+    const float half = __uint_as_float(bits & 0x7f800000u) * 0x1p-24f;
+    const float inner = (bits & 0x007fffffu) == 0u ? half * 0.5f : half;
+    const float up = v.hi > 0.0f ? half : inner;
+    const float down = v.hi > 0.0f ? inner : half;
     return v.lo + tolerance < up && tolerance - v.lo < down;
+}
+
+// Df times a float (error < 2^-47 relative).
+__device__ __forceinline__ Df df_mul_f(Df a, float s) {
+    const float p = a.hi * s;
+    const float e = __fmaf_rn(a.hi, s, -p) + a.lo * s;
+    return quick_two_sum(p, e);
 }
 
 // The same sample without FP64, with identical results.  The four bilinear
@@ -131,15 +147,19 @@ __device__ __forceinline__ bool decided_float(Df v, float tolerance, float& out)
 // over exterior corners follow.  The reference's double forms differ from
 // these exact sums by < 2^-49 relatively, the double-float forms by
 // < 2^-44, so:
-//  * interior: I >= 1/2 is decided when |I - 1/2| > 2^-40;
-//  * a value: float(N / E) is decided when N / E +- 2^-40 max |v_k + bias|
+//  * interior: I >= 1/2 is decided when |I - 1/2| > 2^-42;
+//  * a value: float(N / E) is decided when N / E +- 2^-42 max |v_k + bias|
 //    lies inside one float's rounding cell (E = 1 exactly in real
-//    arithmetic when all four corners are exterior, so no division then);
+//    arithmetic when all four corners are exterior, so no division then).
+//    Both error bounds are relative to the sample scale, not to E: the
+//    reference's D errs by < 14 * 2^-53 max |v_k + bias| (weights, products,
+//    sums, quotient), the double-float N / E by < 2^-46 of it;
 //  * E <= 1e-12 (no usable corner) is decided away from 1e-12.
 // Undecided samples (about one in 2^16, and exact 1/2 ties of I) take the
 // reference's FP64 form.
+template <bool Exact>
 __device__ __forceinline__ Sample sample_preserving_interior(const SourceView& src, const AtlasAxis& ax,
-                                                             const AtlasAxis& ay, int x, int y) {
+                                                             const AtlasAxis& ay, int x, int y, bool& undecided) {
     const int x0 = __ldg(ax.index0 + x), x1 = __ldg(ax.index1 + x);
     const float xw = __ldg(ax.weight + x);
     const int y0 = __ldg(ay.index0 + y), y1 = __ldg(ay.index1 + y);
@@ -147,6 +167,9 @@ __device__ __forceinline__ Sample sample_preserving_interior(const SourceView& s
     const float* top = src.data + static_cast<long long>(y0) * src.width;
     const float* bottom = src.data + static_cast<long long>(y1) * src.width;
     const float values[4] = {__ldg(top + x0), __ldg(top + x1), __ldg(bottom + x0), __ldg(bottom + x1)};
+    if constexpr (Exact) {
+        return sample_exact(src, values, static_cast<double>(xw), static_cast<double>(yw));
+    }
     int interior_mask = 0, exterior_mask = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -159,6 +182,28 @@ __device__ __forceinline__ Sample sample_preserving_interior(const SourceView& s
         }
     }
     if (interior_mask == 15) return Sample{static_cast<float>(src.max_iter), true};
+    if (exterior_mask == 15) {
+        // N = T + y (B - T) with the row values T = u0 + x (u1 - u0),
+        // B = u2 + x (u3 - u2): the same exact real as the four weighted
+        // corners (weights sum to 1), in fewer double-float steps.
+        Df u0{values[0], 0.0f}, u2{values[2], 0.0f};
+        if (src.bias_hi != 0.0f) {
+            u0 = two_sum(values[0], src.bias_hi);
+            u0 = quick_two_sum(u0.hi, u0.lo + src.bias_lo);
+            u2 = two_sum(values[2], src.bias_hi);
+            u2 = quick_two_sum(u2.hi, u2.lo + src.bias_lo);
+        }
+        const Df row_top = df_add(u0, df_mul_f(two_sum(values[1], -values[0]), xw));
+        const Df row_bottom = df_add(u2, df_mul_f(two_sum(values[3], -values[2]), xw));
+        const Df n = df_add(row_top, df_mul_f(df_add(row_bottom, Df{-row_top.hi, -row_top.lo}), yw));
+        const float magnitude = fmaxf(fmaxf(fabsf(values[0]), fabsf(values[1])), fmaxf(fabsf(values[2]),
+                                                                                      fabsf(values[3])))
+            + fabsf(src.bias_hi);
+        float result;
+        if (decided_float(n, magnitude * 0x1p-42f + 0x1p-120f, result)) return Sample{result, false};
+        undecided = true;
+        return Sample{0.0f, false};
+    }
     const Df x_left = two_sum(1.0f, -xw), y_top = two_sum(1.0f, -yw);
     const Df x_right{xw, 0.0f}, y_bottom{yw, 0.0f};
     const Df w[4] = {df_mul(y_top, x_left), df_mul(y_top, x_right), df_mul(y_bottom, x_left),
@@ -171,8 +216,8 @@ __device__ __forceinline__ Sample sample_preserving_interior(const SourceView& s
             if (interior_mask & (1 << i)) interior = df_add(interior, w[i]);
         }
         const Df margin = df_add(interior, Df{-0.5f, 0.0f});
-        if (margin.hi > 0x1p-40f) return Sample{static_cast<float>(src.max_iter), true};
-        decided = margin.hi < -0x1p-40f;
+        if (margin.hi > 0x1p-42f) return Sample{static_cast<float>(src.max_iter), true};
+        decided = margin.hi < -0x1p-42f;
     }
     if (decided) {
         Df n{0.0f, 0.0f}, e{0.0f, 0.0f};
@@ -190,15 +235,14 @@ __device__ __forceinline__ Sample sample_preserving_interior(const SourceView& s
             e = df_add(e, w[i]);
         }
         float result;
-        if (exterior_mask == 15) {
-            if (decided_float(n, magnitude * 0x1p-40f + 0x1p-120f, result)) return Sample{result, false};
-        } else if (e.hi > 2.0e-12f) {
-            if (decided_float(df_div(n, e), magnitude * 0x1p-40f + 0x1p-120f, result)) return Sample{result, false};
+        if (e.hi > 2.0e-12f) {
+            if (decided_float(df_div(n, e), magnitude * 0x1p-42f + 0x1p-120f, result)) return Sample{result, false};
         } else if (e.hi < 0.5e-12f) {
             return Sample{0.0f, false};
         }
     }
-    return sample_exact(src, values, static_cast<double>(xw), static_cast<double>(yw));
+    undecided = true;  // left to the exact pass
+    return Sample{0.0f, false};
 }
 
 // write_colour_pixel (renderer.cpp:5210-5237).  The palette index is
@@ -270,38 +314,21 @@ __device__ __forceinline__ std::uint8_t blend_byte(std::uint8_t p, std::uint8_t 
     return static_cast<std::uint8_t>(base < 0 ? 0 : (base > 255 ? 255 : base));
 }
 
-// One entry of a bilinear axis: `source` samples resampled to `destination`
-// after a centred crop by `zoom` (at least 1).
-__device__ void axis_entry(int source, int destination, double zoom, int d, int* index0, int* index1,
-                           float* weight) {
-    zoom = zoom > 1.0 ? zoom : 1.0;
-    const double inverse = 1.0 / zoom;
-    const double crop = static_cast<double>(source) * inverse;
-    const double left = (static_cast<double>(source) - crop) * 0.5;
-    const double step = crop / static_cast<double>(destination);
-    double position = left + (static_cast<double>(d) + 0.5) * step - 0.5;
-    const double top = static_cast<double>(source - 1);
-    position = position < 0.0 ? 0.0 : (position > top ? top : position);
-    const int i = static_cast<int>(floor(position));
-    index0[d] = i;
-    index1[d] = i + 1 < source - 1 ? i + 1 : source - 1;
-    weight[d] = static_cast<float>(position - static_cast<double>(i));
-}
-
-// fill_bilinear_axis_window (renderer.cpp:4969-5003) at the visible child
-// pixel d: the halo offset cancels, so the logical pixel is d + 1/2.
-__device__ void window_entry(int source, double span, double zoom, int d, int* index0, int* index1,
-                             float* weight) {
-    zoom = zoom > 1.0 ? zoom : 1.0;
-    const double crop = static_cast<double>(source) / zoom;
-    const double left = (static_cast<double>(source) - crop) * 0.5;
+// One entry of a bilinear axis (fill_bilinear_axis, renderer.cpp:4931-4961):
+// `source` samples resampled after a centred crop, position
+// left + (d + 1/2) step - 1/2 with the axis constants formed on the host in
+// the reference's order; the window form (fill_bilinear_axis_window,
+// renderer.cpp:4969-5003, at the visible child pixel d, where the halo
+// offset cancels) is left + (d + 1/2) crop / span - 1/2.
+__device__ void axis_entry(const AtlasAxisPlan& plan, int d, int* index0, int* index1, float* weight) {
     const double logical = static_cast<double>(d) + 0.5;
-    double position = left + logical * crop / span - 0.5;
-    const double top = static_cast<double>(source - 1);
+    double position = plan.window ? plan.left + logical * plan.crop / plan.span - 0.5
+                                  : plan.left + logical * plan.step - 0.5;
+    const double top = static_cast<double>(plan.source - 1);
     position = position < 0.0 ? 0.0 : (position > top ? top : position);
     const int i = static_cast<int>(floor(position));
     index0[d] = i;
-    index1[d] = i + 1 < source - 1 ? i + 1 : source - 1;
+    index1[d] = i + 1 < plan.source - 1 ? i + 1 : plan.source - 1;
     weight[d] = static_cast<float>(position - static_cast<double>(i));
 }
 
@@ -332,6 +359,7 @@ __device__ float edge_ramp(int size, int feather, int i) {
 }
 
 __global__ void atlas_axes_kernel(const AtlasLaunch a, AtlasTables t) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.exact_count = 0;
     const int segments[7] = {t.parent_x_size, t.parent_y_size, t.child_x_size, t.child_y_size, t.edge_x_size,
                              t.edge_y_size, t.alpha_size};
     int total = 0;
@@ -341,32 +369,10 @@ __global__ void atlas_axes_kernel(const AtlasLaunch a, AtlasTables t) {
         int d = e, s = 0;
         while (d >= segments[s]) d -= segments[s++];
         switch (s) {
-            case 0:
-                axis_entry(a.parent_width, t.parent_x_size, a.parent_zoom, d, t.parent_x.i0, t.parent_x.i1,
-                           t.parent_x.w);
-                break;
-            case 1:
-                axis_entry(a.parent_height, t.parent_y_size, a.parent_zoom, d, t.parent_y.i0, t.parent_y.i1,
-                           t.parent_y.w);
-                break;
-            case 2:
-                if (a.mode == kAtlasKfpSurface) {
-                    window_entry(a.child_width, static_cast<double>(t.child_x_size), a.child_zoom, d, t.child_x.i0,
-                                 t.child_x.i1, t.child_x.w);
-                } else {
-                    axis_entry(a.child_width, t.child_x_size, a.child_zoom, d, t.child_x.i0, t.child_x.i1,
-                               t.child_x.w);
-                }
-                break;
-            case 3:
-                if (a.mode == kAtlasKfpSurface) {
-                    window_entry(a.child_height, static_cast<double>(t.child_y_size), a.child_zoom, d, t.child_y.i0,
-                                 t.child_y.i1, t.child_y.w);
-                } else {
-                    axis_entry(a.child_height, t.child_y_size, a.child_zoom, d, t.child_y.i0, t.child_y.i1,
-                               t.child_y.w);
-                }
-                break;
+            case 0: axis_entry(t.plan[0], d, t.parent_x.i0, t.parent_x.i1, t.parent_x.w); break;
+            case 1: axis_entry(t.plan[1], d, t.parent_y.i0, t.parent_y.i1, t.parent_y.w); break;
+            case 2: axis_entry(t.plan[2], d, t.child_x.i0, t.child_x.i1, t.child_x.w); break;
+            case 3: axis_entry(t.plan[3], d, t.child_y.i0, t.child_y.i1, t.child_y.w); break;
             case 4:
                 t.edge_x[d] = edge_ramp(t.edge_x_size, a.feather, d);
                 break;
@@ -406,18 +412,19 @@ __device__ __forceinline__ float seam_alpha(const AtlasLaunch& a, int cx, int cy
 }
 
 // Scalar output of one pixel (fractal_atlas_field_ex's per-pixel body).
-__device__ __forceinline__ float field_pixel(const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
+template <bool Exact>
+__device__ __forceinline__ float field_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
                                              int x, int y) {
     const float bias = a.output_bias_f;
     if (a.full_child) {
-        const Sample c = sample_preserving_interior(child, a.child_x, a.child_y, x, y);
+        const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, x, y, undecided);
         return c.inside ? a.interior_value : c.value - bias;
     }
-    const Sample p = sample_preserving_interior(parent, a.parent_x, a.parent_y, x, y);
+    const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
     float value = p.inside ? a.interior_value : p.value - bias;
     const int cx = x - a.child_left, cy = y - a.child_top;
     if (in_child(a, cx, cy)) {
-        const Sample c = sample_preserving_interior(child, a.child_x, a.child_y, cx, cy);
+        const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
         const float child_value = c.inside ? a.interior_value : c.value - bias;
         const float alpha = seam_alpha(a, cx, cy);
         value = value * (1.0f - alpha) + child_value * alpha;
@@ -433,13 +440,14 @@ __device__ __forceinline__ float encode_sample(const AtlasLaunch& a, float value
 
 // Scalar surface of one pixel (fractal_atlas_colourise_kfp_raw's parent
 // view, then the child's ownership blend).
-__device__ __forceinline__ float surface_pixel(const AtlasLaunch& a, const SourceView& parent,
+template <bool Exact>
+__device__ __forceinline__ float surface_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent,
                                                const SourceView& child, int x, int y) {
-    const Sample p = sample_preserving_interior(parent, a.parent_x, a.parent_y, x, y);
+    const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
     const float parent_value = p.inside ? a.interior_value : encode_sample(a, p.value);
     const int cx = x - a.child_left, cy = y - a.child_top;
     if (!in_child(a, cx, cy)) return parent_value;
-    const Sample c = sample_preserving_interior(child, a.child_x, a.child_y, cx, cy);
+    const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
     const float child_value = c.inside ? a.interior_value : encode_sample(a, c.value);
     const float alpha = seam_alpha(a, cx, cy);
     if (alpha >= 0.999999f) return child_value;
@@ -447,27 +455,28 @@ __device__ __forceinline__ float surface_pixel(const AtlasLaunch& a, const Sourc
 }
 
 // RGB8 of one pixel (atlas_colourise_impl's per-pixel body).
-__device__ __forceinline__ void colour_pixel(const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
+template <bool Exact>
+__device__ __forceinline__ void colour_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
                                              int x, int y, std::uint8_t* dst) {
     const float cap = static_cast<float>(a.palette_iter);
     if (a.full_child) {
-        const Sample c = sample_preserving_interior(child, a.child_x, a.child_y, x, y);
+        const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, x, y, undecided);
         aurora_colour(a, c.inside ? cap : c.value, dst);
         return;
     }
     const int cx = x - a.child_left, cy = y - a.child_top;
     if (!in_child(a, cx, cy)) {
-        const Sample p = sample_preserving_interior(parent, a.parent_x, a.parent_y, x, y);
+        const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
         aurora_colour(a, p.inside ? cap : p.value, dst);
         return;
     }
-    const Sample c = sample_preserving_interior(child, a.child_x, a.child_y, cx, cy);
+    const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
     const float alpha = seam_alpha(a, cx, cy);
     if (alpha >= 0.999999f) {
         aurora_colour(a, c.inside ? cap : c.value, dst);
         return;
     }
-    const Sample p = sample_preserving_interior(parent, a.parent_x, a.parent_y, x, y);
+    const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
     std::uint8_t prgb[3], crgb[3];
     aurora_colour(a, p.inside ? cap : p.value, prgb);
     aurora_colour(a, c.inside ? cap : c.value, crgb);
@@ -540,9 +549,10 @@ __device__ __forceinline__ void rgb_pixel(const AtlasLaunch& a, int x, int y, st
 
 // crop_colourise_impl's per-pixel body (renderer.cpp:19053-19078): interior
 // colour for an interior sample, else the palette entry (no cap test).
-__device__ __forceinline__ void crop_aurora_pixel(const AtlasLaunch& a, const SourceView& parent, int x, int y,
+template <bool Exact>
+__device__ __forceinline__ void crop_aurora_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent, int x, int y,
                                                   std::uint8_t* dst) {
-    const Sample p = sample_preserving_interior(parent, a.parent_x, a.parent_y, x, y);
+    const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
     if (p.inside) {
         dst[0] = static_cast<std::uint8_t>(a.interior[0]);
         dst[1] = static_cast<std::uint8_t>(a.interior[1]);
@@ -552,10 +562,40 @@ __device__ __forceinline__ void crop_aurora_pixel(const AtlasLaunch& a, const So
     palette_entry(a, p.value, dst);
 }
 
-// Four horizontally adjacent pixels per thread.  `quads_per_row` =
-// ceil(width / 4); a row's last quad may be partial.  Full quads of a row
-// whose width is a multiple of four store 16 bytes (field) or 12 bytes (RGB,
-// three aligned words); everything else stores per pixel.
+// One output pixel of any mode: a float (field_out modes) into *value or
+// three bytes into rgb.
+template <bool Exact>
+__device__ __forceinline__ void atlas_pixel(const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
+                                            int x, int y, bool& undecided, float* value, std::uint8_t* rgb) {
+    switch (a.mode) {
+        case kAtlasKfpSurface: *value = surface_pixel<Exact>(undecided, a, parent, child, x, y); break;
+        case kAtlasCropField: *value = crop_pixel(a, x, y); break;
+        case kAtlasField: *value = field_pixel<Exact>(undecided, a, parent, child, x, y); break;
+        case kAtlasRgb: rgb_pixel(a, x, y, rgb); break;
+        case kAtlasCropAurora: crop_aurora_pixel<Exact>(undecided, a, parent, x, y, rgb); break;
+        default: colour_pixel<Exact>(undecided, a, parent, child, x, y, rgb); break;
+    }
+}
+
+// Queues pixel `index` for the exact pass (warp-aggregated append).
+__device__ __forceinline__ void queue_exact(const AtlasLaunch& a, bool undecided, unsigned index) {
+    const unsigned active = __activemask();
+    const unsigned want = __ballot_sync(active, undecided);
+    if (!undecided) return;
+    const int leader = __ffs(want) - 1;
+    const int lane = threadIdx.x & 31;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(a.exact_count, static_cast<unsigned>(__popc(want)));
+    base = __shfl_sync(want, base, leader);
+    a.exact_pixels[base + __popc(want & ((1u << lane) - 1u))] = index;
+}
+
+// The fast pass: four horizontally adjacent pixels per thread, no FP64.
+// `quads_per_row` = ceil(width / 4); a row's last quad may be partial.  Full
+// quads of a row whose width is a multiple of four store 16 bytes (field) or
+// 12 bytes (RGB, three aligned words); everything else stores per pixel.  A
+// pixel whose sample could not be decided in double-float is written with a
+// placeholder and queued for atlas_exact_kernel, which rewrites it.
 __global__ void __launch_bounds__(256) atlas_kernel(const AtlasLaunch a, unsigned quads_per_row,
                                                     unsigned total_quads) {
     const bool vector_rows = (a.out_width & 3) == 0;
@@ -565,38 +605,21 @@ __global__ void __launch_bounds__(256) atlas_kernel(const AtlasLaunch a, unsigne
         const int x0 = static_cast<int>(q - static_cast<unsigned>(y) * quads_per_row) * 4;
         const long long row = static_cast<long long>(y) * a.out_width;
         const int n = a.out_width - x0 < 4 ? a.out_width - x0 : 4;
-        if (a.field_out) {
-            float v[4];
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        std::uint8_t out[12];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (k >= n) {
-                    v[k] = 0.0f;
-                } else if (a.mode == kAtlasKfpSurface) {
-                    v[k] = surface_pixel(a, parent, child, x0 + k, y);
-                } else if (a.mode == kAtlasCropField) {
-                    v[k] = crop_pixel(a, x0 + k, y);
-                } else {
-                    v[k] = field_pixel(a, parent, child, x0 + k, y);
-                }
-            }
+        for (int k = 0; k < 4; ++k) {
+            bool undecided = false;
+            if (k < n) atlas_pixel<false>(a, parent, child, x0 + k, y, undecided, v + k, out + 3 * k);
+            queue_exact(a, undecided, static_cast<unsigned>(row + x0 + k));
+        }
+        if (a.field_out) {
             if (vector_rows) {
                 __stcs(reinterpret_cast<float4*>(a.field_out + row + x0), make_float4(v[0], v[1], v[2], v[3]));
             } else {
                 for (int k = 0; k < n; ++k) a.field_out[row + x0 + k] = v[k];
             }
         } else {
-            std::uint8_t out[12];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (k >= n) continue;
-                if (a.mode == kAtlasRgb) {
-                    rgb_pixel(a, x0 + k, y, out + 3 * k);
-                } else if (a.mode == kAtlasCropAurora) {
-                    crop_aurora_pixel(a, parent, x0 + k, y, out + 3 * k);
-                } else {
-                    colour_pixel(a, parent, child, x0 + k, y, out + 3 * k);
-                }
-            }
             std::uint8_t* dst = a.rgb + 3 * (row + x0);
             if (vector_rows) {
                 std::uint32_t* words = reinterpret_cast<std::uint32_t*>(dst);
@@ -612,11 +635,36 @@ __global__ void __launch_bounds__(256) atlas_kernel(const AtlasLaunch a, unsigne
     }
 }
 
+// The exact pass: the queued pixels, one per thread, every sample in the
+// reference's FP64 form.  Dense warps, so the FP64 pipe runs with all lanes
+// active; the list is usually a few hundred pixels, up to a few percent of a
+// frame whose axes fall on exact halves (2:1 resampling).
+__global__ void __launch_bounds__(256) atlas_exact_kernel(const AtlasLaunch a) {
+    const SourceView parent = parent_view(a), child = child_view(a);
+    const unsigned count = *a.exact_count;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const unsigned index = a.exact_pixels[i];
+        const int y = static_cast<int>(index / static_cast<unsigned>(a.out_width));
+        const int x = static_cast<int>(index - static_cast<unsigned>(y) * static_cast<unsigned>(a.out_width));
+        bool undecided = false;
+        float value = 0.0f;
+        std::uint8_t rgb[3];
+        atlas_pixel<true>(a, parent, child, x, y, undecided, &value, rgb);
+        if (a.field_out) {
+            a.field_out[index] = value;
+        } else {
+            a.rgb[3ull * index] = rgb[0];
+            a.rgb[3ull * index + 1] = rgb[1];
+            a.rgb[3ull * index + 2] = rgb[2];
+        }
+    }
+}
+
 }  // namespace
 
 // Entries of each per-frame table: the bilinear axes the mode reads, the
 // float edge ramps (interior-preserving modes) or the double alpha table
-// (RGB composite).
+// (RGB composite); and the four axes' constants.
 static void atlas_table_sizes(const AtlasLaunch& a, AtlasTables& t) {
     t.parent_x_size = a.full_child ? 0 : a.out_width;
     t.parent_y_size = a.full_child ? 0 : a.out_height;
@@ -626,6 +674,22 @@ static void atlas_table_sizes(const AtlasLaunch& a, AtlasTables& t) {
     t.edge_x_size = ramps ? a.child_visible_width : 0;
     t.edge_y_size = ramps ? a.child_visible_height : 0;
     t.alpha_size = a.feather >= 2 && a.mode == kAtlasRgb ? a.feather : 0;
+    // Axis constants in the reference's operation order (fill_bilinear_axis:
+    // zoom >= 1, crop = source * (1 / zoom), left = (source - crop) / 2,
+    // step = crop / destination; the window form: crop = source / zoom).
+    const int sources[4] = {a.parent_width, a.parent_height, a.child_width, a.child_height};
+    const int sizes[4] = {t.parent_x_size, t.parent_y_size, t.child_x_size, t.child_y_size};
+    for (int k = 0; k < 4; ++k) {
+        AtlasAxisPlan& plan = t.plan[k];
+        const double zoom = std::max(k < 2 ? a.parent_zoom : a.child_zoom, 1.0);
+        const double source = static_cast<double>(sources[k]);
+        plan.source = sources[k];
+        plan.window = k >= 2 && a.mode == kAtlasKfpSurface;
+        plan.crop = plan.window ? source / zoom : source * (1.0 / zoom);
+        plan.left = (source - plan.crop) * 0.5;
+        plan.span = static_cast<double>(sizes[k]);
+        plan.step = sizes[k] > 0 ? plan.crop / static_cast<double>(sizes[k]) : 0.0;
+    }
 }
 
 std::size_t atlas_table_bytes(const AtlasLaunch& a) {
@@ -633,9 +697,11 @@ std::size_t atlas_table_bytes(const AtlasLaunch& a) {
     atlas_table_sizes(a, t);
     const std::size_t axes = static_cast<std::size_t>(t.parent_x_size) + t.parent_y_size + t.child_x_size
         + t.child_y_size;
-    // Fourteen tables, each padded to 256 bytes.
+    // Fourteen tables, each padded to 256 bytes, then the exact-pass counter
+    // and pixel list (one entry per output pixel at most).
     return axes * 12 + (static_cast<std::size_t>(t.edge_x_size) + t.edge_y_size) * 4
-        + static_cast<std::size_t>(t.alpha_size) * 8 + 16 * 256;
+        + static_cast<std::size_t>(t.alpha_size) * 8 + 16 * 256 + 256
+        + static_cast<std::size_t>(a.out_width) * a.out_height * 4;
 }
 
 namespace {
@@ -701,6 +767,8 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
     t.edge_y = reinterpret_cast<float*>(take(t.edge_y_size * sizeof(float)));
     t.alpha = reinterpret_cast<double*>(take(t.alpha_size * sizeof(double)));
     a.alpha = t.alpha;
+    a.exact_count = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
+    a.exact_pixels = reinterpret_cast<unsigned*>(take(static_cast<std::size_t>(a.out_width) * a.out_height * 4));
     a.parent_x = AtlasAxis{t.parent_x.i0, t.parent_x.i1, t.parent_x.w};
     a.parent_y = AtlasAxis{t.parent_y.i0, t.parent_y.i1, t.parent_y.w};
     a.child_x = AtlasAxis{t.child_x.i0, t.child_x.i1, t.child_x.w};
@@ -710,11 +778,10 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
 
     const int entries = t.parent_x_size + t.parent_y_size + t.child_x_size + t.child_y_size + t.edge_x_size
         + t.edge_y_size + t.alpha_size;
-    if (entries > 0) {
-        atlas_axes_kernel<<<static_cast<unsigned>((entries + 255) / 256), 256, 0, stream>>>(a, t);
-        const cudaError_t status = cudaGetLastError();
-        if (status != cudaSuccess) return status;
-    }
+    // Always launched: it also clears the exact-pass counter.
+    atlas_axes_kernel<<<static_cast<unsigned>(entries > 0 ? (entries + 255) / 256 : 1), 256, 0, stream>>>(a, t);
+    cudaError_t status = cudaGetLastError();
+    if (status != cudaSuccess) return status;
     int device = 0, sms = 152;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -723,6 +790,9 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
     long long blocks = (static_cast<long long>(total) + 255) / 256;
     if (blocks > static_cast<long long>(sms) * 8) blocks = static_cast<long long>(sms) * 8;
     atlas_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, stream>>>(a, quads_per_row, total);
+    status = cudaGetLastError();
+    if (status != cudaSuccess) return status;
+    atlas_exact_kernel<<<static_cast<unsigned>(sms) * 2, 256, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

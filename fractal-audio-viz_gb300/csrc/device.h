@@ -396,7 +396,14 @@ struct AtlasAxis {
     const int* index1;
     const float* weight;
 };
+// Per-axis constants, formed on the host in the reference's order.
+struct AtlasAxisPlan {
+    double left, step, crop, span;
+    int source;
+    int window;  // fill_bilinear_axis_window form (raw KFP child axes)
+};
 struct AtlasTables {
+    AtlasAxisPlan plan[4];  // parent x, parent y, child x, child y
     struct Axis {
         int* i0;
         int* i1;
@@ -441,6 +448,8 @@ struct AtlasLaunch {
     float output_bias_f;
     int output_bias_exact;                  // output_bias is a float
     float interior_value;                   // the output value of an interior sample
+    unsigned* exact_count;                  // pixels queued for the exact (FP64) pass
+    unsigned* exact_pixels;
     // Scalar output (fractal_atlas_field_ex; the KFP surface, where
     // output_bias is the KFP field bias and effective_iter the cap) ...
     float* field_out;

@@ -73,6 +73,7 @@ struct ThreadRuntime {
     cudaStream_t tile_stream = nullptr;  // stream of the last tile-scheduled batch
     cudaStream_t batch_stream = nullptr; // stream of the last keyframe batch
     int last_tiles = 0;
+    unsigned* atlas_exact_count = nullptr;  // exact-pass counter of the last atlas frame
     bool shapes_pinned = false;
     double last_kernel_ms = 0.0;
     ~ThreadRuntime();

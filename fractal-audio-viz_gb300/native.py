@@ -380,6 +380,7 @@ _GB300_ABI = (
      (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
       ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
       ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)),
+    ("fractal_gb300_atlas_last_exact_pixels", ctypes.c_longlong, ()),
     ("fractal_gb300_render_keyframes_device", ctypes.c_int,
      (ctypes.POINTER(Keyframe), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions), ctypes.c_int,

@@ -446,6 +446,11 @@ int fractal_gb300_atlas_kfp_surface_device(const float *parent, int parent_width
                                            double child_fraction, double child_zoom, int max_iter,
                                            double field_bias, void *stream);
 
+/* Pixels of the last atlas frame of the calling thread that the fast
+ * (FP32 / double-float) pass could not decide and the exact FP64 pass
+ * computed; synchronises the device.  -1 before any atlas frame. */
+long long fractal_gb300_atlas_last_exact_pixels(void);
+
 /* One keyframe of a batch: device outputs (`counts` may be NULL), its zoom,
  * the reference handle it renders from (NULL: the direct FP64 path at the
  * batch centre, which the reference pipeline takes below 1e12,
