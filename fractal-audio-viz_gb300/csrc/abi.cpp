@@ -17,6 +17,7 @@
 #include <functional>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "device.h"
@@ -235,11 +236,21 @@ DeepGeometry deep_geometry(const fx::Fe& zoom, int width, int height, int coordi
     return g;
 }
 
+// A point render's inputs (fractal_render_points_impl, renderer.cpp:
+// 20019-20186): device dc list, the largest |dc| (it replaces the view
+// radius in the BLA and series decisions) and the exact-repair flags.
+struct PointInput {
+    const fx::Sc* points = nullptr;
+    fx::Fe radius = {0.0, 0};
+    std::uint8_t* exact_flags = nullptr;
+};
+
 void launch_deep_mandelbrot(ReferenceContext& ctx, DeviceTables& dev, const Outputs& out, int width, int height,
                             const fx::Fe& zoom, int max_iter, int series_order, int series_block,
                             const FractalRenderOptions& o, bool collect_stats, ThreadRuntime& rt,
-                            cudaStream_t stream) {
-    const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+                            cudaStream_t stream, const PointInput* points = nullptr) {
+    DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
+    if (points) g.current_input_radius = points->radius;
     const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
     const bool disable_bla = !covers || o.disable_bla != 0;
     const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
@@ -295,13 +306,15 @@ void launch_deep_mandelbrot(ReferenceContext& ctx, DeviceTables& dev, const Outp
         p.budget_ns = static_cast<unsigned long long>(o.time_budget_ms) * 1000000ull;
     }
     p.stats = collect_stats ? rt.stats : nullptr;
+    p.points = points ? points->points : nullptr;
+    p.exact_flags = points ? points->exact_flags : nullptr;
     check_cuda(launch_plain_mandelbrot(p, out.p_iter != nullptr, collect_stats, stream),
                "plain Mandelbrot kernel launch");
 }
 
 void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outputs& out, int width, int height,
                            const fx::Fe& zoom, int max_iter, const FractalRenderOptions& o, bool collect_stats,
-                           ThreadRuntime& rt, cudaStream_t stream) {
+                           ThreadRuntime& rt, cudaStream_t stream, const PointInput* points = nullptr) {
     const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
     AltParams p{};
     p.orbit = dev.orbit;
@@ -344,7 +357,9 @@ void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outpu
     p.disable_bla = o.disable_bla != 0 ? 1 : 0;
     p.max_lin_len = std::clamp(static_cast<int>(o.max_linear_bla_length), 2, kMaxSafeLinearBlaLength);
     p.series_on = ctx.formula == kFormulaJulia && ctx.series.enabled && ctx.series.iteration < max_iter
-        && dev.series_terms > 1;
+        && dev.series_terms > 1
+        && (points == nullptr || fx::fe_cmp(points->radius, fx::fe_sqrt(ctx.series.r2)) <= 0);
+    p.points = points ? points->points : nullptr;
     p.cycle = (o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0)) ? 1 : 0;
     if (o.time_budget_ms > 0) {
         check_cuda(launch_stamp_time(rt.stamp, stream), "time stamp launch");
@@ -1621,6 +1636,182 @@ int fractal_render_reference_ex_planes(float* output, int width, int height, con
     });
 }
 
+}  // extern "C"
+
+namespace {
+
+constexpr int kMaxPoints = 100'000'000;          // MAX_NATIVE_POINTS (renderer.cpp:92)
+constexpr int kMaxExactRepairPoints = 8192;      // MAX_EXACT_POINT_REPAIR_PIXELS (renderer.cpp:76)
+
+// fractal_render_points_impl (renderer.cpp:20019-20186): an arbitrary list of
+// scaled offsets from the reference centre rendered by the deep kernels.
+// Strict Mandelbrot lists of at most 8192 points repair their glitch pixels
+// exactly: the kernel flags them, the host iterates each in MPFR (as the
+// reference does) on `threads` workers, and any the repair declines are
+// rendered again without the flag (rebase or NaN per the options).
+int render_points(float* output, int count, const char* zoom_text, const double* real, const double* imag,
+                  const std::int32_t* exponents, void* handle, int max_iter, int threads, int series_order,
+                  int series_block, const FractalRenderOptions* supplied, FractalRenderPlanes* planes) {
+    return guarded("native point render failed with an unknown exception", [&] {
+        if (!output || count <= 0 || count > kMaxPoints || !zoom_text || !real || !imag || !exponents || !handle
+            || (planes != nullptr && !valid_planes(planes, count, 1))) {
+            throw Failure{"invalid native point-render arguments"};
+        }
+        if (!valid_iterations(max_iter) || !valid_threads(threads) || !valid_series(series_order, series_block)) {
+            throw Failure{"invalid native point-render limits"};
+        }
+        const FractalRenderOptions o = checked_options(supplied);
+        check_backend(o);
+        const auto ctx = acquire_reference(handle);
+        if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
+        if (max_iter > ctx->requested_max_iter) throw Failure{"point render iteration count exceeds prepared reference"};
+        const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx->precision_bits);
+        std::vector<fx::Sc> points(static_cast<std::size_t>(count));
+        fx::Nrm largest = fx::nrm_make(0.0, 0);
+        for (int i = 0; i < count; ++i) {
+            fx::Sc point = fx::sc_make(real[i], imag[i], exponents[i]);
+            if (!fx::sc_finite(point)) throw Failure{"non-finite point offset"};
+            fx::sc_normalize(point);
+            points[static_cast<std::size_t>(i)] = point;
+            const fx::Nrm radius = fx::sc_norm2(point);
+            if (fx::nrm_cmp(radius, largest) > 0) largest = radius;
+        }
+        const fx::Fe point_radius = fx::fe_sqrt(fx::fe_make(largest.m, largest.e));
+        const bool repair = ctx->formula == kFormulaMandelbrot && o.strict != 0 && count <= kMaxExactRepairPoints;
+        std::vector<std::uint8_t> flags(repair ? static_cast<std::size_t>(count) : 0);
+
+        auto render_list = [&](const std::vector<fx::Sc>& list, float* out_field, FractalRenderPlanes* out_planes,
+                               std::uint8_t* host_flags) {
+            const int n = static_cast<int>(list.size());
+            render_to_host(out_field, out_planes, n, 1, [&](const Outputs& out, bool collect, ThreadRuntime& rt,
+                                                            cudaStream_t stream) {
+                const std::size_t point_bytes = list.size() * sizeof(fx::Sc);
+                const std::size_t flag_offset = (point_bytes + 255) / 256 * 256;
+                char* base = static_cast<char*>(scratch(rt, kScratchPoints, flag_offset + list.size()));
+                check_cuda(cudaMemcpyAsync(base, list.data(), point_bytes, cudaMemcpyHostToDevice, stream),
+                           "upload points");
+                PointInput input;
+                input.points = reinterpret_cast<const fx::Sc*>(base);
+                input.radius = point_radius;
+                if (host_flags) {
+                    input.exact_flags = reinterpret_cast<std::uint8_t*>(base + flag_offset);
+                    check_cuda(cudaMemsetAsync(input.exact_flags, 0, list.size(), stream), "clear repair flags");
+                }
+                std::shared_ptr<DeviceTables> dev = device_tables(*ctx);
+                if (ctx->formula != kFormulaMandelbrot) {
+                    launch_deep_alternate(*ctx, *dev, out, n, 1, zoom, max_iter, o, collect, rt, stream, &input);
+                } else {
+                    launch_deep_mandelbrot(*ctx, *dev, out, n, 1, zoom, max_iter, series_order, series_block, o,
+                                           collect, rt, stream, &input);
+                }
+                if (host_flags) {
+                    check_cuda(cudaMemcpyAsync(host_flags, input.exact_flags, list.size(), cudaMemcpyDeviceToHost,
+                                               stream), "copy repair flags");
+                }
+            });
+        };
+        render_list(points, output, planes, repair ? flags.data() : nullptr);
+        if (!repair) return;
+
+        std::vector<int> flagged;
+        for (int i = 0; i < count; ++i) {
+            if (flags[static_cast<std::size_t>(i)]) flagged.push_back(i);
+        }
+        if (flagged.empty()) return;
+        const fx::Fe spacing = deep_geometry(zoom, count, 1, o.coordinate_mode).pixel_spacing;
+        std::vector<std::uint8_t> repaired(flagged.size(), 0);
+        std::vector<ExactPlanes> repair_planes(flagged.size());
+        std::vector<float> repair_values(flagged.size());
+        const unsigned hardware = std::max(1u, std::thread::hardware_concurrency());
+        const unsigned workers = std::min<unsigned>(threads > 0 ? static_cast<unsigned>(threads) : hardware,
+                                                    static_cast<unsigned>(flagged.size()));
+        std::atomic<std::size_t> next{0};
+        auto work = [&] {
+            for (std::size_t k = next.fetch_add(1); k < flagged.size(); k = next.fetch_add(1)) {
+                const std::size_t i = static_cast<std::size_t>(flagged[k]);
+                repaired[k] = exact_mandelbrot_pixel(*ctx, points[i], max_iter, o.output_bias, o.escape_radius_mode,
+                                                     spacing, repair_values[k],
+                                                     planes ? &repair_planes[k] : nullptr) ? 1 : 0;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (unsigned w = 1; w < workers; ++w) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+        std::vector<fx::Sc> retry;
+        std::vector<int> retry_index;
+        for (std::size_t k = 0; k < flagged.size(); ++k) {
+            const std::size_t i = static_cast<std::size_t>(flagged[k]);
+            if (!repaired[k]) {
+                retry.push_back(points[i]);
+                retry_index.push_back(static_cast<int>(i));
+                continue;
+            }
+            output[i] = repair_values[k];
+            if (planes) {
+                planes->orbit_iteration[i] = repair_planes[k].iteration;
+                planes->phase[i] = repair_planes[k].phase;
+                planes->de_x[i] = repair_planes[k].de_x;
+                planes->de_y[i] = repair_planes[k].de_y;
+                planes->test1[i] = repair_planes[k].test1;
+                planes->test2[i] = repair_planes[k].test2;
+            }
+        }
+        if (retry.empty()) return;
+        // Points the exact repair declined: the kernel's own glitch handling.
+        const std::size_t n = retry.size();
+        std::vector<float> field(n);
+        std::vector<std::int64_t> iters(planes ? n : 0);
+        std::vector<double> phase(planes ? n : 0), dex(planes ? n : 0), dey(planes ? n : 0), t1(planes ? n : 0),
+            t2(planes ? n : 0);
+        FractalRenderPlanes sub{};
+        if (planes) {
+            sub = *planes;
+            sub.orbit_iteration = iters.data();
+            sub.phase = phase.data();
+            sub.de_x = dex.data();
+            sub.de_y = dey.data();
+            sub.test1 = t1.data();
+            sub.test2 = t2.data();
+        }
+        render_list(retry, field.data(), planes ? &sub : nullptr, nullptr);
+        for (std::size_t k = 0; k < n; ++k) {
+            const std::size_t i = static_cast<std::size_t>(retry_index[k]);
+            output[i] = field[k];
+            if (planes) {
+                planes->orbit_iteration[i] = iters[k];
+                planes->phase[i] = phase[k];
+                planes->de_x[i] = dex[k];
+                planes->de_y[i] = dey[k];
+                planes->test1[i] = t1[k];
+                planes->test2[i] = t2[k];
+            }
+        }
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+// fractal_render_points (renderer.h:287-300).
+int fractal_render_points(float* output, int point_count, const char* zoom_text, const double* real_mantissa,
+                          const double* imag_mantissa, const int32_t* exponents, void* handle, int max_iter,
+                          int threads, int series_order, int series_block, const FractalRenderOptions* options) {
+    return render_points(output, point_count, zoom_text, real_mantissa, imag_mantissa, exponents, handle, max_iter,
+                         threads, series_order, series_block, options, nullptr);
+}
+
+// fractal_render_points_ex_planes (renderer.h:302-320).
+int fractal_render_points_ex_planes(float* output, int point_count, const char* zoom_text,
+                                    const double* real_mantissa, const double* imag_mantissa,
+                                    const int32_t* exponents, void* handle, int max_iter, int threads,
+                                    int series_order, int series_block, const FractalRenderOptions* options,
+                                    FractalRenderPlanes* planes) {
+    return render_points(output, point_count, zoom_text, real_mantissa, imag_mantissa, exponents, handle, max_iter,
+                         threads, series_order, series_block, options, planes);
+}
+
 int fractal_render_reference_ex(float* output, int width, int height, const char* zoom_text, void* handle,
                                 int max_iter, int threads, int series_order, int series_block,
                                 const FractalRenderOptions* options) {
@@ -2722,6 +2913,26 @@ long long fractal_gb300_atlas_last_exact_pixels(void) {
     } catch (...) {
         return -1;
     }
+}
+
+// Video-frame handoff (no reference counterpart): device RGB8 packed into
+// the encoder pipe's layout (rgb24, rgb0, rgba, yuv420p, nv12 = 0..4).
+long long fractal_gb300_packed_frame_bytes(int width, int height, int format) {
+    if (!valid_dims(width, height)) return -1;
+    const std::size_t bytes = packed_frame_bytes(width, height, format);
+    return bytes == 0 ? -1 : static_cast<long long>(bytes);
+}
+
+int fractal_gb300_pack_frame_device(const uint8_t* rgb, int width, int height, int format, uint8_t* output,
+                                    void* stream_handle) {
+    return guarded("device frame pack failed with an unknown exception", [&] {
+        if (!rgb || !output || !valid_dims(width, height) || packed_frame_bytes(width, height, format) == 0) {
+            throw Failure{"invalid frame pack dimensions or format"};
+        }
+        ThreadRuntime& rt = thread_runtime();
+        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+        check_cuda(launch_pack_frame(rgb, width, height, format, output, stream), "frame pack launch");
+    });
 }
 
 // Device-pointer atlas frames (no reference counterpart): sources and output

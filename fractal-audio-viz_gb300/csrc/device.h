@@ -117,6 +117,11 @@ struct PlainParams {
     const unsigned long long* deadline_base;  // globaltimer at launch, or null
     unsigned long long budget_ns;
     unsigned long long* stats;
+    // Point renders (fractal_render_points): pixel i takes dc = points[i]
+    // instead of the grid offset; glitch pixels are flagged in exact_flags
+    // (when non-null) and left for the host's exact MPFR repair.
+    const fx::Sc* points;
+    std::uint8_t* exact_flags;
 };
 
 // Parameters of one plain-form deep alternate-formula field render.
@@ -161,6 +166,7 @@ struct AltParams {
     const unsigned long long* deadline_base;
     unsigned long long budget_ns;
     unsigned long long* stats;
+    const fx::Sc* points;  // point renders: dc = points[i] (see PlainParams)
 };
 
 // Direct (shallow, plain double) render of any formula.
@@ -468,6 +474,12 @@ std::size_t atlas_table_bytes(const AtlasLaunch& launch);
 // Builds the tables in `tables` (atlas_table_bytes, 256-byte aligned), then
 // composes the frame: two kernels on `stream`.
 cudaError_t launch_atlas(AtlasLaunch& launch, void* tables, cudaStream_t stream);
+
+// Video-frame packing (pack.cu): RGB8 into rgb24 / rgb0 / rgba / yuv420p /
+// nv12 (format 0..4); bytes of a packed frame, 0 for an unknown format.
+std::size_t packed_frame_bytes(int width, int height, int format);
+cudaError_t launch_pack_frame(const std::uint8_t* rgb, int width, int height, int format, std::uint8_t* out,
+                              cudaStream_t stream);
 
 // Records %globaltimer into *slot (the time-budget origin of the next kernel).
 cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream);

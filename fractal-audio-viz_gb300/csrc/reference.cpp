@@ -71,6 +71,12 @@ struct MpfrApi {
     int (*cmp_ui)(mpfr_srcptr, unsigned long) = nullptr;
     double (*get_d)(mpfr_srcptr, int) = nullptr;
     double (*get_d_2exp)(long*, mpfr_srcptr, int) = nullptr;
+    // Used by the exact point repair only.
+    int (*log)(mpfr_ptr, mpfr_srcptr, int) = nullptr;
+    long double (*get_ld)(mpfr_srcptr, int) = nullptr;
+    int (*cmp_d)(mpfr_srcptr, double) = nullptr;
+    int (*mul_2si)(mpfr_ptr, mpfr_srcptr, long, int) = nullptr;
+    bool exact_ok = false;
 };
 
 template <typename T>
@@ -120,6 +126,11 @@ const MpfrApi& mpfr() {
             && bind_symbol(library, "mpfr_get_d", result.get_d, e)
             && bind_symbol(library, "mpfr_get_d_2exp", result.get_d_2exp, e);
         result.ok = ok;
+        std::string unused;
+        result.exact_ok = ok && bind_symbol(library, "mpfr_log", result.log, unused)
+            && bind_symbol(library, "mpfr_get_ld", result.get_ld, unused)
+            && bind_symbol(library, "mpfr_cmp_d", result.cmp_d, unused)
+            && bind_symbol(library, "mpfr_mul_2si", result.mul_2si, unused);
         return result;
     }();
     return api;
@@ -927,6 +938,131 @@ std::vector<OrbitRec> make_orbit_records(const ReferenceContext& ctx) {
         r.glitch = (norm.m != 0.0 && fx::fe_finite(norm)) ? fx::fe_mul(norm, 1.0e-7) : fx::fe_zero();
     }
     return records;
+}
+
+
+// ------------------------------------------------------------ exact points
+namespace {
+
+// render_plane_phase (renderer.cpp:8075-8082).
+double exact_plane_phase(const fx::Sc& v) {
+    const double re = fx::sc_re_d(v);
+    const double im = fx::sc_im_d(v);
+    if (!std::isfinite(re) || !std::isfinite(im)) return 0.0;
+    constexpr double two_pi = 6.283185307179586476925286766559005768;
+    double phase = std::atan2(im, re) / two_pi;
+    phase -= std::floor(phase);
+    return std::isfinite(phase) ? phase : 0.0;
+}
+
+// render_plane_de (renderer.cpp:7845-7897), with its long double log2 term.
+bool exact_plane_de(const fx::Sc& total, const fx::Sc& derivative, const fx::Fe& spacing, double& out_re,
+                    double& out_im) {
+    constexpr long double log_two = 0.693147180559945309417232121458176568L;
+    const double mag = std::hypot(total.re, total.im);
+    if (!(mag > 0.0) || !std::isfinite(mag)) return false;
+    const double log_mag = static_cast<double>(std::log(mag) + static_cast<double>(total.e) * log_two);
+    if (!(log_mag > 0.0) || !std::isfinite(log_mag)) return false;
+    const fx::Sc unit = fx::sc_from_fe(fx::fe_from(total.re / mag, 0), fx::fe_from(total.im / mag, 0));
+    const fx::Sc spacing_c = fx::sc_from_fe(spacing, fx::fe_zero());
+    const fx::Sc den = fx::sc_mul(unit, fx::sc_mul(fx::sc_conj(derivative), spacing_c));
+    const double den2 = den.re * den.re + den.im * den.im;
+    if (!(den2 > 0.0) || !std::isfinite(den2)) return false;
+    fx::Sc r = fx::sc_make(mag * log_mag * den.re / den2, -mag * log_mag * den.im / den2,
+                           fx::sat_exp(static_cast<long long>(total.e) - den.e));
+    fx::sc_normalize(r);
+    out_re = fx::sc_re_d(r);
+    out_im = fx::sc_im_d(r);
+    return std::isfinite(out_re) && std::isfinite(out_im);
+}
+
+}  // namespace
+
+bool exact_mandelbrot_pixel(const ReferenceContext& ctx, const fx::Sc& dc, int max_iter, double output_bias,
+                            int escape_mode, const fx::Fe& pixel_spacing, float& out, ExactPlanes* planes) {
+    const MpfrApi& m = mpfr();
+    if (!m.exact_ok || ctx.x_text.empty() || ctx.y_text.empty() || ctx.precision_bits < 128
+        || !fx::sc_finite(dc)) {
+        return false;
+    }
+    // Precision floor from the pixel spacing (renderer.cpp:10953-10961).
+    long precision = ctx.precision_bits;
+    if (pixel_spacing.e < 0) {
+        const long spacing_precision = -static_cast<long>(pixel_spacing.e) + 128;
+        precision = std::min(precision, std::max(256L, spacing_precision));
+    }
+    Mp cr(precision), ci(precision), zr(precision), zi(precision), dr(precision), di(precision);
+    Mp nr(precision), ni(precision), ndr(precision), ndi(precision), t(precision), n2(precision);
+    if (m.set_str(cr, ctx.x_text.c_str(), 10, RNDN) != 0 || m.set_str(ci, ctx.y_text.c_str(), 10, RNDN) != 0) {
+        return false;
+    }
+    // c = centre + dc, the binary offset added at full precision.
+    m.set_d(t, dc.re, RNDN);
+    m.mul_2si(t, t, static_cast<long>(dc.e), RNDN);
+    m.add(cr, cr, t, RNDN);
+    m.set_d(t, dc.im, RNDN);
+    m.mul_2si(t, t, static_cast<long>(dc.e), RNDN);
+    m.add(ci, ci, t, RNDN);
+    m.set_zero(zr, 0);
+    m.set_zero(zi, 0);
+    m.set_zero(dr, 0);
+    m.set_zero(di, 0);
+    fx::Nrm previous = fx::nrm_make(0.0, 0);
+    const double escape2 = fx::escape_r2_d(escape_mode);
+    for (int iteration = 1; iteration <= max_iter; ++iteration) {
+        m.mul(nr, zr, zr, RNDN);
+        m.mul(t, zi, zi, RNDN);
+        m.sub(nr, nr, t, RNDN);
+        m.mul(ni, zr, zi, RNDN);
+        m.mul_ui(ni, ni, 2, RNDN);
+        m.add(nr, nr, cr, RNDN);
+        m.add(ni, ni, ci, RNDN);
+        m.mul(ndr, zr, dr, RNDN);
+        m.mul(t, zi, di, RNDN);
+        m.sub(ndr, ndr, t, RNDN);
+        m.mul_ui(ndr, ndr, 2, RNDN);
+        m.add_ui(ndr, ndr, 1, RNDN);
+        m.mul(ndi, zr, di, RNDN);
+        m.mul(t, zi, dr, RNDN);
+        m.add(ndi, ndi, t, RNDN);
+        m.mul_ui(ndi, ndi, 2, RNDN);
+        m.set(zr, nr, RNDN);
+        m.set(zi, ni, RNDN);
+        m.set(dr, ndr, RNDN);
+        m.set(di, ndi, RNDN);
+        m.mul(n2, zr, zr, RNDN);
+        m.mul(t, zi, zi, RNDN);
+        m.add(n2, n2, t, RNDN);
+        const fx::Sc total = fx::sc_from_fe(fe_from_mpfr(zr), fe_from_mpfr(zi));
+        const fx::Nrm current = fx::sc_norm2(total);
+        if (m.cmp_d(n2, escape2) > 0) {
+            m.log(t, n2, RNDN);
+            const long double log_magnitude = 0.5L * m.get_ld(t, RNDN);
+            if (!(log_magnitude > 0.0L) || !std::isfinite(log_magnitude)) return false;
+            constexpr long double log_two = 0.693147180559945309417232121458176568L;
+            const long double smooth = static_cast<long double>(iteration) - std::log(log_magnitude) / log_two;
+            out = static_cast<float>(smooth - static_cast<long double>(output_bias));
+            if (planes) {
+                const fx::Sc derivative = fx::sc_from_fe(fe_from_mpfr(dr), fe_from_mpfr(di));
+                planes->iteration = iteration - 1 > 0 ? iteration - 1 : 0;
+                planes->phase = exact_plane_phase(total);
+                planes->de_x = 0.0;
+                planes->de_y = 0.0;
+                double de_x = 0.0, de_y = 0.0;
+                if (exact_plane_de(total, derivative, pixel_spacing, de_x, de_y)) {
+                    planes->de_x = de_x;
+                    planes->de_y = de_y;
+                }
+                planes->test1 = fx::nrm_to_d(current);
+                planes->test2 = fx::nrm_to_d(previous);
+            }
+            return true;
+        }
+        previous = current;
+    }
+    out = static_cast<float>(static_cast<long double>(max_iter) - static_cast<long double>(output_bias));
+    if (planes) *planes = ExactPlanes{max_iter, 0.0, 0.0, 0.0, 0.0, 0.0};
+    return true;
 }
 
 }  // namespace fgb

@@ -159,4 +159,17 @@ void build_bla_on_device(ReferenceContext& ctx, int base_count);
 void build_alt_bla_on_device(ReferenceContext& ctx, int first_index, int base_count);
 void retarget_bla_on_device(ReferenceContext& ctx, const ReferenceContext& source);
 
+// One point's render planes (FractalRenderPlanes entries).
+struct ExactPlanes {
+    long long iteration;
+    double phase, de_x, de_y, test1, test2;
+};
+
+// render_exact_mandelbrot_pixel (renderer.cpp:10931-11150): the pixel at
+// centre + dc iterated from scratch in MPFR (host), with its derivative for
+// the planes.  False when the context cannot support it (no centre text, <128
+// bits, no MPFR) or the escape log is not finite.
+bool exact_mandelbrot_pixel(const ReferenceContext& ctx, const fx::Sc& dc, int max_iter, double output_bias,
+                            int escape_mode, const fx::Fe& pixel_spacing, float& out, ExactPlanes* planes);
+
 }  // namespace fgb

@@ -246,7 +246,8 @@ __global__ void __launch_bounds__(128) alt_kernel(const AltParams p) {
     if constexpr (WithPlanes) planes.clear(index, p.max_iter);
     const double xf = pixel_offset(px, p.width, p.coordinate_mode) / static_cast<double>(p.width);
     const double yf = -pixel_offset(py, p.height, p.coordinate_mode) / static_cast<double>(p.height);
-    const Sc dc = sc_from_fe(fe_mul(p.view_width, xf), fe_mul(p.view_height, yf));
+    const Sc dc = p.points ? sc_make(p.points[index].re, p.points[index].im, p.points[index].e)
+                           : sc_from_fe(fe_mul(p.view_width, xf), fe_mul(p.view_height, yf));
     const bool julia = p.formula == kFormulaJulia;
     const Sc pd = julia ? sc_zero() : dc;
     const Nrm pnorm = sc_norm2(pd);

@@ -526,9 +526,11 @@ __global__ void __launch_bounds__(128) plain_mandelbrot_kernel(const PlainParams
 
     // Pixel offsets (renderer.cpp:12764-12783): the view span times the
     // signed pixel-centre fraction, both in FloatExp.
+    // A point render takes dc from its list (renderer.cpp:12838-12842).
     const double x_fraction = pixel_offset(px, p.width, p.coordinate_mode) / static_cast<double>(p.width);
     const double y_fraction = -pixel_offset(py, p.height, p.coordinate_mode) / static_cast<double>(p.height);
-    const Sc dc = sc_from_fe(fe_mul(p.view_width, x_fraction), fe_mul(p.view_height, y_fraction));
+    const Sc dc = p.points ? sc_make(p.points[index].re, p.points[index].im, p.points[index].e)
+                           : sc_from_fe(fe_mul(p.view_width, x_fraction), fe_mul(p.view_height, y_fraction));
     const unsigned long long deadline_ns = p.deadline_base ? *p.deadline_base + p.budget_ns : 0ull;
     if constexpr (Planes) planes.clear(index, p.max_iter);
     Sc delta = dc;
@@ -598,6 +600,15 @@ __global__ void __launch_bounds__(128) plain_mandelbrot_kernel(const PlainParams
         const Fe glitch = orbit.glitch(ref);
         if (glitch.m != 0.0 && fe_cmp(fe_make(total_norm.m, total_norm.e), glitch) < 0) {
             st.add(kGlitchCount);
+            if (p.exact_flags) {
+                // Strict point renders repair the pixel exactly (MPFR, on
+                // the host) before any rebase (renderer.cpp:12944-12966).
+                p.exact_flags[index] = 1;
+                out_value = nan_f();
+                out_count = 0;
+                escaped = true;  // finished by the repair, as in the reference
+                break;
+            }
             if (p.allow_recovery && sc_finite(total) && ++rebases <= 64) {
                 delta = total;
                 ref = 0;

@@ -42,6 +42,7 @@ enum ScratchSlot {
     kScratchSeries,
     kScratchAtlas,
     kScratchSurface,
+    kScratchPoints,
     kScratchCount
 };
 

@@ -268,6 +268,13 @@ _ABI = (
       ctypes.c_int, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
       ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
       ctypes.POINTER(KfpOptions), _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_render_points", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_char_p, _c_double_p, _c_double_p, ctypes.POINTER(ctypes.c_int32),
+      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions))),
+    ("fractal_render_points_ex_planes", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_char_p, _c_double_p, _c_double_p, ctypes.POINTER(ctypes.c_int32),
+      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions),
+      ctypes.POINTER(RenderPlanes))),
     ("fractal_crop_field", ctypes.c_int,
      (_c_float_p, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_int)),
@@ -381,6 +388,9 @@ _GB300_ABI = (
       ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
       ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)),
     ("fractal_gb300_atlas_last_exact_pixels", ctypes.c_longlong, ()),
+    ("fractal_gb300_packed_frame_bytes", ctypes.c_longlong, (ctypes.c_int, ctypes.c_int, ctypes.c_int)),
+    ("fractal_gb300_pack_frame_device", ctypes.c_int,
+     (ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)),
     ("fractal_gb300_render_keyframes_device", ctypes.c_int,
      (ctypes.POINTER(Keyframe), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions), ctypes.c_int,
@@ -698,6 +708,31 @@ def atlas_colourise_kfp_raw(library, parent, parent_shape, parent_max_iter, chil
         max_iter, *colour, ctypes.byref(options), lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
     _check(library, status, "fractal_atlas_colourise_kfp_raw")
     return output
+
+
+def render_points(library, handle: int, zoom: bytes, real, imag, exponents, max_iter: int, *, threads: int = 0,
+                  series_order: int = 3, series_block: int = 256, options: Optional[RenderOptions] = None,
+                  planes: bool = False):
+    """``fractal_render_points[_ex_planes]`` (renderer.h:287-320): one value
+    per offset (real * 2^e, imag * 2^e) from the reference centre; returns
+    (field, planes dict or None)."""
+    real = np.ascontiguousarray(real, dtype=np.float64)
+    imag = np.ascontiguousarray(imag, dtype=np.float64)
+    exponents = np.ascontiguousarray(exponents, dtype=np.int32)
+    count = real.size
+    field = np.empty(count, dtype=np.float32)
+    options = options or RenderOptions()
+    args = (field.ctypes.data_as(_c_float_p), count, _text(zoom), real.ctypes.data_as(_c_double_p),
+            imag.ctypes.data_as(_c_double_p), exponents.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), handle,
+            max_iter, threads, series_order, series_block, ctypes.byref(options))
+    if planes:
+        plane_struct, arrays = allocate_planes(count, 1)
+        status = library.fractal_render_points_ex_planes(*args, ctypes.byref(plane_struct))
+        _check(library, status, "fractal_render_points_ex_planes")
+        return field, arrays
+    status = library.fractal_render_points(*args)
+    _check(library, status, "fractal_render_points")
+    return field, None
 
 
 def crop_field(library, source, source_shape, output_shape, zoom, threads=0) -> np.ndarray:

@@ -206,6 +206,24 @@ int render_mandelbrot(float *output, int width, int height, const char *zoom_tex
                       const char *x_center, const char *y_center, int max_iter,
                       int precision_bits, int use_perturbation, int threads);
 
+/* renderer.h:287-300: render an arbitrary list of offsets from the
+ * reference centre, point i at (real[i] + i imag[i]) * 2^exponents[i]; one
+ * float per point.  The largest offset replaces the view radius in the BLA and
+ * series decisions.  Strict Mandelbrot lists of at most 8192 points repair
+ * their glitch points exactly (MPFR iteration from scratch, on the host). */
+int fractal_render_points(float *output, int point_count, const char *zoom_text,
+                          const double *real_mantissa, const double *imag_mantissa,
+                          const int32_t *exponents, void *handle, int max_iter, int threads,
+                          int series_order, int series_block, const FractalRenderOptions *options);
+/* renderer.h:302-320: the same with the six render planes (point_count
+ * entries each). */
+int fractal_render_points_ex_planes(float *output, int point_count, const char *zoom_text,
+                                    const double *real_mantissa, const double *imag_mantissa,
+                                    const int32_t *exponents, void *handle, int max_iter,
+                                    int threads, int series_order, int series_block,
+                                    const FractalRenderOptions *options,
+                                    FractalRenderPlanes *planes);
+
 /* renderer.h:400-411: aurora palette. */
 int fractal_colourise(const float *field, uint8_t *output, int width, int height, int max_iter,
                       double phase, double vocal, double instrumental, double pitch,
@@ -450,6 +468,14 @@ int fractal_gb300_atlas_kfp_surface_device(const float *parent, int parent_width
  * (FP32 / double-float) pass could not decide and the exact FP64 pass
  * computed; synchronises the device.  -1 before any atlas frame. */
 long long fractal_gb300_atlas_last_exact_pixels(void);
+
+/* Video-frame handoff: device RGB8 (width x height x 3) packed into the
+ * layout an encoder pipe takes.  format: 0 rgb24, 1 rgb0 (R,G,B,0), 2 rgba
+ * (R,G,B,255), 3 yuv420p and 4 nv12, both BT.709 limited range with the 2x2
+ * mean as chroma.  packed_frame_bytes gives the output size (-1: invalid). */
+long long fractal_gb300_packed_frame_bytes(int width, int height, int format);
+int fractal_gb300_pack_frame_device(const uint8_t *rgb, int width, int height, int format,
+                                    uint8_t *output, void *stream);
 
 /* One keyframe of a batch: device outputs (`counts` may be NULL), its zoom,
  * the reference handle it renders from (NULL: the direct FP64 path at the

@@ -1208,13 +1208,14 @@ void* clone(void* source, const char* z) {
 }
 
 void deep(const Reference& R, float* out, int W, int H, const char* zs, int max_iter, int threads, int order,
-          int block, const FractalRenderOptions& o, FractalRenderPlanes* planes) {
+          int block, const FractalRenderOptions& o, FractalRenderPlanes* planes,
+          const std::vector<SC>* points = nullptr, const FE* point_radius = nullptr) {
     FE zoom = zoom_of(zs, R.bits);
     FE inv = divide(fe(1.0, 0), zoom);
     double hf = height_factor(o.coordinate_mode);
     FE vh = mul(inv, hf), vw = mul(vh, static_cast<double>(W) / static_cast<double>(H));
     FE spacing = divide(vh, fe(static_cast<double>(H), 0));
-    FE cur = mul(inv, hf);
+    FE cur = point_radius ? *point_radius : mul(inv, hf);
     bool no_bla = cmp(cur, R.radius) > 0 || o.disable_bla != 0;
     bool cyc = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
     bool use_deep = cmp(cur, R.deep_radius) <= 0;
@@ -1233,8 +1234,9 @@ void deep(const Reference& R, float* out, int W, int H, const char* zs, int max_
 #pragma omp parallel for schedule(dynamic, 256)
     for (long long i = 0; i < static_cast<long long>(W) * H; ++i) {
         int py = static_cast<int>(i / W), px = static_cast<int>(i % W);
-        Pixel p{R, o, sink, static_cast<std::size_t>(i), from_fc(xo[static_cast<std::size_t>(px)], yo[static_cast<std::size_t>(py)]),
-                max_iter, spacing, cyc};
+        const SC dc = points ? (*points)[static_cast<std::size_t>(i)]
+                             : from_fc(xo[static_cast<std::size_t>(px)], yo[static_cast<std::size_t>(py)]);
+        Pixel p{R, o, sink, static_cast<std::size_t>(i), dc, max_iter, spacing, cyc};
         p.run(lin, no_bla, series_ok, oc, bla_len, lin_len);
         out[i] = p.out;
     }
@@ -1986,6 +1988,38 @@ int fractal_crop_colourise_accents(const float* S, int sw, int sh, uint8_t* out,
                                    const uint8_t* accents, int r, int g, int b, int) {
     const int interior[3] = {r, g, b};
     return status_of([&] { crop_colour(S, sw, sh, out, W, H, zoom, max_iter, phase, vocal, instrumental, pitch, interior, accents); });
+}
+
+// fractal_render_points (renderer.cpp:20019-20186) for Mandelbrot references:
+// the point list and its largest radius drive the same pixel loop.  The
+// exact MPFR repair of strict glitch points is not restated here.
+int fractal_render_points_ex_planes(float* out, int n, const char* z, const double* re, const double* im,
+                                    const int32_t* ex, void* h, int max_iter, int threads, int order, int block,
+                                    const FractalRenderOptions* opt, FractalRenderPlanes* planes) {
+    return status_of([&] {
+        if (!out || n <= 0 || !z || !re || !im || !ex || !h) throw Oops("invalid native point-render arguments");
+        const FractalRenderOptions o = checked(opt);
+        auto R = lookup(h);
+        if (!R) throw Oops("invalid or already-destroyed reference handle");
+        if (max_iter > R->max_iter) throw Oops("point render iteration count exceeds prepared reference");
+        std::vector<SC> points(static_cast<std::size_t>(n));
+        NM largest{};
+        for (int i = 0; i < n; ++i) {
+            SC p{re[i], im[i], ex[i]};
+            if (!std::isfinite(p.x) || !std::isfinite(p.y)) throw Oops("non-finite point offset");
+            fix(p);
+            points[static_cast<std::size_t>(i)] = p;
+            const NM r = norm(p);
+            if (ncmp(r, largest) > 0) largest = r;
+        }
+        const FE radius = root(FE{largest.m, largest.e});
+        deep(*R, out, n, 1, z, max_iter, threads, order, block, o, planes, &points, &radius);
+    });
+}
+
+int fractal_render_points(float* out, int n, const char* z, const double* re, const double* im, const int32_t* ex,
+                          void* h, int max_iter, int threads, int order, int block, const FractalRenderOptions* opt) {
+    return fractal_render_points_ex_planes(out, n, z, re, im, ex, h, max_iter, threads, order, block, opt, nullptr);
 }
 
 // Test-only export: the raw KFP atlas surface (no reference symbol).
