@@ -30,6 +30,7 @@ native = _load("native")
 atlas = _load("atlas")
 kfp = _load("kfp")
 costnet = _load("costnet")
+frames = _load("frames")
 _builder = _load("build")
 LIBRARY_PATH = _builder.LIBRARY
 

@@ -1,0 +1,115 @@
+// Video-frame handoff: RGB8 frames packed on the device into the layout the
+// encoder pipe takes, so the host copies one finished buffer per frame.
+//
+// The reference writes rgb24 to FFmpeg's stdin, or rgb0 for NVENC's packed
+// RGB input (visualizer.py:3203-3260, 12916-12942).  Formats here:
+//   0 rgb24   the frame as is
+//   1 rgb0    R, G, B, 0 per pixel
+//   2 rgba    R, G, B, 255 per pixel
+//   3 yuv420p BT.709 limited range, planes Y (W x H), U, V (ceil(W/2) x
+//             ceil(H/2)); chroma from the mean of each 2x2 block
+//   4 nv12    the same Y plane, then U/V interleaved
+// The YUV conversion is the integer BT.709 form
+//   Y = 16 + ((47 R + 157 G + 16 B + 128) >> 8)
+//   U = 128 + ((-26 R - 86 G + 112 B + 128) >> 8)
+//   V = 128 + ((112 R - 102 G - 10 B + 128) >> 8)
+// (coefficients: the BT.709 matrix scaled to 8-bit studio swing, x 256,
+// rounded so that each chroma row sums to zero: greys map to 128), chroma
+// taken from the rounded mean of the 2x2 block's R, G, B.
+// One thread per 2x2 block: its four Y samples and one chroma pair; HBM-bound
+// (3 B in, 1.5 B out per pixel for YUV).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device.h"
+
+namespace fgb {
+namespace {
+
+__device__ __forceinline__ int luma(int r, int g, int b) { return 16 + ((47 * r + 157 * g + 16 * b + 128) >> 8); }
+__device__ __forceinline__ int chroma_u(int r, int g, int b) { return 128 + ((-26 * r - 86 * g + 112 * b + 128) >> 8); }
+__device__ __forceinline__ int chroma_v(int r, int g, int b) { return 128 + ((112 * r - 102 * g - 10 * b + 128) >> 8); }
+
+__global__ void pack_rgbx_kernel(const std::uint8_t* __restrict__ rgb, std::uint32_t* __restrict__ out,
+                                 long long pixels, std::uint32_t alpha) {
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const std::uint8_t* p = rgb + 3 * i;
+        out[i] = static_cast<std::uint32_t>(p[0]) | (static_cast<std::uint32_t>(p[1]) << 8)
+            | (static_cast<std::uint32_t>(p[2]) << 16) | (alpha << 24);
+    }
+}
+
+__global__ void pack_yuv_kernel(const std::uint8_t* __restrict__ rgb, std::uint8_t* __restrict__ out, int width,
+                                int height, int interleaved) {
+    const int cw = (width + 1) / 2, ch = (height + 1) / 2;
+    const long long blocks = static_cast<long long>(cw) * ch;
+    std::uint8_t* y_plane = out;
+    std::uint8_t* u_plane = out + static_cast<long long>(width) * height;
+    std::uint8_t* v_plane = u_plane + blocks;
+    for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < blocks;
+         k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int by = static_cast<int>(k / cw), bx = static_cast<int>(k - static_cast<long long>(by) * cw);
+        int sr = 0, sg = 0, sb = 0, n = 0;
+        for (int dy = 0; dy < 2; ++dy) {
+            const int y = 2 * by + dy;
+            if (y >= height) continue;
+            for (int dx = 0; dx < 2; ++dx) {
+                const int x = 2 * bx + dx;
+                if (x >= width) continue;
+                const long long i = static_cast<long long>(y) * width + x;
+                const int r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+                y_plane[i] = static_cast<std::uint8_t>(luma(r, g, b));
+                sr += r;
+                sg += g;
+                sb += b;
+                ++n;
+            }
+        }
+        const int r = (sr + n / 2) / n, g = (sg + n / 2) / n, b = (sb + n / 2) / n;
+        const std::uint8_t u = static_cast<std::uint8_t>(chroma_u(r, g, b));
+        const std::uint8_t v = static_cast<std::uint8_t>(chroma_v(r, g, b));
+        if (interleaved) {
+            u_plane[2 * k] = u;
+            u_plane[2 * k + 1] = v;
+        } else {
+            u_plane[k] = u;
+            v_plane[k] = v;
+        }
+    }
+}
+
+}  // namespace
+
+std::size_t packed_frame_bytes(int width, int height, int format) {
+    const std::size_t pixels = static_cast<std::size_t>(width) * height;
+    const std::size_t chroma = static_cast<std::size_t>((width + 1) / 2) * ((height + 1) / 2);
+    switch (format) {
+        case 0: return pixels * 3;
+        case 1:
+        case 2: return pixels * 4;
+        case 3:
+        case 4: return pixels + 2 * chroma;
+        default: return 0;
+    }
+}
+
+cudaError_t launch_pack_frame(const std::uint8_t* rgb, int width, int height, int format, std::uint8_t* out,
+                              cudaStream_t stream) {
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const long long pixels = static_cast<long long>(width) * height;
+    if (format == 0) return cudaMemcpyAsync(out, rgb, pixels * 3, cudaMemcpyDeviceToDevice, stream);
+    const unsigned blocks = static_cast<unsigned>(sms) * 8;
+    if (format == 1 || format == 2) {
+        pack_rgbx_kernel<<<blocks, 256, 0, stream>>>(rgb, reinterpret_cast<std::uint32_t*>(out), pixels,
+                                                     format == 2 ? 255u : 0u);
+    } else {
+        pack_yuv_kernel<<<blocks, 256, 0, stream>>>(rgb, out, width, height, format == 4 ? 1 : 0);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace fgb
