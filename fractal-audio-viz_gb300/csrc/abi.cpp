@@ -15,6 +15,7 @@
 #include <cstddef>
 #include <cstring>
 #include <functional>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -880,7 +881,8 @@ KfpDeviceInputs kfp_inputs(ThreadRuntime& rt, const FractalKfpOptions& o, const 
 // Resolves the per-pass constants and launches (write_kfp_pixel inputs).
 void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height, int max_iter,
                 const FractalKfpOptions& o, const KfpDeviceInputs& in, int lut_size, ThreadRuntime& rt,
-                cudaStream_t stream) {
+                cudaStream_t stream, const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,
+                const std::uint8_t* flags = nullptr) {
     KfpLaunch k{};
     k.width = width;
     k.height = height;
@@ -915,8 +917,13 @@ void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height
     k.lut_size = lut_size;
     if (o.color_method == 4) {
         unsigned long long* bounds = static_cast<unsigned long long*>(scratch(rt, kScratchWork, 16));
-        check_cuda(launch_kfp_bounds(d_field, static_cast<long long>(width) * height, max_iter, o.field_bias,
-                                     k.smooth_offset, bounds, stream), "KFP bounds launch");
+        if (planes != nullptr && planes->has_iteration) {
+            check_cuda(launch_kfp_plane_bounds(samples, flags, static_cast<long long>(width) * height, max_iter,
+                                               bounds, stream), "KFP plane bounds launch");
+        } else {
+            check_cuda(launch_kfp_bounds(d_field, static_cast<long long>(width) * height, max_iter, o.field_bias,
+                                         k.smooth_offset, bounds, stream), "KFP bounds launch");
+        }
         unsigned long long host[2];
         check_cuda(cudaMemcpyAsync(host, bounds, sizeof host, cudaMemcpyDeviceToHost, stream), "KFP bounds");
         check_cuda(cudaStreamSynchronize(stream), "KFP bounds");
@@ -931,8 +938,39 @@ void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height
             k.transfer_max = unorder(host[1]);
         }
     }
-    check_cuda(launch_kfp(d_field, d_rgb, k, in.lut, in.period, in.type, stream), "KFP kernel launch");
+    check_cuda(launch_kfp(d_field, d_rgb, k, in.lut, in.period, in.type, stream, planes, samples, flags),
+               "KFP kernel launch");
 }
+
+// kfp_selected_bailout_radius / _norm (renderer.cpp:5672-5716).
+double kfp_bailout_radius(const FractalKfpOptions& o) {
+    double radius = 10000.0;
+    switch (o.bailout_radius_preset) {
+        case 0: radius = 10000.0; break;
+        case 1: radius = 2.0; break;
+        case 2:
+            if (o.power > 1.0 && std::isfinite(o.power)) {
+                radius = std::pow(2.0, 1.0 / (o.power - 1.0));
+            } else {
+                return 0.0;
+            }
+            break;
+        case 3: radius = o.bailout_radius_custom; break;
+        default: return 0.0;
+    }
+    return std::isfinite(radius) && radius > 1.0 ? radius : 0.0;
+}
+
+double kfp_bailout_norm(const FractalKfpOptions& o) {
+    switch (o.bailout_norm_preset) {
+        case 0: return 1.0;
+        case 1: return 2.0;
+        case 2: return std::numeric_limits<double>::infinity();
+        case 3: return std::isfinite(o.bailout_norm_custom) && o.bailout_norm_custom > 0.0 ? o.bailout_norm_custom : 0.0;
+        default: return 0.0;
+    }
+}
+
 
 int kfp_host(const float* field, uint8_t* output, int width, int height, int max_iter, double phase, double vocal,
              double instrumental, double pitch, const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
@@ -958,6 +996,135 @@ int kfp_host(const float* field, uint8_t* output, int width, int height, int max
         check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
         check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream), "copy RGB to host");
         check_cuda(cudaStreamSynchronize(rt.stream), "KFP colour");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+// fractal_colourise_kfp_planes (renderer.cpp:16729-16748 through
+// fractal_colourise_kfp_impl, 16314-16545): the planes copied to the device,
+// the pixel context resolved here, one samples pass, then the KFP pass.
+int kfp_planes_host(const float* field, uint8_t* output, int width, int height, int max_iter, double phase,
+                    double vocal, double instrumental, double pitch, const FractalKfpOptions* options,
+                    const FractalKfpPlanes* planes, const uint8_t* lut, int lut_size, int threads) {
+    return guarded("native KFP colouriser failed with an unknown exception", [&] {
+        bool planes_ok = true;
+        if (planes != nullptr) {
+            planes_ok = planes->struct_size >= sizeof(FractalKfpPlanes) && planes->version == FRACTAL_KFP_PLANES_VERSION;
+            if (planes_ok && planes->texture_rgb == nullptr) {
+                planes_ok = planes->texture_width == 0 && planes->texture_height == 0 && planes->texture_stride == 0;
+            } else if (planes_ok) {
+                planes_ok = planes->texture_width > 0 && planes->texture_height > 0
+                    && static_cast<long long>(planes->texture_stride) >= static_cast<long long>(planes->texture_width) * 3;
+            }
+        }
+        if (!field || !output || !valid_dims(width, height) || !valid_iterations(max_iter) || !valid_threads(threads)
+            || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut || !valid_kfp(options, lut_size)
+            || !planes_ok) {
+            throw Failure{"invalid native KFP colour dimensions or controls"};
+        }
+        if (options->field_bias > static_cast<double>(max_iter)) {
+            throw Failure{"native KFP field bias exceeds iteration cap"};
+        }
+        const FractalKfpOptions& o = *options;
+        if (planes == nullptr) {
+            if (kfp_host(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, options, lut,
+                         lut_size, threads) != 0) {
+                throw Failure{last_error};
+            }
+            return;
+        }
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        const std::size_t pixels = static_cast<std::size_t>(width) * static_cast<std::size_t>(height);
+        // Device layout: field, then each present plane, then samples and flags.
+        const void* host_arrays[9] = {planes->orbit_iteration, planes->bailout, planes->iteration, planes->transition,
+                                      planes->phase, planes->de_x, planes->de_y, planes->test1, planes->test2};
+        auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
+        const bool texture = planes->texture_rgb != nullptr && o.texture_enabled != 0;
+        // The texture rows the merge can address: (height - 1) strides plus one row.
+        const std::size_t texture_bytes = texture
+            ? static_cast<std::size_t>(planes->texture_height - 1) * static_cast<std::size_t>(planes->texture_stride)
+                + static_cast<std::size_t>(planes->texture_width) * 3
+            : 0;
+        std::size_t total = up(pixels * sizeof(float)) + up(pixels * 8) + up(pixels) + up(texture_bytes);
+        for (const void* a : host_arrays) total += a ? up(pixels * 8) : 0;
+        char* base = static_cast<char*>(scratch(rt, kScratchPlanesIn, total));
+        std::size_t at = 0;
+        auto put = [&](const void* data, std::size_t bytes) -> void* {
+            void* dst = base + at;
+            if (data) check_cuda(cudaMemcpyAsync(dst, data, bytes, cudaMemcpyHostToDevice, rt.stream), "upload planes");
+            at += up(bytes);
+            return dst;
+        };
+        float* d_field = static_cast<float*>(put(field, pixels * sizeof(float)));
+        const void* d_arrays[9];
+        for (int a = 0; a < 9; ++a) d_arrays[a] = host_arrays[a] ? put(host_arrays[a], pixels * 8) : nullptr;
+        void* samples = put(nullptr, pixels * 8);
+        std::uint8_t* flags = static_cast<std::uint8_t*>(put(nullptr, pixels));
+        const void* d_texture = texture ? put(planes->texture_rgb, texture_bytes) : nullptr;
+        KfpPlanesLaunch pl{};
+        if (texture) {
+            pl.texture = static_cast<const std::uint8_t*>(d_texture);
+            pl.texture_active = 1;
+            pl.texture_width = planes->texture_width;
+            pl.texture_height = planes->texture_height;
+            pl.texture_stride = planes->texture_stride;
+            pl.texture_power = o.texture_power;
+            pl.texture_ratio = o.texture_ratio;
+            pl.texture_merge = o.texture_merge;
+            pl.image_offset = std::isfinite(o.texture_power)
+                ? static_cast<int>(std::clamp(o.texture_power / 64.0,
+                                              static_cast<double>(std::numeric_limits<int>::min()),
+                                              static_cast<double>(std::numeric_limits<int>::max())))
+                : 0;
+        }
+        pl.orbit_iteration = static_cast<const long long*>(d_arrays[0]);
+        pl.bailout = static_cast<const double*>(d_arrays[1]);
+        pl.iteration = static_cast<const long long*>(d_arrays[2]);
+        pl.transition = static_cast<const double*>(d_arrays[3]);
+        pl.phase = static_cast<const double*>(d_arrays[4]);
+        pl.de_x = static_cast<const double*>(d_arrays[5]);
+        pl.de_y = static_cast<const double*>(d_arrays[6]);
+        pl.test1 = static_cast<const double*>(d_arrays[7]);
+        pl.test2 = static_cast<const double*>(d_arrays[8]);
+        pl.has_iteration = planes->orbit_iteration != nullptr || planes->iteration != nullptr;
+        const std::uint32_t glitch_field = static_cast<std::uint32_t>(offsetof(FractalKfpOptions, show_glitches));
+        pl.show_glitches = o.struct_size < glitch_field + sizeof(o.show_glitches) ? 1 : (o.show_glitches != 0);
+        pl.analytic = o.differences == 7 && planes->de_x != nullptr && planes->de_y != nullptr;
+        // kfp_pixel_context (renderer.cpp:5723-5763).
+        pl.smooth_method = o.smooth_method;
+        pl.has_constant_bailout = planes->bailout == nullptr;
+        pl.smooth_bailout_radius = kfp_bailout_radius(o);
+        pl.power = o.power;
+        if (std::isfinite(o.power) && o.power > 1.0) {
+            pl.smooth_power_log = std::log(o.power);
+            pl.has_smooth_power_log = std::isfinite(pl.smooth_power_log) && pl.smooth_power_log != 0.0;
+        }
+        if (pl.has_constant_bailout && pl.smooth_bailout_radius > 1.0 && std::isfinite(pl.smooth_bailout_radius)) {
+            pl.smooth_bailout_log = std::log(pl.smooth_bailout_radius);
+            pl.has_smooth_bailout_log = std::isfinite(pl.smooth_bailout_log) && pl.smooth_bailout_log != 0.0;
+        }
+        const double norm = kfp_bailout_norm(o);
+        if (norm > 0.0 && std::isfinite(norm)) {
+            pl.smooth_norm_exponent = 1.0 / norm;
+            pl.has_smooth_norm_exponent = 1;
+        } else if (std::isinf(norm) && norm > 0.0) {
+            pl.smooth_norm_exponent = 1.0;
+            pl.has_smooth_norm_exponent = 1;
+        }
+        pl.phase_scale = o.phase_color_strength / 100.0 * 1024.0;
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, o, lut, lut_size, false);
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        if (pl.has_iteration) {
+            check_cuda(launch_kfp_plane_samples(pl, max_iter, static_cast<long long>(pixels), samples, flags,
+                                                rt.stream), "KFP plane samples launch");
+        }
+        kfp_colour(d_field, d_rgb, width, height, max_iter, o, in, lut_size, rt, rt.stream, &pl, samples, flags);
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream), "copy RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP plane colour");
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
     });
@@ -1964,6 +2131,14 @@ int fractal_colourise_kfp(const float* field, uint8_t* output, int width, int he
                           const uint8_t* lut, int lut_size, int threads) {
     return kfp_host(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, options, lut, lut_size,
                     threads);
+}
+
+int fractal_colourise_kfp_planes(const float* field, uint8_t* output, int width, int height, int max_iter,
+                                 double phase, double vocal, double instrumental, double pitch,
+                                 const FractalKfpOptions* options, const FractalKfpPlanes* planes, const uint8_t* lut,
+                                 int lut_size, int threads) {
+    return kfp_planes_host(field, output, width, height, max_iter, phase, vocal, instrumental, pitch, options, planes,
+                           lut, lut_size, threads);
 }
 
 int fractal_colourise_kfp_precise(const float* field, uint8_t* output, int width, int height, int max_iter,

@@ -214,9 +214,93 @@ __device__ __forceinline__ float df_value(Df x) { return __fadd_rn(x.hi, x.lo); 
 
 __device__ __forceinline__ bool df_negative(Df x) { return x.hi < 0.0f || (x.hi == 0.0f && x.lo < 0.0f); }
 
+// ---- plane path (fractal_colourise_kfp_planes, renderer.cpp:16314-16728)
+
+// kfp_plane_smooth_part (renderer.cpp:5775-5842): the fractional part of a
+// Kalles orbit sample from |z|^2 at escape (test1), the previous |z|^2
+// (test2) and the bailout, by SmoothMethod 0 (log-log) or 1 (norm roots).
+__device__ double plane_smooth_part(const KfpPlanesLaunch& pl, long long i) {
+    if (pl.test1 == nullptr) return 0.0;
+    const double test1 = pl.test1[i];
+    if (!isfinite(test1) || test1 <= 0.0) return 0.0;
+    double radius = pl.smooth_bailout_radius;
+    if (!pl.has_constant_bailout) {
+        const double b = pl.bailout[i];
+        radius = isfinite(b) && b > 1.0 ? b : pl.smooth_bailout_radius;
+    }
+    double smooth = 0.0;
+    if (pl.smooth_method == 0) {
+        if (radius > 1.0 && isfinite(pl.power) && pl.power > 1.0) {
+            const double numerator = log(sqrt(test1));
+            const double denominator = pl.has_smooth_bailout_log ? pl.smooth_bailout_log : log(radius);
+            const double power_log = pl.has_smooth_power_log ? pl.smooth_power_log : log(pl.power);
+            if (isfinite(numerator) && numerator > 0.0 && isfinite(denominator) && denominator != 0.0
+                && isfinite(power_log) && power_log != 0.0) {
+                smooth = 1.0 - log(numerator / denominator) / power_log;
+            }
+        }
+    } else if (pl.smooth_method == 1 && pl.test2 != nullptr) {
+        const double test2 = pl.test2[i];
+        if (isfinite(test2) && test2 >= 0.0 && pl.has_smooth_norm_exponent) {
+            const double root1 = pow(test1, pl.smooth_norm_exponent);
+            const double root2 = pow(test2, pl.smooth_norm_exponent);
+            const double denominator = root1 - root2;
+            if (isfinite(root1) && isfinite(root2) && isfinite(radius) && denominator != 0.0) {
+                smooth = 1.0 - (root1 - radius) / denominator;
+            }
+        }
+    }
+    return isfinite(smooth) ? smooth : 0.0;
+}
+
+// The colour sample of every pixel from its planes, as a double-float, with
+// flags (bit 0 interior, bit 1 hidden glitch): kfp_plane_orbit_sample
+// (renderer.cpp:5844-5866) from orbit_iteration + the smoothing part, else
+// stored iteration + 1 - transition (kfp_plane_colour_sample, 5868-5911).
+__global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter, long long pixels, float2* samples,
+                                         unsigned char* flags) {
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        double value;
+        bool inside;
+        if (pl.orbit_iteration != nullptr) {
+            const long long raw = pl.orbit_iteration[i] > 0 ? pl.orbit_iteration[i] : 0;
+            if (raw >= max_iter) {
+                value = static_cast<double>(max_iter) + 1.0;
+                inside = true;
+            } else {
+                const double combined = static_cast<double>(raw) + plane_smooth_part(pl, i);
+                inside = combined >= static_cast<double>(max_iter);
+                value = inside ? static_cast<double>(max_iter) + 1.0 : combined;
+            }
+        } else {
+            const long long stored = pl.iteration[i];
+            inside = stored >= max_iter;
+            if (inside) {
+                value = static_cast<double>(max_iter) + 1.0;
+            } else {
+                const double transition = pl.transition != nullptr ? pl.transition[i] : 1.0;
+                value = static_cast<double>(stored > 0 ? stored : 0) + 1.0 - (isfinite(transition) ? transition : 1.0);
+            }
+        }
+        const float hi = static_cast<float>(value);
+        samples[i] = make_float2(hi, static_cast<float>(value - static_cast<double>(hi)));
+        const bool hidden = pl.transition != nullptr && pl.transition[i] < 0.0 && !pl.show_glitches;
+        flags[i] = static_cast<unsigned char>((inside ? 1 : 0) | (hidden ? 2 : 0));
+    }
+}
+
+// ColorMethod 4 bounds over plane samples (kfp_transfer_bounds_planes,
+// renderer.cpp:7335-7393): floor(sample) of escaped pixels below max_iter - 1.
+__global__ void kfp_plane_bounds_kernel(const float2* __restrict__ samples, const unsigned char* __restrict__ flags,
+                                        long long pixels, int max_iter, unsigned long long* bounds);
+
+template <bool Planes>
 __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
                                                   const KfpDevice k, const unsigned char* __restrict__ lut_global,
-                                                  const double* __restrict__ mc_period, const int* __restrict__ mc_type) {
+                                                  const double* __restrict__ mc_period, const int* __restrict__ mc_type,
+                                                  const KfpPlanesLaunch pl, const float2* __restrict__ psamples,
+                                                  const unsigned char* __restrict__ pflags) {
     extern __shared__ unsigned char lut[];
     for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < k.lut_size * 3; i += blockDim.x * blockDim.y) {
         lut[i] = lut_global[i];
@@ -227,50 +311,126 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     if (x >= k.width || y >= k.height) return;
     const long long index = static_cast<long long>(y) * k.width + x;
     unsigned char* out = rgb + 3 * index;
-    const float raw = __ldg(field + index);
-    if (isfinite(raw) && raw >= k.sample_hi) {  // the double test raw >= max_iter - bias, exactly
+    // Plane samples (when the planes carry iterations) are double-float
+    // values; the stencil then works on their differences from the centre,
+    // so `centre` is 0 and each neighbour is its difference.
+    const bool plane_samples = Planes && pl.has_iteration;
+    // With a texture, interior pixels run the whole pass: the interior colour
+    // replaces the palette just before the texture merge (renderer.cpp:
+    // 6790-6796, 7181-7189).
+    const bool texture = Planes && pl.texture_active;
+    bool inside;
+    if (plane_samples) {
+        const unsigned char f = pflags[index];
+        if (f & 2) {  // a hidden glitch pixel: black (renderer.cpp:6733-6743)
+            out[0] = 0;
+            out[1] = 0;
+            out[2] = 0;
+            return;
+        }
+        inside = (f & 1) != 0;
+    } else {
+        if constexpr (Planes) {
+            if (pl.transition != nullptr && pl.transition[index] < 0.0 && !pl.show_glitches) {
+                out[0] = 0;
+                out[1] = 0;
+                out[2] = 0;
+                return;
+            }
+        }
+        const float raw = __ldg(field + index);
+        inside = isfinite(raw) && raw >= k.sample_hi;  // the double test raw >= max_iter - bias, exactly
+    }
+    if (inside && !texture) {
         out[0] = static_cast<unsigned char>(k.interior[0]);
         out[1] = static_cast<unsigned char>(k.interior[1]);
         out[2] = static_cast<unsigned char>(k.interior[2]);
         return;
     }
-    const float centre = sample(field, k, x, y);
-    const Df centre_value = df_add(Df{centre, 0.0f}, Df{k.shift_hi, k.shift_lo});
+    Df centre_value;
+    float centre;
+    if (plane_samples) {
+        const float2 c = psamples[index];
+        centre_value = Df{c.x, c.y};
+        centre = 0.0f;
+    } else {
+        centre = sample(field, k, x, y);
+        centre_value = df_add(Df{centre, 0.0f}, Df{k.shift_hi, k.shift_lo});
+    }
     const Df colour_iter_df = k.flat ? df_floor(centre_value) : centre_value;
     const float colour_iter = df_value(colour_iter_df);
+    auto plane_difference_df = [&](int dx, int dy) -> Df {
+        const int sx = x + dx, sy = y + dy;
+        if (sx >= 0 && sx < k.width && sy >= 0 && sy < k.height) {
+            const float2 v = psamples[static_cast<long long>(sy) * k.width + sx];
+            return df_add(Df{v.x, v.y}, df_neg(centre_value));
+        }
+        const int ox = x - dx, oy = y - dy;
+        if (ox >= 0 && ox < k.width && oy >= 0 && oy < k.height) {
+            const float2 v = psamples[static_cast<long long>(oy) * k.width + ox];
+            return df_add(centre_value, df_neg(Df{v.x, v.y}));
+        }
+        return Df{0.0f, 0.0f};
+    };
+    auto plane_difference = [&](int dx, int dy) -> float { return df_value(plane_difference_df(dx, dy)); };
+    auto neighbour = [&](int dx, int dy) -> float {
+        if constexpr (Planes) {
+            if (plane_samples) return plane_difference(dx, dy);
+        }
+        return reflected(field, k, x, y, dx, dy, centre);
+    };
     float l = centre, r = centre, u = centre, d = centre, tl = centre, tr = centre, bl = centre, br = centre;
-    if (k.needs_difference || k.needs_slopes) {
-        l = reflected(field, k, x, y, -1, 0, centre);
-        u = reflected(field, k, x, y, 0, -1, centre);
+    if (k.needs_difference || k.needs_slopes || texture) {
+        l = neighbour(-1, 0);
+        u = neighbour(0, -1);
         if (k.needs_difference) {
             switch (k.differences) {
                 case 0:
-                    tl = reflected(field, k, x, y, -1, -1, centre);
-                    bl = reflected(field, k, x, y, -1, 1, centre);
+                    tl = neighbour(-1, -1);
+                    bl = neighbour(-1, 1);
                     break;
                 case 1: case 2: case 5: case 6:
-                    r = reflected(field, k, x, y, 1, 0, centre);
-                    d = reflected(field, k, x, y, 0, 1, centre);
-                    tl = reflected(field, k, x, y, -1, -1, centre);
-                    tr = reflected(field, k, x, y, 1, -1, centre);
-                    bl = reflected(field, k, x, y, -1, 1, centre);
-                    br = reflected(field, k, x, y, 1, 1, centre);
+                    r = neighbour(1, 0);
+                    d = neighbour(0, 1);
+                    tl = neighbour(-1, -1);
+                    tr = neighbour(1, -1);
+                    bl = neighbour(-1, 1);
+                    br = neighbour(1, 1);
                     break;
                 case 3: case 4:
-                    tl = reflected(field, k, x, y, -1, -1, centre);
+                    tl = neighbour(-1, -1);
                     break;
                 default:
-                    r = reflected(field, k, x, y, 1, 0, centre);
-                    d = reflected(field, k, x, y, 0, 1, centre);
+                    r = neighbour(1, 0);
+                    d = neighbour(0, 1);
                     break;
             }
         }
-        if (k.needs_slopes) {
-            if (x == 0) r = reflected(field, k, x, y, 1, 0, centre);
-            if (y == 0) d = reflected(field, k, x, y, 0, 1, centre);
+        if (k.needs_slopes || texture) {
+            if (x == 0) r = neighbour(1, 0);
+            if (y == 0) d = neighbour(0, 1);
         }
     }
-    float gradient = k.needs_difference ? difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br) : 0.0f;
+    float gradient = 0.0f;
+    float analytic_x = 0.0f, analytic_y = 0.0f;
+    bool analytic = false;
+    if constexpr (Planes) {
+        // Differences 7 with DE planes: Kalles' float reciprocal norm of the
+        // analytic derivative (renderer.cpp:6942-6962).
+        if ((k.needs_difference || k.needs_slopes) && pl.analytic) {
+            analytic = true;
+            const double ex = pl.de_x[index], ey = pl.de_y[index];
+            const float de_x = static_cast<float>(isfinite(ex) ? ex : 0.0);
+            const float de_y = static_cast<float>(isfinite(ey) ? ey : 0.0);
+            const float denominator = de_x * de_x + de_y * de_y;
+            if (denominator > 0.0f && isfinite(denominator)) {
+                gradient = 1.0f / sqrtf(denominator);
+                analytic_x = de_x / denominator;
+                analytic_y = -de_y / denominator;
+            }
+        }
+    }
+    if (!analytic && k.needs_difference) gradient = difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br);
     float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.width) / 640.0f;
     if (distance < 0.0f) distance = 0.0f;
     Df transfer_df = colour_iter_df;  // kept in double-float for methods 0, 4 and 6's iteration branch
@@ -311,6 +471,16 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
     }
     if (k.has_div) palette_value = df_mul(palette_value, Df{k.inv_div_hi, k.inv_div_lo});
     const Df base = df_add(palette_value, Df{k.offset_hi, k.offset_lo});
+    // The phase colour shift of the ordinary palette (renderer.cpp:7045-7048).
+    Df palette_base = base;
+    if constexpr (Planes) {
+        if (pl.phase != nullptr) {
+            const double ph = pl.phase[index];
+            const double shift = pl.phase_scale * (isfinite(ph) ? ph : 0.0);
+            const float hi = static_cast<float>(shift);
+            palette_base = df_add(base, Df{hi, static_cast<float>(shift - static_cast<double>(hi))});
+        }
+    }
     float red, green, blue;
     auto palette_rgb = [&](Df input, float& o_r, float& o_g, float& o_b) {
         Df position;
@@ -360,7 +530,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         float mr, mg, mb;
         hsv_to_rgb(hc ? hs / hc : 0.0f, sc ? ss / sc : 0.0f, vc ? vs / vc : 0.0f, mr, mg, mb);
         if (k.blend_multi_color) {
-            palette_rgb(base, red, green, blue);
+            palette_rgb(palette_base, red, green, blue);
             red = (red + mr) * 0.5f;
             green = (green + mg) * 0.5f;
             blue = (blue + mb) * 0.5f;
@@ -370,11 +540,58 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
             blue = mb;
         }
     } else {
-        palette_rgb(base, red, green, blue);
+        palette_rgb(palette_base, red, green, blue);
+    }
+    if constexpr (Planes) {
+        if (texture) {
+            if (inside) {
+                red = static_cast<float>(k.interior[0]) / 255.0f;
+                green = static_cast<float>(k.interior[1]) / 255.0f;
+                blue = static_cast<float>(k.interior[2]) / 255.0f;
+            }
+            // SetTexture (renderer.cpp:7191-7248): the texel is displaced by
+            // a warp of the one-sided stencil differences, in FP64 because
+            // the texel index is a floor of it.
+            auto difference = [&](int dx, int dy) -> double {  // in-frame neighbour minus centre
+                if (plane_samples) {
+                    const Df v = plane_difference_df(dx, dy);
+                    return static_cast<double>(v.hi) + static_cast<double>(v.lo);
+                }
+                return static_cast<double>(sample(field, k, x + dx, y + dy)) - static_cast<double>(centre);
+            };
+            const double tdx = x > 0 ? difference(-1, 0) : (x + 1 < k.width ? -difference(1, 0) : 0.0);
+            const double tdy = y > 0 ? difference(0, -1) : (y + 1 < k.height ? -difference(0, 1) : 0.0);
+            auto warp = [&](double delta) -> double {
+                const double powered = pow(1.0 + delta, pl.texture_power);
+                const bool forward = powered > 1.0;
+                const double selected = forward ? powered : 1.0 / powered;
+                const double quarter = 3.14159265358979323846 / 4.0;
+                const double mapped = !isnan(selected)
+                    ? (atan(selected) - quarter) / quarter * (pl.texture_ratio / 100.0) : 0.0;
+                return isfinite(mapped) ? (forward ? pl.texture_power * mapped : -pl.texture_power * mapped) : 0.0;
+            };
+            auto texel = [](double v, int limit) -> int {  // kfp_texture_index (renderer.cpp:5971-5976)
+                if (limit <= 0 || !isfinite(v) || v <= 0.0) return 0;
+                if (v >= static_cast<double>(limit - 1)) return limit - 1;
+                return static_cast<int>(v);
+            };
+            const int sx = texel(static_cast<double>(static_cast<long long>(x) + pl.image_offset) + warp(tdx),
+                                 pl.texture_width);
+            const int sy = texel(static_cast<double>(static_cast<long long>(y) + pl.image_offset) + warp(tdy),
+                                 pl.texture_height);
+            const unsigned char* t = pl.texture + static_cast<long long>(pl.texture_height - 1 - sy) * pl.texture_stride
+                + static_cast<long long>(sx) * 3;
+            const double merge = pl.texture_merge;
+            red = static_cast<float>(static_cast<double>(red) * (1.0 - merge) + merge * static_cast<double>(t[0]) / 255.0);
+            green = static_cast<float>(static_cast<double>(green) * (1.0 - merge)
+                                       + merge * static_cast<double>(t[1]) / 255.0);
+            blue = static_cast<float>(static_cast<double>(blue) * (1.0 - merge)
+                                      + merge * static_cast<double>(t[2]) / 255.0);
+        }
     }
     if (k.needs_slopes) {
-        const float horizontal = x > 0 ? l - centre : centre - r;
-        const float vertical = y == 0 ? centre - d : u - centre;
+        const float horizontal = analytic ? analytic_x : (x > 0 ? l - centre : centre - r);
+        const float vertical = analytic ? analytic_y : (y == 0 ? centre - d : u - centre);
         const float projected = (horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
             * static_cast<float>(k.width) / 640.0f;
         const float strength = atanf(fabsf(projected)) / (kPiF / 2.0f) * k.slope_ratio / 100.0f;
@@ -399,6 +616,25 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
 __device__ __forceinline__ unsigned long long ordered(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void kfp_plane_bounds_kernel(const float2* __restrict__ samples, const unsigned char* __restrict__ flags,
+                                        long long pixels, int max_iter, unsigned long long* bounds) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        if (flags[i] & 1) continue;
+        const float2 s = samples[i];
+        double value = static_cast<double>(s.x) + static_cast<double>(s.y);
+        value = value > static_cast<double>(max_iter) ? static_cast<double>(max_iter) : value;
+        value = floor(value > 0.0 ? value : 0.0);
+        if (value >= static_cast<double>(max_iter - 1)) continue;
+        const unsigned long long o = ordered(value);
+        lo = o < lo ? o : lo;
+        hi = o > hi ? o : hi;
+    }
+    if (lo != ~0ull) atomicMin(bounds, lo);
+    if (hi != 0ull) atomicMax(bounds + 1, hi);
 }
 
 __global__ void kfp_bounds_kernel(const float* __restrict__ field, long long pixels, int max_iter, double field_bias,
@@ -447,8 +683,31 @@ cudaError_t launch_kfp_bounds(const float* field, long long pixels, int max_iter
     return cudaGetLastError();
 }
 
+cudaError_t launch_kfp_plane_samples(const KfpPlanesLaunch& planes, int max_iter, long long pixels, void* samples,
+                                     std::uint8_t* flags, cudaStream_t stream) {
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    long long blocks = (pixels + 255) / 256;
+    if (blocks > static_cast<long long>(sms) * 16) blocks = static_cast<long long>(sms) * 16;
+    kfp_plane_samples_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, stream>>>(
+        planes, max_iter, pixels, static_cast<float2*>(samples), flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kfp_plane_bounds(const void* samples, const std::uint8_t* flags, long long pixels, int max_iter,
+                                    unsigned long long* bounds, cudaStream_t stream) {
+    const unsigned long long init[2] = {~0ull, 0ull};
+    cudaError_t status = cudaMemcpyAsync(bounds, init, sizeof init, cudaMemcpyHostToDevice, stream);
+    if (status != cudaSuccess) return status;
+    kfp_plane_bounds_kernel<<<152 * 4, 256, 0, stream>>>(static_cast<const float2*>(samples), flags, pixels, max_iter,
+                                                         bounds);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
-                       const double* mc_period, const int* mc_type, cudaStream_t stream) {
+                       const double* mc_period, const int* mc_type, cudaStream_t stream,
+                       const KfpPlanesLaunch* planes, const void* samples, const std::uint8_t* flags) {
     KfpDevice k{};
     k.width = launch.width;
     k.height = launch.height;
@@ -502,10 +761,21 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
     const dim3 block(32, 8);
     const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
     const std::size_t shared = static_cast<std::size_t>(launch.lut_size) * 3;
-    if (shared > 48 * 1024) {
-        cudaFuncSetAttribute(kfp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
+    if (planes != nullptr) {
+        if (shared > 48 * 1024) {
+            cudaFuncSetAttribute(kfp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(shared));
+        }
+        kfp_kernel<true><<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type, *planes,
+                                                          static_cast<const float2*>(samples), flags);
+    } else {
+        if (shared > 48 * 1024) {
+            cudaFuncSetAttribute(kfp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(shared));
+        }
+        kfp_kernel<false><<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
+                                                           nullptr, nullptr);
     }
-    kfp_kernel<<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type);
     return cudaGetLastError();
 }
 

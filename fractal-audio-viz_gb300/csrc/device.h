@@ -222,8 +222,46 @@ struct KfpLaunch {
     int lut_size;
 };
 
+// The plane inputs of fractal_colourise_kfp_planes (device copies of the
+// FractalKfpPlanes arrays, null when absent) and the smoothing constants of
+// kfp_pixel_context (renderer.cpp:5723-5763), resolved on the host.
+struct KfpPlanesLaunch {
+    const long long* orbit_iteration;
+    const double* bailout;
+    const long long* iteration;
+    const double* transition;
+    const double* phase;
+    const double* de_x;
+    const double* de_y;
+    const double* test1;
+    const double* test2;
+    int has_iteration;   // orbit_iteration or iteration present
+    int show_glitches;
+    int analytic;        // Differences 7 with both DE planes
+    int smooth_method;
+    int has_constant_bailout;
+    double smooth_bailout_radius, power;
+    int has_smooth_power_log, has_smooth_bailout_log, has_smooth_norm_exponent;
+    double smooth_power_log, smooth_bailout_log, smooth_norm_exponent;
+    double phase_scale;  // phase_color_strength / 100 * 1024
+    // Texture merging (planes->texture_rgb with texture_enabled): top-down
+    // RGB8 rows of `texture_stride` bytes on the device.
+    const std::uint8_t* texture;
+    int texture_active, texture_width, texture_height, texture_stride;
+    int image_offset;    // int(clamp(texture_power / 64)), 0 for a non-finite power
+    double texture_power, texture_ratio, texture_merge;
+};
+// Plane samples (double-float) and flags of every pixel into samples/flags.
+cudaError_t launch_kfp_plane_samples(const KfpPlanesLaunch& planes, int max_iter, long long pixels, void* samples,
+                                     std::uint8_t* flags, cudaStream_t stream);
+cudaError_t launch_kfp_plane_bounds(const void* samples, const std::uint8_t* flags, long long pixels, int max_iter,
+                                    unsigned long long* bounds, cudaStream_t stream);
+// With `planes` non-null the plane path runs (samples/flags from
+// launch_kfp_plane_samples when the planes carry iterations).
 cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
-                       const double* mc_period, const int* mc_type, cudaStream_t stream);
+                       const double* mc_period, const int* mc_type, cudaStream_t stream,
+                       const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,
+                       const std::uint8_t* flags = nullptr);
 cudaError_t launch_kfp_bounds(const float* field, long long pixels, int max_iter, double field_bias,
                               double smooth_offset, unsigned long long* bounds, cudaStream_t stream);
 

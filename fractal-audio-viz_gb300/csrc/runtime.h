@@ -43,6 +43,7 @@ enum ScratchSlot {
     kScratchAtlas,
     kScratchSurface,
     kScratchPoints,
+    kScratchPlanesIn,
     kScratchCount
 };
 

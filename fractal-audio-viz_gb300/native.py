@@ -131,6 +131,28 @@ class RenderPlanes(ctypes.Structure):
     ]
 
 
+class KfpPlanes(ctypes.Structure):
+    """``FractalKfpPlanes`` (renderer.h:135-153)."""
+
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("version", ctypes.c_uint32),
+        ("orbit_iteration", ctypes.POINTER(ctypes.c_int64)),
+        ("bailout", ctypes.POINTER(ctypes.c_double)),
+        ("iteration", ctypes.POINTER(ctypes.c_int64)),
+        ("transition", ctypes.POINTER(ctypes.c_double)),
+        ("phase", ctypes.POINTER(ctypes.c_double)),
+        ("de_x", ctypes.POINTER(ctypes.c_double)),
+        ("de_y", ctypes.POINTER(ctypes.c_double)),
+        ("test1", ctypes.POINTER(ctypes.c_double)),
+        ("test2", ctypes.POINTER(ctypes.c_double)),
+        ("texture_rgb", ctypes.POINTER(ctypes.c_uint8)),
+        ("texture_width", ctypes.c_int32),
+        ("texture_height", ctypes.c_int32),
+        ("texture_stride", ctypes.c_int32),
+    ]
+
+
 class KfpOptions(ctypes.Structure):
     """``FractalKfpOptions`` version 3 (renderer.h:75-119)."""
 
@@ -250,6 +272,10 @@ _ABI = (
      (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
       _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_colourise_kfp_planes", ctypes.c_int,
+     (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
+      ctypes.POINTER(KfpPlanes), _c_u8_p, ctypes.c_int, ctypes.c_int)),
     ("fractal_colourise_kfp_precise", ctypes.c_int,
      (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
@@ -733,6 +759,40 @@ def render_points(library, handle: int, zoom: bytes, real, imag, exponents, max_
     status = library.fractal_render_points(*args)
     _check(library, status, "fractal_render_points")
     return field, None
+
+
+def colourise_kfp_planes(library, field, width: int, height: int, max_iter: int, options, planes: dict, lut,
+                         colour=(0.0, 0.0, 0.0, 0.5), threads: int = 0) -> np.ndarray:
+    """``fractal_colourise_kfp_planes`` (renderer.h:483-497); `planes` maps
+    FractalKfpPlanes field names to arrays (absent names pass NULL), and
+    ``texture`` to (top-down RGB8 rows, width, height, stride)."""
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    struct = KfpPlanes()
+    struct.struct_size = ctypes.sizeof(KfpPlanes)
+    struct.version = 1
+    keep = []
+    for name in ("orbit_iteration", "iteration"):
+        if planes.get(name) is not None:
+            array = np.ascontiguousarray(planes[name], dtype=np.int64)
+            keep.append(array)
+            setattr(struct, name, array.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    for name in ("bailout", "transition", "phase", "de_x", "de_y", "test1", "test2"):
+        if planes.get(name) is not None:
+            array = np.ascontiguousarray(planes[name], dtype=np.float64)
+            keep.append(array)
+            setattr(struct, name, array.ctypes.data_as(_c_double_p))
+    if planes.get("texture") is not None:
+        rows, struct.texture_width, struct.texture_height, struct.texture_stride = planes["texture"]
+        rows = np.ascontiguousarray(rows, dtype=np.uint8)
+        keep.append(rows)
+        struct.texture_rgb = rows.ctypes.data_as(_c_u8_p)
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_colourise_kfp_planes(
+        field.ctypes.data_as(_c_float_p), output.ctypes.data_as(_c_u8_p), width, height, max_iter, *colour,
+        ctypes.byref(options), ctypes.byref(struct), lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
+    _check(library, status, "fractal_colourise_kfp_planes")
+    return output
 
 
 def crop_field(library, source, source_shape, output_shape, zoom, threads=0) -> np.ndarray:

@@ -111,6 +111,26 @@ typedef struct FractalKfpOptions {
     int32_t show_glitches;
 } FractalKfpOptions;
 
+/* renderer.h:135-153: per-pixel Kalles metadata read by the KFP plane
+ * path (row-major, width*height entries; any array may be NULL). */
+typedef struct FractalKfpPlanes {
+    uint32_t struct_size;
+    uint32_t version;
+    const int64_t *orbit_iteration;
+    const double *bailout;
+    const int64_t *iteration;
+    const double *transition;
+    const double *phase;
+    const double *de_x;
+    const double *de_y;
+    const double *test1;
+    const double *test2;
+    const uint8_t *texture_rgb;
+    int32_t texture_width;
+    int32_t texture_height;
+    int32_t texture_stride;
+} FractalKfpPlanes;
+
 /* renderer.h:155-170 */
 typedef struct FractalRenderPlanes {
     uint32_t struct_size;
@@ -235,6 +255,16 @@ int fractal_colourise_kfp(const float *field, uint8_t *output, int width, int he
                           double phase, double vocal, double instrumental, double pitch,
                           const FractalKfpOptions *options, const uint8_t *lut, int lut_size,
                           int threads);
+/* renderer.h:483-497: the KFP transfer fed by Kalles metadata planes:
+ * orbit iteration + test1/test2/bailout smoothing (or stored iteration and
+ * transition), the phase colour, analytic DE for Differences 7, hidden
+ * glitch pixels.  Texture merging is not supported: a texture with
+ * texture_enabled fails with a message. */
+int fractal_colourise_kfp_planes(const float *field, uint8_t *output, int width, int height,
+                                 int max_iter, double phase, double vocal, double instrumental,
+                                 double pitch, const FractalKfpOptions *options,
+                                 const FractalKfpPlanes *planes, const uint8_t *lut, int lut_size,
+                                 int threads);
 /* renderer.h:503-516: compatibility name of the same transfer. */
 int fractal_colourise_kfp_precise(const float *field, uint8_t *output, int width, int height,
                                   int max_iter, double phase, double vocal, double instrumental,
