@@ -878,11 +878,8 @@ KfpDeviceInputs kfp_inputs(ThreadRuntime& rt, const FractalKfpOptions& o, const 
     return in;
 }
 
-// Resolves the per-pass constants and launches (write_kfp_pixel inputs).
-void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height, int max_iter,
-                const FractalKfpOptions& o, const KfpDeviceInputs& in, int lut_size, ThreadRuntime& rt,
-                cudaStream_t stream, const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,
-                const std::uint8_t* flags = nullptr) {
+// The per-pass constants of write_kfp_pixel for a width x height field.
+KfpLaunch kfp_constants(const FractalKfpOptions& o, int width, int height, int max_iter, int lut_size) {
     KfpLaunch k{};
     k.width = width;
     k.height = height;
@@ -915,28 +912,50 @@ void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height
     k.slope_ratio = o.slope_ratio;
     for (int c = 0; c < 3; ++c) k.interior[c] = o.interior_color[c];
     k.lut_size = lut_size;
+    return k;
+}
+
+// ColorMethod 4's transfer bounds (kfp_transfer_bounds, renderer.cpp:
+// 7296-7393) of a scalar field or of plane samples, read back to the host;
+// (0, 1) when no pixel qualifies.
+void kfp_transfer_bounds(ThreadRuntime& rt, const float* d_field, long long pixels, int max_iter,
+                         const FractalKfpOptions& o, double smooth_offset, cudaStream_t stream, double& minimum,
+                         double& maximum, const void* samples = nullptr, const std::uint8_t* flags = nullptr) {
+    unsigned long long* bounds = static_cast<unsigned long long*>(scratch(rt, kScratchWork, 16));
+    if (samples != nullptr) {
+        check_cuda(launch_kfp_plane_bounds(samples, flags, pixels, max_iter, bounds, stream), "KFP plane bounds launch");
+    } else {
+        check_cuda(launch_kfp_bounds(d_field, pixels, max_iter, o.field_bias, smooth_offset, bounds, stream),
+                   "KFP bounds launch");
+    }
+    unsigned long long host[2];
+    check_cuda(cudaMemcpyAsync(host, bounds, sizeof host, cudaMemcpyDeviceToHost, stream), "KFP bounds");
+    check_cuda(cudaStreamSynchronize(stream), "KFP bounds");
+    auto unorder = [](unsigned long long v) {
+        const unsigned long long bits = (v & 0x8000000000000000ull) ? (v & 0x7fffffffffffffffull) : ~v;
+        double d;
+        std::memcpy(&d, &bits, sizeof d);
+        return d;
+    };
+    minimum = 0.0;
+    maximum = 1.0;
+    if (host[0] != ~0ull && host[1] != 0ull) {
+        minimum = unorder(host[0]);
+        maximum = unorder(host[1]);
+    }
+}
+
+// Resolves the per-pass constants and launches (write_kfp_pixel inputs).
+void kfp_colour(const float* d_field, std::uint8_t* d_rgb, int width, int height, int max_iter,
+                const FractalKfpOptions& o, const KfpDeviceInputs& in, int lut_size, ThreadRuntime& rt,
+                cudaStream_t stream, const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,
+                const std::uint8_t* flags = nullptr) {
+    KfpLaunch k = kfp_constants(o, width, height, max_iter, lut_size);
     if (o.color_method == 4) {
-        unsigned long long* bounds = static_cast<unsigned long long*>(scratch(rt, kScratchWork, 16));
-        if (planes != nullptr && planes->has_iteration) {
-            check_cuda(launch_kfp_plane_bounds(samples, flags, static_cast<long long>(width) * height, max_iter,
-                                               bounds, stream), "KFP plane bounds launch");
-        } else {
-            check_cuda(launch_kfp_bounds(d_field, static_cast<long long>(width) * height, max_iter, o.field_bias,
-                                         k.smooth_offset, bounds, stream), "KFP bounds launch");
-        }
-        unsigned long long host[2];
-        check_cuda(cudaMemcpyAsync(host, bounds, sizeof host, cudaMemcpyDeviceToHost, stream), "KFP bounds");
-        check_cuda(cudaStreamSynchronize(stream), "KFP bounds");
-        auto unorder = [](unsigned long long v) {
-            const unsigned long long bits = (v & 0x8000000000000000ull) ? (v & 0x7fffffffffffffffull) : ~v;
-            double d;
-            std::memcpy(&d, &bits, sizeof d);
-            return d;
-        };
-        if (host[0] != ~0ull && host[1] != 0ull) {
-            k.transfer_min = unorder(host[0]);
-            k.transfer_max = unorder(host[1]);
-        }
+        const bool plane_samples = planes != nullptr && planes->has_iteration;
+        kfp_transfer_bounds(rt, d_field, static_cast<long long>(width) * height, max_iter, o, k.smooth_offset, stream,
+                            k.transfer_min, k.transfer_max, plane_samples ? samples : nullptr,
+                            plane_samples ? flags : nullptr);
     }
     check_cuda(launch_kfp(d_field, d_rgb, k, in.lut, in.period, in.type, stream, planes, samples, flags),
                "KFP kernel launch");
@@ -1001,6 +1020,75 @@ int kfp_host(const float* field, uint8_t* output, int width, int height, int max
     });
 }
 
+// kfp_pixel_context (renderer.cpp:5723-5763) for planes whose device
+// pointers are already in `pl`.
+void plane_context(KfpPlanesLaunch& pl, const FractalKfpOptions& o) {
+    pl.has_iteration = pl.orbit_iteration != nullptr || pl.iteration != nullptr;
+    const std::uint32_t glitch_field = static_cast<std::uint32_t>(offsetof(FractalKfpOptions, show_glitches));
+    pl.show_glitches = o.struct_size < glitch_field + sizeof(o.show_glitches) ? 1 : (o.show_glitches != 0);
+    pl.analytic = o.differences == 7 && pl.de_x != nullptr && pl.de_y != nullptr;
+    pl.smooth_method = o.smooth_method;
+    pl.has_constant_bailout = pl.bailout == nullptr;
+    pl.smooth_bailout_radius = kfp_bailout_radius(o);
+    pl.power = o.power;
+    if (std::isfinite(o.power) && o.power > 1.0) {
+        pl.smooth_power_log = std::log(o.power);
+        pl.has_smooth_power_log = std::isfinite(pl.smooth_power_log) && pl.smooth_power_log != 0.0;
+    }
+    if (pl.has_constant_bailout && pl.smooth_bailout_radius > 1.0 && std::isfinite(pl.smooth_bailout_radius)) {
+        pl.smooth_bailout_log = std::log(pl.smooth_bailout_radius);
+        pl.has_smooth_bailout_log = std::isfinite(pl.smooth_bailout_log) && pl.smooth_bailout_log != 0.0;
+    }
+    const double norm = kfp_bailout_norm(o);
+    if (norm > 0.0 && std::isfinite(norm)) {
+        pl.smooth_norm_exponent = 1.0 / norm;
+        pl.has_smooth_norm_exponent = 1;
+    } else if (std::isinf(norm) && norm > 0.0) {
+        pl.smooth_norm_exponent = 1.0;
+        pl.has_smooth_norm_exponent = 1;
+    }
+    pl.phase_scale = o.phase_color_strength / 100.0 * 1024.0;
+}
+
+// Bytes of a texture the merge can address: (height - 1) strides plus one row.
+std::size_t texture_bytes(const FractalKfpPlanes& planes) {
+    return static_cast<std::size_t>(planes.texture_height - 1) * static_cast<std::size_t>(planes.texture_stride)
+        + static_cast<std::size_t>(planes.texture_width) * 3;
+}
+
+// SetTexture's constants (renderer.cpp:7191-7226) for a texture on the device.
+void attach_texture(KfpPlanesLaunch& pl, const FractalKfpPlanes& planes, const FractalKfpOptions& o,
+                    const void* d_texture) {
+    pl.texture = static_cast<const std::uint8_t*>(d_texture);
+    pl.texture_active = 1;
+    pl.texture_width = planes.texture_width;
+    pl.texture_height = planes.texture_height;
+    pl.texture_stride = planes.texture_stride;
+    pl.texture_power = o.texture_power;
+    pl.texture_ratio = o.texture_ratio;
+    pl.texture_merge = o.texture_merge;
+    pl.image_offset = std::isfinite(o.texture_power)
+        ? static_cast<int>(std::clamp(o.texture_power / 64.0, static_cast<double>(std::numeric_limits<int>::min()),
+                                      static_cast<double>(std::numeric_limits<int>::max())))
+        : 0;
+}
+
+// valid_kfp_planes (renderer.cpp:7467-7491).
+bool valid_kfp_planes(const FractalKfpPlanes* planes, int width, int height) {
+    if (planes == nullptr) return true;
+    if (planes->struct_size < sizeof(FractalKfpPlanes) || planes->version != FRACTAL_KFP_PLANES_VERSION) return false;
+    if (planes->texture_rgb == nullptr) {
+        return planes->texture_width == 0 && planes->texture_height == 0 && planes->texture_stride == 0;
+    }
+    if (planes->texture_width <= 0 || planes->texture_height <= 0
+        || static_cast<long long>(planes->texture_stride) < static_cast<long long>(planes->texture_width) * 3) {
+        return false;
+    }
+    const unsigned long long bytes = static_cast<unsigned long long>(planes->texture_stride)
+        * static_cast<unsigned long long>(planes->texture_height);
+    return bytes <= static_cast<unsigned long long>(kMaxPixels) * 3ull && valid_dims(width, height);
+}
+
 // fractal_colourise_kfp_planes (renderer.cpp:16729-16748 through
 // fractal_colourise_kfp_impl, 16314-16545): the planes copied to the device,
 // the pixel context resolved here, one samples pass, then the KFP pass.
@@ -1008,16 +1096,7 @@ int kfp_planes_host(const float* field, uint8_t* output, int width, int height, 
                     double vocal, double instrumental, double pitch, const FractalKfpOptions* options,
                     const FractalKfpPlanes* planes, const uint8_t* lut, int lut_size, int threads) {
     return guarded("native KFP colouriser failed with an unknown exception", [&] {
-        bool planes_ok = true;
-        if (planes != nullptr) {
-            planes_ok = planes->struct_size >= sizeof(FractalKfpPlanes) && planes->version == FRACTAL_KFP_PLANES_VERSION;
-            if (planes_ok && planes->texture_rgb == nullptr) {
-                planes_ok = planes->texture_width == 0 && planes->texture_height == 0 && planes->texture_stride == 0;
-            } else if (planes_ok) {
-                planes_ok = planes->texture_width > 0 && planes->texture_height > 0
-                    && static_cast<long long>(planes->texture_stride) >= static_cast<long long>(planes->texture_width) * 3;
-            }
-        }
+        const bool planes_ok = valid_kfp_planes(planes, width, height);
         if (!field || !output || !valid_dims(width, height) || !valid_iterations(max_iter) || !valid_threads(threads)
             || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut || !valid_kfp(options, lut_size)
             || !planes_ok) {
@@ -1042,12 +1121,8 @@ int kfp_planes_host(const float* field, uint8_t* output, int width, int height, 
                                       planes->phase, planes->de_x, planes->de_y, planes->test1, planes->test2};
         auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
         const bool texture = planes->texture_rgb != nullptr && o.texture_enabled != 0;
-        // The texture rows the merge can address: (height - 1) strides plus one row.
-        const std::size_t texture_bytes = texture
-            ? static_cast<std::size_t>(planes->texture_height - 1) * static_cast<std::size_t>(planes->texture_stride)
-                + static_cast<std::size_t>(planes->texture_width) * 3
-            : 0;
-        std::size_t total = up(pixels * sizeof(float)) + up(pixels * 8) + up(pixels) + up(texture_bytes);
+        const std::size_t texture_size = texture ? texture_bytes(*planes) : 0;
+        std::size_t total = up(pixels * sizeof(float)) + up(pixels * 8) + up(pixels) + up(texture_size);
         for (const void* a : host_arrays) total += a ? up(pixels * 8) : 0;
         char* base = static_cast<char*>(scratch(rt, kScratchPlanesIn, total));
         std::size_t at = 0;
@@ -1062,23 +1137,9 @@ int kfp_planes_host(const float* field, uint8_t* output, int width, int height, 
         for (int a = 0; a < 9; ++a) d_arrays[a] = host_arrays[a] ? put(host_arrays[a], pixels * 8) : nullptr;
         void* samples = put(nullptr, pixels * 8);
         std::uint8_t* flags = static_cast<std::uint8_t*>(put(nullptr, pixels));
-        const void* d_texture = texture ? put(planes->texture_rgb, texture_bytes) : nullptr;
+        const void* d_texture = texture ? put(planes->texture_rgb, texture_size) : nullptr;
         KfpPlanesLaunch pl{};
-        if (texture) {
-            pl.texture = static_cast<const std::uint8_t*>(d_texture);
-            pl.texture_active = 1;
-            pl.texture_width = planes->texture_width;
-            pl.texture_height = planes->texture_height;
-            pl.texture_stride = planes->texture_stride;
-            pl.texture_power = o.texture_power;
-            pl.texture_ratio = o.texture_ratio;
-            pl.texture_merge = o.texture_merge;
-            pl.image_offset = std::isfinite(o.texture_power)
-                ? static_cast<int>(std::clamp(o.texture_power / 64.0,
-                                              static_cast<double>(std::numeric_limits<int>::min()),
-                                              static_cast<double>(std::numeric_limits<int>::max())))
-                : 0;
-        }
+        if (texture) attach_texture(pl, *planes, o, d_texture);
         pl.orbit_iteration = static_cast<const long long*>(d_arrays[0]);
         pl.bailout = static_cast<const double*>(d_arrays[1]);
         pl.iteration = static_cast<const long long*>(d_arrays[2]);
@@ -1088,32 +1149,7 @@ int kfp_planes_host(const float* field, uint8_t* output, int width, int height, 
         pl.de_y = static_cast<const double*>(d_arrays[6]);
         pl.test1 = static_cast<const double*>(d_arrays[7]);
         pl.test2 = static_cast<const double*>(d_arrays[8]);
-        pl.has_iteration = planes->orbit_iteration != nullptr || planes->iteration != nullptr;
-        const std::uint32_t glitch_field = static_cast<std::uint32_t>(offsetof(FractalKfpOptions, show_glitches));
-        pl.show_glitches = o.struct_size < glitch_field + sizeof(o.show_glitches) ? 1 : (o.show_glitches != 0);
-        pl.analytic = o.differences == 7 && planes->de_x != nullptr && planes->de_y != nullptr;
-        // kfp_pixel_context (renderer.cpp:5723-5763).
-        pl.smooth_method = o.smooth_method;
-        pl.has_constant_bailout = planes->bailout == nullptr;
-        pl.smooth_bailout_radius = kfp_bailout_radius(o);
-        pl.power = o.power;
-        if (std::isfinite(o.power) && o.power > 1.0) {
-            pl.smooth_power_log = std::log(o.power);
-            pl.has_smooth_power_log = std::isfinite(pl.smooth_power_log) && pl.smooth_power_log != 0.0;
-        }
-        if (pl.has_constant_bailout && pl.smooth_bailout_radius > 1.0 && std::isfinite(pl.smooth_bailout_radius)) {
-            pl.smooth_bailout_log = std::log(pl.smooth_bailout_radius);
-            pl.has_smooth_bailout_log = std::isfinite(pl.smooth_bailout_log) && pl.smooth_bailout_log != 0.0;
-        }
-        const double norm = kfp_bailout_norm(o);
-        if (norm > 0.0 && std::isfinite(norm)) {
-            pl.smooth_norm_exponent = 1.0 / norm;
-            pl.has_smooth_norm_exponent = 1;
-        } else if (std::isinf(norm) && norm > 0.0) {
-            pl.smooth_norm_exponent = 1.0;
-            pl.has_smooth_norm_exponent = 1;
-        }
-        pl.phase_scale = o.phase_color_strength / 100.0 * 1024.0;
+        plane_context(pl, o);
         std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
         const KfpDeviceInputs in = kfp_inputs(rt, o, lut, lut_size, false);
         check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
@@ -2767,6 +2803,260 @@ int fractal_atlas_colourise_kfp_raw(const float* parent, int parent_width, int p
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
     });
+}
+
+// fractal_atlas_colourise_kfp (renderer.h:554-576, renderer.cpp:
+// 16750-17321): parent and child coloured as separate KFP tiles at output
+// scale, each with its own stencil edges and ColorMethod 4 bounds, the child
+// over its rectangle with a smoothstep band of `feather` pixels.
+int fractal_atlas_colourise_kfp(const float* parent, int parent_width, int parent_height, const float* child,
+                                int child_width, int child_height, uint8_t* output, int output_width,
+                                int output_height, int max_iter, int child_left, int child_top, int feather,
+                                double phase, double vocal, double instrumental, double pitch,
+                                const FractalKfpOptions* options, const uint8_t* lut, int lut_size, int threads) {
+    return guarded("native KFP atlas colouriser failed with an unknown exception", [&] {
+        if (!parent || !output || !valid_dims(parent_width, parent_height) || !valid_dims(output_width, output_height)
+            || parent_width != output_width || parent_height != output_height || !valid_iterations(max_iter)
+            || !valid_threads(threads) || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut
+            || !valid_kfp(options, lut_size)) {
+            throw Failure{"invalid native KFP atlas dimensions or controls"};
+        }
+        const bool use_child = child != nullptr;
+        if (use_child) {
+            if (!valid_dims(child_width, child_height) || child_left < 0 || child_top < 0
+                || child_width > output_width - child_left || child_height > output_height - child_top || feather < 0
+                || feather > std::min(child_width, child_height)) {
+                throw Failure{"invalid native KFP atlas child rectangle"};
+            }
+        } else if (child_width != 0 || child_height != 0 || child_left != 0 || child_top != 0 || feather != 0) {
+            throw Failure{"invalid native KFP atlas child absence"};
+        }
+        const FractalKfpOptions& o = *options;
+        if (o.field_bias > static_cast<double>(max_iter)) throw Failure{"native KFP field bias exceeds iteration cap"};
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
+        const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
+        const std::size_t child_pixels = use_child ? static_cast<std::size_t>(child_width) * child_height : 0;
+        char* base = static_cast<char*>(scratch(rt, kScratchAtlas, up(pixels * 4) + up(child_pixels * 4)));
+        check_cuda(cudaMemcpyAsync(base, parent, pixels * 4, cudaMemcpyHostToDevice, rt.stream), "atlas parent");
+        float* d_child = reinterpret_cast<float*>(base + up(pixels * 4));
+        if (use_child) {
+            check_cuda(cudaMemcpyAsync(d_child, child, child_pixels * 4, cudaMemcpyHostToDevice, rt.stream),
+                       "atlas child");
+        }
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, o, lut, lut_size, false);
+        KfpLaunch k = kfp_constants(o, output_width, output_height, max_iter, lut_size);
+        KfpAtlasLaunch at{};
+        at.parent = reinterpret_cast<const float*>(base);
+        at.child = use_child ? d_child : nullptr;
+        at.child_width = child_width;
+        at.child_height = child_height;
+        at.child_left = child_left;
+        at.child_top = child_top;
+        at.feather = feather;
+        at.child_transfer_min = 0.0;
+        at.child_transfer_max = 1.0;
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        if (o.color_method == 4) {
+            kfp_transfer_bounds(rt, at.parent, static_cast<long long>(pixels), max_iter, o, k.smooth_offset, rt.stream,
+                                k.transfer_min, k.transfer_max);
+            if (use_child) {
+                kfp_transfer_bounds(rt, d_child, static_cast<long long>(child_pixels), max_iter, o, k.smooth_offset,
+                                    rt.stream, at.child_transfer_min, at.child_transfer_max);
+            }
+        }
+        check_cuda(launch_kfp_atlas(at, d_rgb, k, in.lut, in.period, in.type, rt.stream), "KFP atlas launch");
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
+                   "copy atlas RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "KFP atlas");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+// fractal_atlas_colourise_kfp_precise (renderer.h:577-603): the same pass
+// under its compatibility name.
+int fractal_atlas_colourise_kfp_precise(const float* parent, int parent_width, int parent_height, const float* child,
+                                        int child_width, int child_height, uint8_t* output, int output_width,
+                                        int output_height, int max_iter, int child_left, int child_top, int feather,
+                                        double phase, double vocal, double instrumental, double pitch,
+                                        const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                        int threads) {
+    return fractal_atlas_colourise_kfp(parent, parent_width, parent_height, child, child_width, child_height, output,
+                                       output_width, output_height, max_iter, child_left, child_top, feather, phase,
+                                       vocal, instrumental, pitch, options, lut, lut_size, threads);
+}
+
+// fractal_atlas_colourise_kfp_planes (renderer.h:604-631, renderer.cpp:
+// 17323-17783): the scalar surface and every present render plane of the
+// primary tile (the child when it fills the frame) reprojected to the
+// output, the child blended in over its rectangle, then the plane-aware KFP
+// pass over the composed frame.
+int fractal_atlas_colourise_kfp_planes(const float* parent, int parent_width, int parent_height, int parent_max_iter,
+                                       const FractalKfpPlanes* parent_planes, const float* child, int child_width,
+                                       int child_height, int child_max_iter, const FractalKfpPlanes* child_planes,
+                                       uint8_t* output, int output_width, int output_height, double parent_zoom,
+                                       double child_fraction, double child_zoom, int max_iter, int centered_input,
+                                       double phase, double vocal, double instrumental, double pitch,
+                                       const FractalKfpOptions* options, const uint8_t* lut, int lut_size,
+                                       int threads) {
+    return guarded("native plane-aware KFP atlas colourizer failed with an unknown exception", [&] {
+        if (!parent || !output || !parent_planes || !valid_dims(parent_width, parent_height)
+            || !valid_dims(output_width, output_height) || !valid_iterations(parent_max_iter)
+            || !valid_iterations(max_iter) || !valid_threads(threads) || centered_input < 0 || centered_input > 1
+            || !std::isfinite(parent_zoom) || parent_zoom <= 0.0 || !std::isfinite(child_fraction)
+            || child_fraction < 0.0 || child_fraction > 1.0 || !std::isfinite(child_zoom) || child_zoom <= 0.0
+            || !valid_colour_controls(phase, vocal, instrumental, pitch) || !lut || !valid_kfp(options, lut_size)
+            || !valid_kfp_planes(parent_planes, parent_width, parent_height)) {
+            throw Failure{"invalid native plane-aware KFP atlas dimensions or controls"};
+        }
+        const bool use_child = child != nullptr && child_fraction > 0.0;
+        if (use_child) {
+            if (!valid_dims(child_width, child_height) || !valid_iterations(child_max_iter) || !child_planes
+                || !valid_kfp_planes(child_planes, child_width, child_height)) {
+                throw Failure{"invalid native plane-aware KFP atlas child tile"};
+            }
+        } else if (child != nullptr || child_planes != nullptr || child_width != 0 || child_height != 0
+                   || child_max_iter != 0) {
+            throw Failure{"invalid native plane-aware KFP atlas child absence"};
+        }
+        const FractalKfpOptions& o = *options;
+        if (o.field_bias > static_cast<double>(max_iter)) throw Failure{"native KFP field bias exceeds iteration cap"};
+        const AtlasRequest r{parent_width, parent_height, parent_max_iter, child_width, child_height, child_max_iter,
+                             child != nullptr, output_width, output_height, parent_zoom, child_fraction, 0};
+        AtlasLaunch a = atlas_geometry(r);
+        a.mode = kAtlasKfpPlanes;
+        a.parent_zoom = std::max(parent_zoom, 1.0);
+        a.child_zoom = std::max(child_zoom, 1.0);
+        a.parent_bias = centered_input ? static_cast<double>(parent_max_iter) : 0.0;
+        a.child_bias = centered_input ? static_cast<double>(child_max_iter) : 0.0;
+        a.output_bias = o.field_bias;
+        const int target_max_iter = a.full_child ? child_max_iter : max_iter;
+        a.effective_iter = target_max_iter;
+        const bool secondary = a.use_child && !a.full_child;
+        a.feather = secondary ? kfp_seam_feather(a.child_visible_width, a.child_visible_height) : 0;
+        const FractalKfpPlanes* primary_planes = a.full_child ? child_planes : parent_planes;
+        const FractalKfpPlanes* secondary_planes = secondary ? child_planes : nullptr;
+        // Texture coordinates are screen space: one source's image is kept.
+        const FractalKfpPlanes* texture_planes = primary_planes;
+        if (texture_planes->texture_rgb == nullptr && secondary_planes != nullptr
+            && secondary_planes->texture_rgb != nullptr) {
+            texture_planes = secondary_planes;
+        }
+        const bool texture = texture_planes->texture_rgb != nullptr && o.texture_enabled != 0;
+
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        void* tables = stage_atlas_sources(rt, a, parent, child);
+        auto up = [](std::size_t v) { return (v + 255) / 256 * 256; };
+        const std::size_t pixels = static_cast<std::size_t>(output_width) * output_height;
+        auto members = [](const FractalKfpPlanes* p, const void* out[9]) {
+            const void* v[9] = {p ? p->orbit_iteration : nullptr, p ? p->iteration : nullptr, p ? p->bailout : nullptr,
+                                p ? p->transition : nullptr, p ? p->phase : nullptr, p ? p->de_x : nullptr,
+                                p ? p->de_y : nullptr, p ? p->test1 : nullptr, p ? p->test2 : nullptr};
+            for (int i = 0; i < 9; ++i) out[i] = v[i];
+        };
+        const void* primary_host[9];
+        const void* secondary_host[9];
+        members(primary_planes, primary_host);
+        members(secondary_planes, secondary_host);
+        const std::size_t primary_pixels = a.full_child ? static_cast<std::size_t>(child_width) * child_height
+                                                        : static_cast<std::size_t>(parent_width) * parent_height;
+        const std::size_t secondary_pixels = secondary ? static_cast<std::size_t>(child_width) * child_height : 0;
+        const std::size_t texture_size = texture ? texture_bytes(*texture_planes) : 0;
+        std::size_t in_total = up(texture_size);
+        std::size_t out_total = up(pixels * 8) + up(pixels) + up(pixels);
+        for (int i = 0; i < 9; ++i) {
+            in_total += (primary_host[i] ? up(primary_pixels * 8) : 0) + (secondary_host[i] ? up(secondary_pixels * 8) : 0);
+            out_total += primary_host[i] || secondary_host[i] ? up(pixels * 8) : 0;
+        }
+        char* in_base = static_cast<char*>(scratch(rt, kScratchPlanesIn, in_total));
+        char* out_base = static_cast<char*>(scratch(rt, kScratchPlanesOut, out_total));
+        std::size_t in_at = 0, out_at = 0;
+        auto put = [&](const void* data, std::size_t bytes) -> void* {
+            void* dst = in_base + in_at;
+            check_cuda(cudaMemcpyAsync(dst, data, bytes, cudaMemcpyHostToDevice, rt.stream), "upload planes");
+            in_at += up(bytes);
+            return dst;
+        };
+        auto take = [&](std::size_t bytes) -> void* {
+            void* dst = out_base + out_at;
+            out_at += up(bytes);
+            return dst;
+        };
+        KfpPlaneSet primary{}, second{};
+        KfpPlaneOutputs composed{};
+        for (int i = 0; i < 9; ++i) {
+            const void* pd = primary_host[i] ? put(primary_host[i], primary_pixels * 8) : nullptr;
+            const void* sd = secondary_host[i] ? put(secondary_host[i], secondary_pixels * 8) : nullptr;
+            void* od = primary_host[i] || secondary_host[i] ? take(pixels * 8) : nullptr;
+            if (i < 2) {
+                primary.ints[i] = static_cast<const long long*>(pd);
+                second.ints[i] = static_cast<const long long*>(sd);
+                composed.ints[i] = static_cast<long long*>(od);
+            } else {
+                primary.doubles[i - 2] = static_cast<const double*>(pd);
+                second.doubles[i - 2] = static_cast<const double*>(sd);
+                composed.doubles[i - 2] = static_cast<double*>(od);
+            }
+        }
+        const void* d_texture = texture ? put(texture_planes->texture_rgb, texture_size) : nullptr;
+        void* samples = take(pixels * 8);
+        std::uint8_t* flags = static_cast<std::uint8_t*>(take(pixels));
+        a.inside_out = static_cast<std::uint8_t*>(take(pixels));
+        a.field_out = static_cast<float*>(scratch(rt, kScratchSurface, pixels * sizeof(float)));
+        KfpPlanesLaunch pl{};
+        pl.orbit_iteration = composed.ints[0];
+        pl.iteration = composed.ints[1];
+        pl.bailout = composed.doubles[0];
+        pl.transition = composed.doubles[1];
+        pl.phase = composed.doubles[2];
+        pl.de_x = composed.doubles[3];
+        pl.de_y = composed.doubles[4];
+        pl.test1 = composed.doubles[5];
+        pl.test2 = composed.doubles[6];
+        plane_context(pl, o);
+        if (texture) attach_texture(pl, *texture_planes, o, d_texture);
+        std::uint8_t* d_rgb = static_cast<std::uint8_t*>(scratch(rt, kScratchRgb, pixels * 3));
+        const KfpDeviceInputs in = kfp_inputs(rt, o, lut, lut_size, false);
+        check_cuda(cudaEventRecord(rt.start, rt.stream), "cudaEventRecord");
+        check_cuda(run_atlas(rt, a, tables, rt.stream), "atlas surface launch");
+        check_cuda(launch_atlas_planes(a, primary, second, composed, target_max_iter, rt.stream),
+                   "atlas planes launch");
+        if (pl.has_iteration) {
+            check_cuda(launch_kfp_plane_samples(pl, target_max_iter, static_cast<long long>(pixels), samples, flags,
+                                                rt.stream), "KFP plane samples launch");
+        }
+        kfp_colour(a.field_out, d_rgb, output_width, output_height, target_max_iter, o, in, lut_size, rt, rt.stream,
+                   &pl, samples, flags);
+        check_cuda(cudaEventRecord(rt.stop, rt.stream), "cudaEventRecord");
+        check_cuda(cudaMemcpyAsync(output, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, rt.stream),
+                   "copy atlas RGB to host");
+        check_cuda(cudaStreamSynchronize(rt.stream), "plane-aware KFP atlas");
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, rt.start, rt.stop) == cudaSuccess) rt.last_kernel_ms = ms;
+    });
+}
+
+// fractal_atlas_colourise_kfp_planes_precise (renderer.h:632-662): the same
+// pass under its compatibility name.
+int fractal_atlas_colourise_kfp_planes_precise(const float* parent, int parent_width, int parent_height,
+                                               int parent_max_iter, const FractalKfpPlanes* parent_planes,
+                                               const float* child, int child_width, int child_height,
+                                               int child_max_iter, const FractalKfpPlanes* child_planes,
+                                               uint8_t* output, int output_width, int output_height,
+                                               double parent_zoom, double child_fraction, double child_zoom,
+                                               int max_iter, int centered_input, double phase, double vocal,
+                                               double instrumental, double pitch, const FractalKfpOptions* options,
+                                               const uint8_t* lut, int lut_size, int threads) {
+    return fractal_atlas_colourise_kfp_planes(parent, parent_width, parent_height, parent_max_iter, parent_planes,
+                                              child, child_width, child_height, child_max_iter, child_planes, output,
+                                              output_width, output_height, parent_zoom, child_fraction, child_zoom,
+                                              max_iter, centered_input, phase, vocal, instrumental, pitch, options,
+                                              lut, lut_size, threads);
 }
 
 // fractal_atlas_colourise_kfp_raw_precise (renderer.h:688-711): the same

@@ -56,6 +56,7 @@ struct KfpDevice {
     int sample_fast;     // field_bias >= 0 and smooth_offset >= 0
     double inv_iter_div; // 1 / iter_div
     int lut_shift;       // log2(lut_size) when a power of two, else -1
+    int spatial_width;   // the output width the gradient and slopes scale by
 };
 
 // A stencil sample is kept as its raw field value sv with the sample equal to
@@ -295,22 +296,16 @@ __global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter,
 __global__ void kfp_plane_bounds_kernel(const float2* __restrict__ samples, const unsigned char* __restrict__ flags,
                                         long long pixels, int max_iter, unsigned long long* bounds);
 
+// write_kfp_pixel (renderer.cpp:6696-7289) for source pixel (x, y) of a
+// k.width x k.height field, dithered at output position (dither_x,
+// dither_y); `lut` is the palette staged in shared memory.
 template <bool Planes>
-__global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
-                                                  const KfpDevice k, const unsigned char* __restrict__ lut_global,
-                                                  const double* __restrict__ mc_period, const int* __restrict__ mc_type,
-                                                  const KfpPlanesLaunch pl, const float2* __restrict__ psamples,
-                                                  const unsigned char* __restrict__ pflags) {
-    extern __shared__ unsigned char lut[];
-    for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < k.lut_size * 3; i += blockDim.x * blockDim.y) {
-        lut[i] = lut_global[i];
-    }
-    __syncthreads();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= k.width || y >= k.height) return;
+__device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const KfpDevice& k,
+                                          const unsigned char* lut, const double* __restrict__ mc_period,
+                                          const int* __restrict__ mc_type, const KfpPlanesLaunch& pl,
+                                          const float2* __restrict__ psamples, const unsigned char* __restrict__ pflags,
+                                          int x, int y, int dither_x, int dither_y, unsigned char* out) {
     const long long index = static_cast<long long>(y) * k.width + x;
-    unsigned char* out = rgb + 3 * index;
     // Plane samples (when the planes carry iterations) are double-float
     // values; the stencil then works on their differences from the centre,
     // so `centre` is 0 and each neighbour is its difference.
@@ -431,7 +426,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         }
     }
     if (!analytic && k.needs_difference) gradient = difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br);
-    float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.width) / 640.0f;
+    float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.spatial_width) / 640.0f;
     if (distance < 0.0f) distance = 0.0f;
     Df transfer_df = colour_iter_df;  // kept in double-float for methods 0, 4 and 6's iteration branch
     bool exact_transfer = k.color_method == 0 || k.color_method == 4;
@@ -593,7 +588,7 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
         const float horizontal = analytic ? analytic_x : (x > 0 ? l - centre : centre - r);
         const float vertical = analytic ? analytic_y : (y == 0 ? centre - d : u - centre);
         const float projected = (horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
-            * static_cast<float>(k.width) / 640.0f;
+            * static_cast<float>(k.spatial_width) / 640.0f;
         const float strength = atanf(fabsf(projected)) / (kPiF / 2.0f) * k.slope_ratio / 100.0f;
         if (projected >= 0.0f) {
             red *= 1.0f - strength;
@@ -605,9 +600,96 @@ __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ fiel
             blue = blue * (1.0f - strength) + strength;
         }
     }
-    out[0] = dither_byte(red, x, y, 0);
-    out[1] = dither_byte(green, x, y, 1);
-    out[2] = dither_byte(blue, x, y, 2);
+    out[0] = dither_byte(red, dither_x, dither_y, 0);
+    out[1] = dither_byte(green, dither_x, dither_y, 1);
+    out[2] = dither_byte(blue, dither_x, dither_y, 2);
+}
+
+__device__ __forceinline__ void stage_lut(unsigned char* lut, const unsigned char* __restrict__ lut_global, int size) {
+    for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < size * 3; i += blockDim.x * blockDim.y) {
+        lut[i] = lut_global[i];
+    }
+    __syncthreads();
+}
+
+template <bool Planes>
+__global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
+                                                  const KfpDevice k, const unsigned char* __restrict__ lut_global,
+                                                  const double* __restrict__ mc_period, const int* __restrict__ mc_type,
+                                                  const KfpPlanesLaunch pl, const float2* __restrict__ psamples,
+                                                  const unsigned char* __restrict__ pflags) {
+    extern __shared__ unsigned char lut[];
+    stage_lut(lut, lut_global, k.lut_size);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= k.width || y >= k.height) return;
+    kfp_pixel<Planes>(field, k, lut, mc_period, mc_type, pl, psamples, pflags, x, y, x, y,
+                      rgb + 3 * (static_cast<long long>(y) * k.width + x));
+}
+
+// The child tile's smoothstep ramp at distance `i` into a `size`-wide axis
+// (renderer.cpp:16895-16910); no contraction, as in the reference.
+__device__ __forceinline__ float tile_ramp(int i, int size, int feather) {
+    const int edge = i < size - 1 - i ? i : size - 1 - i;
+    float linear = __fdiv_rn(static_cast<float>(edge), static_cast<float>(feather));
+    linear = linear < 1.0f ? linear : 1.0f;
+    return __fmul_rn(__fmul_rn(linear, linear), __fsub_rn(3.0f, __fmul_rn(2.0f, linear)));
+}
+
+// fractal_atlas_colourise_kfp's generic per-pixel body (renderer.cpp:
+// 17097-17265): outside the child rectangle the parent tile; inside, an
+// interior child pixel of the owned region, the child or parent by
+// interior test without a feather band, else both tiles blended in FP64
+// and rounded half-even (rounded_colour_byte).
+__global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at, unsigned char* __restrict__ rgb,
+                                                        const KfpDevice kp, const KfpDevice kc,
+                                                        const unsigned char* __restrict__ lut_global,
+                                                        const double* __restrict__ mc_period,
+                                                        const int* __restrict__ mc_type) {
+    extern __shared__ unsigned char lut[];
+    stage_lut(lut, lut_global, kp.lut_size);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= kp.width || y >= kp.height) return;
+    unsigned char* dst = rgb + 3 * (static_cast<long long>(y) * kp.width + x);
+    const KfpPlanesLaunch none{};
+    const int cx = x - at.child_left, cy = y - at.child_top;
+    const bool in_child = at.child != nullptr && cx >= 0 && cx < at.child_width && cy >= 0 && cy < at.child_height;
+    if (!in_child) {
+        kfp_pixel<false>(at.parent, kp, lut, mc_period, mc_type, none, nullptr, nullptr, x, y, x, y, dst);
+        return;
+    }
+    const float child_raw = __ldg(at.child + static_cast<long long>(cy) * at.child_width + cx);
+    const bool child_inside = isfinite(child_raw) && child_raw >= kc.sample_hi;
+    float alpha = 1.0f;
+    if (at.feather >= 2) {
+        const float ax = tile_ramp(cx, at.child_width, at.feather), ay = tile_ramp(cy, at.child_height, at.feather);
+        alpha = ay < ax ? ay : ax;
+    }
+    if (child_inside && alpha >= 0.999999f) {
+        kfp_pixel<false>(at.child, kc, lut, mc_period, mc_type, none, nullptr, nullptr, cx, cy, x, y, dst);
+        return;
+    }
+    if (at.feather < 2) {
+        const float parent_raw = __ldg(at.parent + static_cast<long long>(y) * kp.width + x);
+        if (!(isfinite(parent_raw) && parent_raw >= kp.sample_hi)) {
+            kfp_pixel<false>(at.parent, kp, lut, mc_period, mc_type, none, nullptr, nullptr, x, y, x, y, dst);
+        } else {
+            kfp_pixel<false>(at.child, kc, lut, mc_period, mc_type, none, nullptr, nullptr, cx, cy, x, y, dst);
+        }
+        return;
+    }
+    unsigned char p[3], c[3];
+    kfp_pixel<false>(at.parent, kp, lut, mc_period, mc_type, none, nullptr, nullptr, x, y, x, y, p);
+    kfp_pixel<false>(at.child, kc, lut, mc_period, mc_type, none, nullptr, nullptr, cx, cy, x, y, c);
+    const double a = static_cast<double>(alpha);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        double v = __dadd_rn(__dmul_rn(static_cast<double>(p[ch]), __dsub_rn(1.0, a)),
+                             __dmul_rn(static_cast<double>(c[ch]), a));
+        v = v < 0.0 ? 0.0 : (v > 255.0 ? 255.0 : v);
+        dst[ch] = static_cast<unsigned char>(__double2int_rn(v));
+    }
 }
 
 // ColorMethod 4 bounds: min/max of floor(sample) over escaped pixels below
@@ -705,9 +787,11 @@ cudaError_t launch_kfp_plane_bounds(const void* samples, const std::uint8_t* fla
     return cudaGetLastError();
 }
 
-cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
-                       const double* mc_period, const int* mc_type, cudaStream_t stream,
-                       const KfpPlanesLaunch* planes, const void* samples, const std::uint8_t* flags) {
+namespace {
+
+// The kernel constants of one KFP pass (doubles split into double-float
+// pairs, exact FP32 thresholds) for a `launch.width`-wide source.
+KfpDevice kfp_device(const KfpLaunch& launch, int spatial_width) {
     KfpDevice k{};
     k.width = launch.width;
     k.height = launch.height;
@@ -758,6 +842,16 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
     for (int shift = 0; shift < 31; ++shift) {
         if ((1 << shift) == launch.lut_size) k.lut_shift = shift;
     }
+    k.spatial_width = spatial_width;
+    return k;
+}
+
+}  // namespace
+
+cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
+                       const double* mc_period, const int* mc_type, cudaStream_t stream,
+                       const KfpPlanesLaunch* planes, const void* samples, const std::uint8_t* flags) {
+    const KfpDevice k = kfp_device(launch, launch.width);
     const dim3 block(32, 8);
     const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
     const std::size_t shared = static_cast<std::size_t>(launch.lut_size) * 3;
@@ -776,6 +870,26 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
         kfp_kernel<false><<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
                                                            nullptr, nullptr);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, const KfpLaunch& parent_launch,
+                             const std::uint8_t* lut, const double* mc_period, const int* mc_type,
+                             cudaStream_t stream) {
+    const KfpDevice kp = kfp_device(parent_launch, parent_launch.width);
+    KfpLaunch child_launch = parent_launch;
+    child_launch.width = atlas.child ? atlas.child_width : 1;
+    child_launch.height = atlas.child ? atlas.child_height : 1;
+    child_launch.transfer_min = atlas.child_transfer_min;
+    child_launch.transfer_max = atlas.child_transfer_max;
+    const KfpDevice kc = kfp_device(child_launch, parent_launch.width);
+    const dim3 block(32, 8);
+    const dim3 grid((parent_launch.width + 31) / 32, (parent_launch.height + 7) / 8);
+    const std::size_t shared = static_cast<std::size_t>(parent_launch.lut_size) * 3;
+    if (shared > 48 * 1024) {
+        cudaFuncSetAttribute(kfp_atlas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
+    }
+    kfp_atlas_kernel<<<grid, block, shared, stream>>>(atlas, rgb, kp, kc, lut, mc_period, mc_type);
     return cudaGetLastError();
 }
 

@@ -454,6 +454,36 @@ __device__ __forceinline__ float surface_pixel(bool& undecided, const AtlasLaunc
     return parent_value * (1.0f - alpha) + child_value * alpha;
 }
 
+// Scalar surface of one pixel of fractal_atlas_colourise_kfp_planes
+// (renderer.cpp:17520-17553, 17686-17706): the primary tile (the child when
+// it fills the frame) everywhere, the child blended in over its rectangle
+// with no shortcut at alpha 1; interior flags for the plane pass.
+template <bool Exact>
+__device__ __forceinline__ float planes_surface_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent,
+                                                      const SourceView& child, int x, int y) {
+    std::uint8_t flags;
+    float value;
+    if (a.full_child) {
+        const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, x, y, undecided);
+        flags = c.inside ? 1 : 0;
+        value = c.inside ? a.interior_value : encode_sample(a, c.value);
+    } else {
+        const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
+        flags = p.inside ? 1 : 0;
+        value = p.inside ? a.interior_value : encode_sample(a, p.value);
+        const int cx = x - a.child_left, cy = y - a.child_top;
+        if (in_child(a, cx, cy)) {
+            const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
+            flags |= c.inside ? 2 : 0;
+            const float child_value = c.inside ? a.interior_value : encode_sample(a, c.value);
+            const float alpha = seam_alpha(a, cx, cy);
+            value = value * (1.0f - alpha) + child_value * alpha;
+        }
+    }
+    a.inside_out[static_cast<long long>(y) * a.out_width + x] = flags;
+    return value;
+}
+
 // RGB8 of one pixel (atlas_colourise_impl's per-pixel body).
 template <bool Exact>
 __device__ __forceinline__ void colour_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
@@ -569,6 +599,7 @@ __device__ __forceinline__ void atlas_pixel(const AtlasLaunch& a, const SourceVi
                                             int x, int y, bool& undecided, float* value, std::uint8_t* rgb) {
     switch (a.mode) {
         case kAtlasKfpSurface: *value = surface_pixel<Exact>(undecided, a, parent, child, x, y); break;
+        case kAtlasKfpPlanes: *value = planes_surface_pixel<Exact>(undecided, a, parent, child, x, y); break;
         case kAtlasCropField: *value = crop_pixel(a, x, y); break;
         case kAtlasField: *value = field_pixel<Exact>(undecided, a, parent, child, x, y); break;
         case kAtlasRgb: rgb_pixel(a, x, y, rgb); break;
@@ -660,7 +691,114 @@ __global__ void __launch_bounds__(256) atlas_exact_kernel(const AtlasLaunch a) {
     }
 }
 
+// One source's bilinear / nearest plane samples at local (x, y) through its
+// axes (sample_bilinear_mapped_double, sample_nearest_mapped_*:
+// renderer.cpp:5076-5138).  Compiled without FMA contraction: the double
+// arithmetic is the reference's operation for operation.
+struct PlaneAxes {
+    AtlasAxis x, y;
+    int width;
+};
+
+__device__ __forceinline__ long long nearest_index(const PlaneAxes& s, int x, int y) {
+    const int xi = __ldg(s.x.weight + x) < 0.5f ? __ldg(s.x.index0 + x) : __ldg(s.x.index1 + x);
+    const int yi = __ldg(s.y.weight + y) < 0.5f ? __ldg(s.y.index0 + y) : __ldg(s.y.index1 + y);
+    return static_cast<long long>(yi) * s.width + xi;
+}
+
+__device__ __forceinline__ double bilinear_double(const double* __restrict__ src, const PlaneAxes& s, int x, int y,
+                                                  bool preserve_negative) {
+    const int x0 = __ldg(s.x.index0 + x), x1 = __ldg(s.x.index1 + x);
+    const double wx = static_cast<double>(__ldg(s.x.weight + x));
+    const int y0 = __ldg(s.y.index0 + y), y1 = __ldg(s.y.index1 + y);
+    const double wy = static_cast<double>(__ldg(s.y.weight + y));
+    const double* top = src + static_cast<long long>(y0) * s.width;
+    const double* bottom = src + static_cast<long long>(y1) * s.width;
+    auto ordinary = [preserve_negative](double v) { return preserve_negative && v < 0.0 ? 0.0 : v; };
+    const double t = ordinary(__ldg(top + x0)) * (1.0 - wx) + ordinary(__ldg(top + x1)) * wx;
+    const double b = ordinary(__ldg(bottom + x0)) * (1.0 - wx) + ordinary(__ldg(bottom + x1)) * wx;
+    double value = t * (1.0 - wy) + b * wy;
+    if (preserve_negative) {
+        const double nearest = __ldg(src + nearest_index(s, x, y));
+        if (nearest < 0.0) value = nearest;
+    }
+    return value;
+}
+
+// Double planes: 0 bailout, 1 transition (keeps negative markers), 2 phase,
+// 3 de_x, 4 de_y, 5 test1, 6 test2; all but the bailout reset to 0 on
+// interior samples.
+__global__ void __launch_bounds__(256) atlas_planes_kernel(const AtlasLaunch a, const KfpPlaneSet primary,
+                                                           const KfpPlaneSet secondary, const KfpPlaneOutputs out,
+                                                           long long target_max_iter) {
+    const PlaneAxes ps = a.full_child ? PlaneAxes{a.child_x, a.child_y, a.child_width}
+                                      : PlaneAxes{a.parent_x, a.parent_y, a.parent_width};
+    const PlaneAxes cs{a.child_x, a.child_y, a.child_width};
+    const bool secondary_tile = a.use_child && !a.full_child;
+    const long long pixels = static_cast<long long>(a.out_width) * a.out_height;
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int y = static_cast<int>(i / a.out_width);
+        const int x = static_cast<int>(i - static_cast<long long>(y) * a.out_width);
+        const std::uint8_t flags = a.inside_out[i];
+        const bool inside = flags & 1;
+        const int cx = x - a.child_left, cy = y - a.child_top;
+        const bool child_here = secondary_tile && in_child(a, cx, cy);
+        const bool child_inside = flags & 2;
+        const float alpha = child_here ? seam_alpha(a, cx, cy) : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (out.ints[k] == nullptr) continue;
+            long long v = 0;
+            if (primary.ints[k] != nullptr) v = inside ? target_max_iter : __ldg(primary.ints[k] + nearest_index(ps, x, y));
+            if (child_here && secondary.ints[k] != nullptr) {
+                v = child_inside ? target_max_iter : __ldg(secondary.ints[k] + nearest_index(cs, cx, cy));
+            }
+            out.ints[k][i] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            if (out.doubles[k] == nullptr) continue;
+            const bool preserve = k == 1, reset = k != 0;
+            double v = 0.0;
+            if (primary.doubles[k] != nullptr) {
+                v = bilinear_double(primary.doubles[k], ps, x, y, preserve);
+                if (inside && reset) v = 0.0;
+            }
+            if (child_here && secondary.doubles[k] != nullptr) {
+                double c = bilinear_double(secondary.doubles[k], cs, cx, cy, preserve);
+                if (child_inside && reset) c = 0.0;
+                if (primary.doubles[k] == nullptr) {
+                    v = c;
+                } else {
+                    const double blended = v * (1.0 - static_cast<double>(alpha)) + c * static_cast<double>(alpha);
+                    if (preserve) {
+                        const double selected = alpha >= 0.5f ? c : v;
+                        v = selected < 0.0 ? selected : blended;
+                    } else {
+                        v = blended;
+                    }
+                }
+            }
+            out.doubles[k][i] = v;
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_atlas_planes(const AtlasLaunch& a, const KfpPlaneSet& primary, const KfpPlaneSet& secondary,
+                                const KfpPlaneOutputs& out, long long target_max_iter, cudaStream_t stream) {
+    int device = 0, sms = 152;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const long long pixels = static_cast<long long>(a.out_width) * a.out_height;
+    long long blocks = (pixels + 255) / 256;
+    if (blocks > static_cast<long long>(sms) * 8) blocks = static_cast<long long>(sms) * 8;
+    atlas_planes_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, stream>>>(a, primary, secondary,
+                                                                                            out, target_max_iter);
+    return cudaGetLastError();
+}
 
 // Entries of each per-frame table: the bilinear axes the mode reads, the
 // float edge ramps (interior-preserving modes) or the double alpha table
@@ -743,7 +881,7 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
     split(a.child_bias, a.child_bias_hi, a.child_bias_lo);
     a.output_bias_f = static_cast<float>(a.output_bias);
     a.output_bias_exact = static_cast<double>(a.output_bias_f) == a.output_bias;
-    a.interior_value = a.mode == kAtlasKfpSurface
+    a.interior_value = a.mode == kAtlasKfpSurface || a.mode == kAtlasKfpPlanes
         ? encode_host(static_cast<double>(a.effective_iter), a.output_bias)
         : static_cast<float>(static_cast<double>(a.effective_iter) - a.output_bias);
     auto align = [](std::size_t v) { return (v + 255) / 256 * 256; };

@@ -258,6 +258,19 @@ cudaError_t launch_kfp_plane_bounds(const void* samples, const std::uint8_t* fla
                                     unsigned long long* bounds, cudaStream_t stream);
 // With `planes` non-null the plane path runs (samples/flags from
 // launch_kfp_plane_samples when the planes carry iterations).
+// fractal_atlas_colourise_kfp (renderer.cpp:16750-17321): parent and child
+// coloured as separate tiles at output scale (each with its own stencil
+// edges and ColorMethod 4 bounds), the child over the rectangle at
+// (child_left, child_top), blended across a smoothstep band of `feather`.
+struct KfpAtlasLaunch {
+    const float* parent;
+    const float* child;  // null: parent only
+    int child_width, child_height, child_left, child_top, feather;
+    double child_transfer_min, child_transfer_max;
+};
+cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, const KfpLaunch& parent_launch,
+                             const std::uint8_t* lut, const double* mc_period, const int* mc_type,
+                             cudaStream_t stream);
 cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
                        const double* mc_period, const int* mc_type, cudaStream_t stream,
                        const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,
@@ -466,6 +479,7 @@ enum AtlasMode {
     kAtlasCropField = 3,    // fractal_crop_field: plain bilinear scalar crop
     kAtlasRgb = 4,          // fractal_crop_rgb / fractal_atlas_composite_rgb: RGB8 sources
     kAtlasCropAurora = 5,   // crop_colourise_impl: aurora crop of one field
+    kAtlasKfpPlanes = 6,    // fractal_atlas_colourise_kfp_planes surface (+ interior flags)
 };
 struct AtlasLaunch {
     int mode;  // AtlasMode: field_out (field, KFP surface) or rgb (aurora)
@@ -506,7 +520,27 @@ struct AtlasLaunch {
     float index_scale;
     int palette_iter;
     int interior[3];
+    // kAtlasKfpPlanes: per output pixel, bit 0 = the primary sample is
+    // interior, bit 1 = the child sample is (inside the child rectangle).
+    std::uint8_t* inside_out;
 };
+// The KFP render planes of one atlas source, or of the composed frame
+// (device; any may be null): orbit_iteration, iteration; bailout,
+// transition, phase, de_x, de_y, test1, test2.
+struct KfpPlaneSet {
+    const long long* ints[2];
+    const double* doubles[7];
+};
+struct KfpPlaneOutputs {
+    long long* ints[2];
+    double* doubles[7];
+};
+// fractal_atlas_colourise_kfp_planes' plane reprojection (renderer.cpp:
+// 17553-17765) over the tables and interior flags of a kAtlasKfpPlanes
+// launch: nearest-sample integer planes, bilinear double planes (transition
+// keeps negative glitch markers), interior resets, the child blend.
+cudaError_t launch_atlas_planes(const AtlasLaunch& launch, const KfpPlaneSet& primary, const KfpPlaneSet& secondary,
+                                const KfpPlaneOutputs& out, long long target_max_iter, cudaStream_t stream);
 // Device bytes of the per-frame tables of `launch` (axes and ramps).
 std::size_t atlas_table_bytes(const AtlasLaunch& launch);
 // Builds the tables in `tables` (atlas_table_bytes, 256-byte aligned), then

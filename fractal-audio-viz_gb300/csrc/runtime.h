@@ -44,6 +44,7 @@ enum ScratchSlot {
     kScratchSurface,
     kScratchPoints,
     kScratchPlanesIn,
+    kScratchPlanesOut,
     kScratchCount
 };
 

@@ -272,6 +272,15 @@ _ABI = (
      (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
       _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_atlas_colourise_kfp", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_int, ctypes.c_int, _c_u8_p, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions), _c_u8_p, ctypes.c_int, ctypes.c_int)),
+    ("fractal_atlas_colourise_kfp_planes", ctypes.c_int,
+     (_c_float_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(KfpPlanes), _c_float_p, ctypes.c_int,
+      ctypes.c_int, ctypes.c_int, ctypes.POINTER(KfpPlanes), _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+      ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions), _c_u8_p, ctypes.c_int, ctypes.c_int)),
     ("fractal_colourise_kfp_planes", ctypes.c_int,
      (_c_float_p, _c_u8_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(KfpOptions),
@@ -761,13 +770,10 @@ def render_points(library, handle: int, zoom: bytes, real, imag, exponents, max_
     return field, None
 
 
-def colourise_kfp_planes(library, field, width: int, height: int, max_iter: int, options, planes: dict, lut,
-                         colour=(0.0, 0.0, 0.0, 0.5), threads: int = 0) -> np.ndarray:
-    """``fractal_colourise_kfp_planes`` (renderer.h:483-497); `planes` maps
-    FractalKfpPlanes field names to arrays (absent names pass NULL), and
-    ``texture`` to (top-down RGB8 rows, width, height, stride)."""
-    field = np.ascontiguousarray(field, dtype=np.float32)
-    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+def kfp_planes_struct(planes: dict):
+    """A FractalKfpPlanes over the arrays of `planes` (field names; absent
+    names pass NULL; ``texture`` = (top-down RGB8 rows, width, height,
+    stride)); returns (struct, arrays to keep alive)."""
     struct = KfpPlanes()
     struct.struct_size = ctypes.sizeof(KfpPlanes)
     struct.version = 1
@@ -787,6 +793,67 @@ def colourise_kfp_planes(library, field, width: int, height: int, max_iter: int,
         rows = np.ascontiguousarray(rows, dtype=np.uint8)
         keep.append(rows)
         struct.texture_rgb = rows.ctypes.data_as(_c_u8_p)
+    return struct, keep
+
+
+def atlas_colourise_kfp(library, parent, output_shape, child, child_shape, child_origin, feather, max_iter, options,
+                        lut, colour=(0.0, 0.0, 0.0, 0.5), threads: int = 0) -> np.ndarray:
+    """``fractal_atlas_colourise_kfp`` (renderer.h:554-576): separate KFP
+    tiles, the output-sized parent and a child rectangle at `child_origin`."""
+    width, height = output_shape
+    parent = np.ascontiguousarray(parent, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    cw, ch = child_shape if child is not None else (0, 0)
+    left, top = child_origin if child is not None else (0, 0)
+    child_ptr = None
+    if child is not None:
+        child = np.ascontiguousarray(child, dtype=np.float32)
+        child_ptr = child.ctypes.data_as(_c_float_p)
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_atlas_colourise_kfp(
+        parent.ctypes.data_as(_c_float_p), width, height, child_ptr, cw, ch, output.ctypes.data_as(_c_u8_p), width,
+        height, max_iter, left, top, feather if child is not None else 0, *colour, ctypes.byref(options),
+        lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
+    _check(library, status, "fractal_atlas_colourise_kfp")
+    return output
+
+
+def atlas_colourise_kfp_planes(library, parent, parent_shape, parent_max_iter, parent_planes, child, child_shape,
+                               child_max_iter, child_planes, output_shape, parent_zoom, child_fraction, child_zoom,
+                               max_iter, centered_input, options, lut, colour=(0.0, 0.0, 0.0, 0.5),
+                               threads: int = 0) -> np.ndarray:
+    """``fractal_atlas_colourise_kfp_planes`` (renderer.h:604-631); plane
+    dicts as for :func:`kfp_planes_struct` (None: no child)."""
+    width, height = output_shape
+    parent = np.ascontiguousarray(parent, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    parent_struct, keep = kfp_planes_struct(parent_planes)
+    child_ptr = child_struct_ref = None
+    cw, ch = child_shape if child is not None else (0, 0)
+    if child is not None:
+        child = np.ascontiguousarray(child, dtype=np.float32)
+        child_ptr = child.ctypes.data_as(_c_float_p)
+        child_struct, more = kfp_planes_struct(child_planes)
+        keep += more
+        child_struct_ref = ctypes.byref(child_struct)
+    output = np.empty(width * height * 3, dtype=np.uint8)
+    status = library.fractal_atlas_colourise_kfp_planes(
+        parent.ctypes.data_as(_c_float_p), parent_shape[0], parent_shape[1], parent_max_iter,
+        ctypes.byref(parent_struct), child_ptr, cw, ch, child_max_iter if child is not None else 0, child_struct_ref,
+        output.ctypes.data_as(_c_u8_p), width, height, parent_zoom, child_fraction, child_zoom, max_iter,
+        centered_input, *colour, ctypes.byref(options), lut.ctypes.data_as(_c_u8_p), lut.shape[0], threads)
+    _check(library, status, "fractal_atlas_colourise_kfp_planes")
+    return output
+
+
+def colourise_kfp_planes(library, field, width: int, height: int, max_iter: int, options, planes: dict, lut,
+                         colour=(0.0, 0.0, 0.0, 0.5), threads: int = 0) -> np.ndarray:
+    """``fractal_colourise_kfp_planes`` (renderer.h:483-497); `planes` maps
+    FractalKfpPlanes field names to arrays (absent names pass NULL), and
+    ``texture`` to (top-down RGB8 rows, width, height, stride)."""
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.uint8)
+    struct, keep = kfp_planes_struct(planes)
     output = np.empty(width * height * 3, dtype=np.uint8)
     status = library.fractal_colourise_kfp_planes(
         field.ctypes.data_as(_c_float_p), output.ctypes.data_as(_c_u8_p), width, height, max_iter, *colour,

@@ -323,6 +323,47 @@ int fractal_atlas_colourise_accents(const float *parent, int parent_width, int p
                                     const uint8_t *accents, int interior_red, int interior_green,
                                     int interior_blue, int threads);
 
+/* fractal_atlas_colourise_kfp (renderer.h:554-576) and its _precise twin
+ * (renderer.h:577-603): parent and child coloured as separate KFP tiles at
+ * output scale (the parent is output-sized; the child covers the rectangle
+ * at child_left/child_top), each with its own stencil edges and ColorMethod 4
+ * bounds, blended across a smoothstep band of `feather` pixels. */
+int fractal_atlas_colourise_kfp(const float *parent, int parent_width, int parent_height, const float *child,
+                                int child_width, int child_height, uint8_t *output, int output_width,
+                                int output_height, int max_iter, int child_left, int child_top, int feather,
+                                double phase, double vocal, double instrumental, double pitch,
+                                const FractalKfpOptions *options, const uint8_t *lut, int lut_size, int threads);
+int fractal_atlas_colourise_kfp_precise(const float *parent, int parent_width, int parent_height, const float *child,
+                                        int child_width, int child_height, uint8_t *output, int output_width,
+                                        int output_height, int max_iter, int child_left, int child_top, int feather,
+                                        double phase, double vocal, double instrumental, double pitch,
+                                        const FractalKfpOptions *options, const uint8_t *lut, int lut_size,
+                                        int threads);
+
+/* fractal_atlas_colourise_kfp_planes (renderer.h:604-631) and its _precise
+ * twin (renderer.h:632-662): the scalar surface and every render plane present
+ * in either tile reprojected to the output (integer planes by nearest sample,
+ * double planes bilinearly, glitch transitions kept, interior samples reset),
+ * the child blended in over its centred rectangle, then the plane-aware KFP
+ * pass (texture merging included) over the composed frame. */
+int fractal_atlas_colourise_kfp_planes(const float *parent, int parent_width, int parent_height, int parent_max_iter,
+                                       const FractalKfpPlanes *parent_planes, const float *child, int child_width,
+                                       int child_height, int child_max_iter, const FractalKfpPlanes *child_planes,
+                                       uint8_t *output, int output_width, int output_height, double parent_zoom,
+                                       double child_fraction, double child_zoom, int max_iter, int centered_input,
+                                       double phase, double vocal, double instrumental, double pitch,
+                                       const FractalKfpOptions *options, const uint8_t *lut, int lut_size,
+                                       int threads);
+int fractal_atlas_colourise_kfp_planes_precise(const float *parent, int parent_width, int parent_height,
+                                               int parent_max_iter, const FractalKfpPlanes *parent_planes,
+                                               const float *child, int child_width, int child_height,
+                                               int child_max_iter, const FractalKfpPlanes *child_planes,
+                                               uint8_t *output, int output_width, int output_height,
+                                               double parent_zoom, double child_fraction, double child_zoom,
+                                               int max_iter, int centered_input, double phase, double vocal,
+                                               double instrumental, double pitch, const FractalKfpOptions *options,
+                                               const uint8_t *lut, int lut_size, int threads);
+
 /* renderer.h:660-687: raw KFP atlas frame.  The parent (crop by
  * parent_zoom) and the child (visible rectangle of child_fraction, crop by
  * child_zoom) are composed into one scalar surface encoded relative to the
