@@ -672,12 +672,81 @@ def run_frame_passes(args) -> int:
     native.atlas_colourise(library, host[0], (width, height), caps[0], host[1], (width, height), caps[1],
                            (width, height), zoom, fraction, 0, 0.3, 0.4, 0.7, 0.5, interior=(0, 0, 0))
     e2e_ms = (time.perf_counter() - t0) * 1e3
+    entries = host_entry_passes(package, library, stack, fields, counts, caps, width, height, zoom, fraction,
+                                args.steps)
     stack.close()
-    print(json.dumps({"frame_passes": results, "parent_zoom": zoom, "child_fraction": fraction,
+    print(json.dumps({"frame_passes": results, "host_entries": entries, "parent_zoom": zoom,
+                      "child_fraction": fraction,
                       "atlas_colourise_cpu_port_ms": round(cpu_ms, 2),
                       "cpu_cores": cores, "atlas_colourise_e2e_host_buffers_ms": round(e2e_ms, 2),
                       "levels": [pair[0][0], pair[1][0]], "caps": caps}))
     return 0
+
+
+def host_entry_passes(package, library, stack, fields, counts, caps, width, height, zoom, fraction, steps):
+    """The renderer.h entries that take host buffers, at 3840x2160: wall time
+    of the call (uploads and readback included) and the device time of its
+    kernels (fractal_gb300_last_kernel_ms), medians of `steps` calls after
+    one warm-up.  Inputs: the two 4K keyframe fields; seeded synthetic render
+    planes (orbit_iteration from the counts, test1 / test2 / phase / DE
+    drawn from fixed distributions); the plane atlas from 1920x1080 halves;
+    the separate-tile child a 1920x1080 centre crop; 2^20 log-polar points
+    around the first keyframe's reference."""
+    import numpy as np
+
+    native, kfp = package.native, package.kfp
+    rng = np.random.default_rng(5)
+    pixels = width * height
+    host = [fields[i].cpu().numpy() for i in range(2)]
+    orbit = [np.maximum(counts[i].cpu().numpy().astype(np.int64) - 1, 0) for i in range(2)]
+
+    def planes_of(i):
+        return {"orbit_iteration": orbit[i], "test1": rng.uniform(1.0e8, 1.0e12, pixels),
+                "test2": rng.uniform(1.0e2, 1.0e6, pixels), "phase": rng.uniform(0.0, 1.0, pixels),
+                "de_x": rng.normal(size=pixels), "de_y": rng.normal(size=pixels)}
+
+    def half(a):
+        return np.ascontiguousarray(a.reshape(height, width)[::2, ::2]).ravel()
+
+    planes = [planes_of(0), planes_of(1)]
+    small = [{k: half(v) for k, v in p.items()} for p in planes]
+    crop = np.ascontiguousarray(host[1].reshape(height, width)[540:1620, 960:2880]).ravel()
+    profile = kfp.recipe("differences7")
+    lut, options = kfp.palette_lut(profile), kfp.options(profile)
+    keyframe = stack.keyframes[0]
+    count = 1 << 20
+    u = rng.uniform(-1.5, 0.5, count)
+    angle = rng.uniform(0.0, 2.0 * math.pi, count)
+    log2_radius = (u - keyframe.log10_zoom) * math.log2(10.0)
+    exponents = np.ceil(log2_radius).astype(np.int32)
+    magnitude = np.exp2(log2_radius - exponents)
+    real, imag = magnitude * np.cos(angle), magnitude * np.sin(angle)
+    cap = max(caps)
+    calls = {
+        "kfp_planes_3840x2160": lambda: native.colourise_kfp_planes(library, host[0], width, height, cap, options,
+                                                                    planes[0], lut),
+        "atlas_kfp_tiles_3840x2160": lambda: native.atlas_colourise_kfp(
+            library, host[0], (width, height), crop, (1920, 1080), (960, 540), 32, cap, options, lut),
+        "atlas_kfp_planes_3840x2160": lambda: native.atlas_colourise_kfp_planes(
+            library, half(host[0]), (1920, 1080), caps[0], small[0], half(host[1]), (1920, 1080), caps[1], small[1],
+            (width, height), zoom, fraction, 1.0, cap, 0, options, lut),
+        "points_1048576": lambda: native.render_points(
+            library, keyframe.reference, package.atlas.zoom_text(keyframe.log10_zoom), real, imag, exponents,
+            keyframe.max_iter),
+    }
+    results = []
+    for name, call in calls.items():
+        walls, kernels = [], []
+        for i in range(1 + steps):
+            t0 = time.perf_counter()
+            call()
+            wall = (time.perf_counter() - t0) * 1e3
+            if i >= 1:
+                walls.append(wall)
+                kernels.append(library.fractal_gb300_last_kernel_ms())
+        results.append({"entry": name, "wall_ms": round(statistics.median(walls), 3),
+                        "device_ms": round(statistics.median(kernels), 4)})
+    return results
 
 
 SONG_FACTOR = 4.0      # atlas keyframe factor of the song workload

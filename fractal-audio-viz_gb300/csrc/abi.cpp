@@ -1048,6 +1048,10 @@ void plane_context(KfpPlanesLaunch& pl, const FractalKfpOptions& o) {
         pl.has_smooth_norm_exponent = 1;
     }
     pl.phase_scale = o.phase_color_strength / 100.0 * 1024.0;
+    pl.smooth_power_ok = std::isfinite(o.power) && o.power > 1.0;
+    pl.smooth_power_log_f = static_cast<float>(pl.has_smooth_power_log ? pl.smooth_power_log : 0.0);
+    pl.smooth_radius_ok = std::isfinite(pl.smooth_bailout_radius) && pl.smooth_bailout_radius > 1.0;
+    pl.smooth_radius_log_f = static_cast<float>(pl.smooth_radius_ok ? std::log(pl.smooth_bailout_radius) : 0.0);
 }
 
 // Bytes of a texture the merge can address: (height - 1) strides plus one row.
@@ -1901,12 +1905,14 @@ int render_points(float* output, int count, const char* zoom_text, const double*
                     check_cuda(cudaMemsetAsync(input.exact_flags, 0, list.size(), stream), "clear repair flags");
                 }
                 std::shared_ptr<DeviceTables> dev = device_tables(*ctx);
+                check_cuda(cudaEventRecord(rt.start, stream), "cudaEventRecord");
                 if (ctx->formula != kFormulaMandelbrot) {
                     launch_deep_alternate(*ctx, *dev, out, n, 1, zoom, max_iter, o, collect, rt, stream, &input);
                 } else {
                     launch_deep_mandelbrot(*ctx, *dev, out, n, 1, zoom, max_iter, series_order, series_block, o,
                                            collect, rt, stream, &input);
                 }
+                check_cuda(cudaEventRecord(rt.stop, stream), "cudaEventRecord");
                 if (host_flags) {
                     check_cuda(cudaMemcpyAsync(host_flags, input.exact_flags, list.size(), cudaMemcpyDeviceToHost,
                                                stream), "copy repair flags");
@@ -1914,6 +1920,11 @@ int render_points(float* output, int count, const char* zoom_text, const double*
             });
         };
         render_list(points, output, planes, repair ? flags.data() : nullptr);
+        ThreadRuntime& timing = thread_runtime();
+        float kernel_ms = 0.0f;
+        if (cudaEventElapsedTime(&kernel_ms, timing.start, timing.stop) == cudaSuccess) {
+            timing.last_kernel_ms = kernel_ms;
+        }
         if (!repair) return;
 
         std::vector<int> flagged;

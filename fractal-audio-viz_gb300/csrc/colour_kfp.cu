@@ -254,6 +254,47 @@ __device__ double plane_smooth_part(const KfpPlanesLaunch& pl, long long i) {
     return isfinite(smooth) ? smooth : 0.0;
 }
 
+// ln x of a positive finite double in FP32 from its exponent field and the
+// top 23 bits of its mantissa (relative error ~2^-23 in the mantissa), so
+// that every double magnitude is in range and no FP64 instruction issues.
+__device__ __forceinline__ float ln_positive(long long bits) {
+    const int exponent = static_cast<int>((bits >> 52) & 0x7ff);
+    if (exponent == 0) return static_cast<float>(log(__longlong_as_double(bits)));  // subnormal
+    const float mantissa = __int_as_float(0x3f800000 | static_cast<int>((bits >> 29) & 0x7fffff));
+    return (static_cast<float>(exponent - 1023) + log2f(mantissa)) * 0.693147180559945309f;
+}
+
+// v < 0 for a double, on its bit pattern (false for -0 and NaN).
+__device__ __forceinline__ bool negative_bits(double v) {
+    const long long b = __double_as_longlong(v);
+    return b < 0 && b != static_cast<long long>(0x8000000000000000ull)
+        && (b & 0x7fffffffffffffffll) <= 0x7ff0000000000000ll;
+}
+
+// SmoothMethod 0 of kfp_plane_smooth_part in FP32: 1 - ln(ln|z| / ln R) /
+// ln p with ln|z| = ln(test1) / 2.  The reference's validity tests reduce to
+// test1 > 1 (finite), R > 1 (finite) and p > 1 (finite), decided on bit
+// patterns.  The term is below 1, so its FP32 error (~1e-7) moves the
+// palette position far less than the +-1 LSB colour budget allows.
+__device__ __forceinline__ float plane_smooth_fast(const KfpPlanesLaunch& pl, long long i) {
+    const long long t = __double_as_longlong(pl.test1[i]);
+    const long long one = 0x3ff0000000000000ll;
+    if (t <= one || ((t >> 52) & 0x7ff) == 0x7ff || !pl.smooth_power_ok) return 0.0f;  // test1 <= 1, NaN / inf
+    float radius_log = pl.smooth_radius_log_f;
+    bool radius_ok = pl.smooth_radius_ok;
+    if (!pl.has_constant_bailout) {
+        const long long b = __double_as_longlong(pl.bailout[i]);
+        if (b > one && ((b >> 52) & 0x7ff) != 0x7ff) {
+            radius_log = ln_positive(b);
+            radius_ok = true;
+        }
+    }
+    if (!radius_ok) return 0.0f;
+    const float numerator = 0.5f * ln_positive(t);
+    const float smooth = 1.0f - logf(numerator / radius_log) / pl.smooth_power_log_f;
+    return isfinite(smooth) ? smooth : 0.0f;
+}
+
 // The colour sample of every pixel from its planes, as a double-float, with
 // flags (bit 0 interior, bit 1 hidden glitch): kfp_plane_orbit_sample
 // (renderer.cpp:5844-5866) from orbit_iteration + the smoothing part, else
@@ -269,6 +310,18 @@ __global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter,
             if (raw >= max_iter) {
                 value = static_cast<double>(max_iter) + 1.0;
                 inside = true;
+            } else if (pl.smooth_method == 0) {
+                // raw < max_iter <= 10^7 < 2^24 is an exact float, so raw +
+                // smooth is an exact double-float, compared with the cap
+                // exactly.
+                const float smooth = pl.test1 != nullptr ? plane_smooth_fast(pl, i) : 0.0f;
+                const Df combined = two_sum(static_cast<float>(raw), smooth);
+                const float cap = static_cast<float>(max_iter);
+                inside = combined.hi > cap || (combined.hi == cap && combined.lo >= 0.0f);
+                samples[i] = inside ? make_float2(cap + 1.0f, 0.0f) : make_float2(combined.hi, combined.lo);
+                const bool hidden = pl.transition != nullptr && !pl.show_glitches && negative_bits(pl.transition[i]);
+                flags[i] = static_cast<unsigned char>((inside ? 1 : 0) | (hidden ? 2 : 0));
+                continue;
             } else {
                 const double combined = static_cast<double>(raw) + plane_smooth_part(pl, i);
                 inside = combined >= static_cast<double>(max_iter);
@@ -286,7 +339,7 @@ __global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter,
         }
         const float hi = static_cast<float>(value);
         samples[i] = make_float2(hi, static_cast<float>(value - static_cast<double>(hi)));
-        const bool hidden = pl.transition != nullptr && pl.transition[i] < 0.0 && !pl.show_glitches;
+        const bool hidden = pl.transition != nullptr && !pl.show_glitches && negative_bits(pl.transition[i]);
         flags[i] = static_cast<unsigned char>((inside ? 1 : 0) | (hidden ? 2 : 0));
     }
 }

@@ -244,6 +244,11 @@ struct KfpPlanesLaunch {
     int has_smooth_power_log, has_smooth_bailout_log, has_smooth_norm_exponent;
     double smooth_power_log, smooth_bailout_log, smooth_norm_exponent;
     double phase_scale;  // phase_color_strength / 100 * 1024
+    // FP32 copies for the SmoothMethod 0 term: log(power) when power is
+    // finite and > 1 (else smooth_power_ok = 0), log of the constant bailout
+    // radius when it is finite and > 1 (else smooth_radius_ok = 0).
+    int smooth_power_ok, smooth_radius_ok;
+    float smooth_power_log_f, smooth_radius_log_f;
     // Texture merging (planes->texture_rgb with texture_enabled): top-down
     // RGB8 rows of `texture_stride` bytes on the device.
     const std::uint8_t* texture;
