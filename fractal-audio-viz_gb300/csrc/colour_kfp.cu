@@ -315,7 +315,7 @@ __global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter,
                 // smooth is an exact double-float, compared with the cap
                 // exactly.
                 const float smooth = pl.test1 != nullptr ? plane_smooth_fast(pl, i) : 0.0f;
-                const Df combined = two_sum(static_cast<float>(raw), smooth);
+                const Df combined = two_sum(static_cast<float>(static_cast<int>(raw)), smooth);
                 const float cap = static_cast<float>(max_iter);
                 inside = combined.hi > cap || (combined.hi == cap && combined.lo >= 0.0f);
                 samples[i] = inside ? make_float2(cap + 1.0f, 0.0f) : make_float2(combined.hi, combined.lo);
@@ -719,7 +719,9 @@ __global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at,
         const float ax = tile_ramp(cx, at.child_width, at.feather), ay = tile_ramp(cy, at.child_height, at.feather);
         alpha = ay < ax ? ay : ax;
     }
-    if (child_inside && alpha >= 0.999999f) {
+    // Alpha exactly 1 outside the band: the reference's blend p * 0 + c * 1
+    // of two finite bytes is c, so only the child tile is coloured.
+    if ((child_inside && alpha >= 0.999999f) || (at.feather >= 2 && alpha == 1.0f)) {
         kfp_pixel<false>(at.child, kc, lut, mc_period, mc_type, none, nullptr, nullptr, cx, cy, x, y, dst);
         return;
     }
