@@ -551,7 +551,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         if (k.smooth) {
             float f = df_value(df_add(position, df_neg(lower_position)));
             if (k.inverse_transition) f = 1.0f - f;
-            const int upper = (lower + 1) % k.lut_size;
+            const int upper = lower + 1 < k.lut_size ? lower + 1 : 0;  // (lower + 1) mod size, lower in [0, size)
             const float g = 1.0f - f;
             o_r = (static_cast<float>(lut[lower * 3]) * g + static_cast<float>(lut[upper * 3]) * f) / 255.0f;
             o_g = (static_cast<float>(lut[lower * 3 + 1]) * g + static_cast<float>(lut[upper * 3 + 1]) * f) / 255.0f;

@@ -443,15 +443,20 @@ __device__ __forceinline__ float encode_sample(const AtlasLaunch& a, float value
 template <bool Exact>
 __device__ __forceinline__ float surface_pixel(bool& undecided, const AtlasLaunch& a, const SourceView& parent,
                                                const SourceView& child, int x, int y) {
+    // The child owns its rectangle outside the seam band, where the parent
+    // sample is not used: it is taken only where a pixel blends.
+    const int cx = x - a.child_left, cy = y - a.child_top;
+    const bool child_here = in_child(a, cx, cy);
+    float child_value = 0.0f, alpha = 0.0f;
+    if (child_here) {
+        const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
+        child_value = c.inside ? a.interior_value : encode_sample(a, c.value);
+        alpha = seam_alpha(a, cx, cy);
+        if (alpha >= 0.999999f) return child_value;
+    }
     const Sample p = sample_preserving_interior<Exact>(parent, a.parent_x, a.parent_y, x, y, undecided);
     const float parent_value = p.inside ? a.interior_value : encode_sample(a, p.value);
-    const int cx = x - a.child_left, cy = y - a.child_top;
-    if (!in_child(a, cx, cy)) return parent_value;
-    const Sample c = sample_preserving_interior<Exact>(child, a.child_x, a.child_y, cx, cy, undecided);
-    const float child_value = c.inside ? a.interior_value : encode_sample(a, c.value);
-    const float alpha = seam_alpha(a, cx, cy);
-    if (alpha >= 0.999999f) return child_value;
-    return parent_value * (1.0f - alpha) + child_value * alpha;
+    return child_here ? parent_value * (1.0f - alpha) + child_value * alpha : parent_value;
 }
 
 // Scalar surface of one pixel of fractal_atlas_colourise_kfp_planes
