@@ -746,6 +746,21 @@ def host_entry_passes(package, library, stack, fields, counts, caps, width, heig
                 kernels.append(library.fractal_gb300_last_kernel_ms())
         results.append({"entry": name, "wall_ms": round(statistics.median(walls), 3),
                         "device_ms": round(statistics.median(kernels), 4)})
+    # The same point render on the host cores through the oracle port (its
+    # own reference at the keyframe's zoom), on the first 2^14 points.
+    port = native.load(os.path.join(ROOT, "oracle", "_ref", "liboracle.so"))
+    zoom = package.atlas.zoom_text(keyframe.log10_zoom)
+    bits = package.atlas.precision_bits(stack.x, stack.y, keyframe.log10_zoom)
+    handle = native.create_reference(port, stack.x, stack.y, zoom, keyframe.max_iter, bits, 32)
+    try:
+        sample = 1 << 14
+        t0 = time.perf_counter()
+        native.render_points(port, handle, zoom, real[:sample], imag[:sample], exponents[:sample], keyframe.max_iter)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+    finally:
+        port.fractal_destroy_reference(handle)
+    results.append({"entry": "points_16384_cpu_port", "wall_ms": round(cpu_ms, 3), "cores": os.cpu_count() or 1,
+                    "points_per_s": round(sample / (cpu_ms * 1e-3), 1)})
     return results
 
 

@@ -765,14 +765,14 @@ __global__ void __launch_bounds__(256) atlas_planes_kernel(const AtlasLaunch a, 
         for (int k = 0; k < 7; ++k) {
             if (out.doubles[k] == nullptr) continue;
             const bool preserve = k == 1, reset = k != 0;
+            // Interior samples of the reset planes are 0 whatever the
+            // interpolation gives, so their FP64 work is skipped.
             double v = 0.0;
-            if (primary.doubles[k] != nullptr) {
+            if (primary.doubles[k] != nullptr && !(inside && reset)) {
                 v = bilinear_double(primary.doubles[k], ps, x, y, preserve);
-                if (inside && reset) v = 0.0;
             }
             if (child_here && secondary.doubles[k] != nullptr) {
-                double c = bilinear_double(secondary.doubles[k], cs, cx, cy, preserve);
-                if (child_inside && reset) c = 0.0;
+                const double c = child_inside && reset ? 0.0 : bilinear_double(secondary.doubles[k], cs, cx, cy, preserve);
                 if (primary.doubles[k] == nullptr) {
                     v = c;
                 } else {
