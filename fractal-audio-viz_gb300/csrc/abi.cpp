@@ -2229,6 +2229,21 @@ int fractal_gb300_device_count(void) {
     return count;
 }
 
+// Self-check of the colour pass's division by a constant: the number of
+// float inputs (of all 2^32) whose quotient differs from IEEE division.
+int fractal_gb300_check_division(float divisor, unsigned long long* mismatches) {
+    return guarded("division check failed with an unknown exception", [&] {
+        if (!mismatches || !std::isfinite(divisor) || divisor == 0.0f) throw Failure{"invalid division check"};
+        ThreadRuntime& rt = thread_runtime();
+        wait_scratch(rt, rt.stream);
+        auto* counter = static_cast<unsigned long long*>(scratch(rt, kScratchWork, sizeof(unsigned long long)));
+        check_cuda(launch_division_check(divisor, counter, rt.stream), "division check launch");
+        check_cuda(cudaMemcpyAsync(mismatches, counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                   rt.stream), "division check");
+        check_cuda(cudaStreamSynchronize(rt.stream), "division check");
+    });
+}
+
 double fractal_gb300_last_kernel_ms(void) {
     try {
         return thread_runtime().last_kernel_ms;

@@ -85,6 +85,25 @@ __device__ __forceinline__ float sample(const float* __restrict__ field, const K
     return v;
 }
 
+// x / d for a constant divisor d with r = RN(1 / d), by Markstein's
+// correction of the rounded product (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): q0 = RN(x r), e = x - q0 d (exact by FMA), q = RN(q0 +
+// e r).  Three FP32 operations instead of a division; for the divisors the
+// colour pass uses, q equals the IEEE quotient x / d for every x with |x| in
+// [2^-100, 2^100], which fractal_gb300_check_division verifies for all 2^32
+// inputs; zero, tiny, huge and non-finite x take the division.
+__device__ __forceinline__ float div_const(float x, float d, float r) {
+    const float ax = fabsf(x);
+    if (!(ax >= 0x1p-100f && ax <= 0x1p100f)) return x / d;
+    const float q0 = __fmul_rn(x, r);
+    const float e = __fmaf_rn(-q0, d, x);
+    return __fmaf_rn(e, r, q0);
+}
+
+constexpr float kHalfPiF = kPiF / 2.0f;
+#define FGB_DIV(x, d) div_const((x), (d), 1.0f / (d))
+
 // kfp_reflected_sample: out-of-frame neighbours mirror through the centre.
 __device__ __forceinline__ float reflected(const float* __restrict__ field, const KfpDevice& k, int x, int y,
                                            int dx, int dy, float centre) {
@@ -126,13 +145,13 @@ __device__ float difference_magnitude(int differences, float c, float l, float r
             return sqrtf(dx * dx + dy * dy) * s;
         }
         case 5: {
-            const float dx = ((r - l) + (tr - tl) + (br - bl)) / 6.0f;
-            const float dy = ((d - u) + (bl - tl) + (br - tr)) / 6.0f;
+            const float dx = FGB_DIV((r - l) + (tr - tl) + (br - bl), 6.0f);
+            const float dy = FGB_DIV((d - u) + (bl - tl) + (br - tr), 6.0f);
             return sqrtf(dx * dx + dy * dy) * s;
         }
         case 6: {
             const float lap = dtl + 4.0f * du + dtr + 4.0f * dl + 4.0f * dr + dbl + 4.0f * dd + dbr;
-            return sqrtf(fabsf(lap / 6.0f * 1.4426950408889634f)) * s;
+            return sqrtf(fabsf(FGB_DIV(lap, 6.0f) * 1.4426950408889634f)) * s;
         }
         default:
             return 0.0f;  // analytic DE needs planes
@@ -479,7 +498,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         }
     }
     if (!analytic && k.needs_difference) gradient = difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br);
-    float distance = isnan(gradient) ? 0.0f : gradient * static_cast<float>(k.spatial_width) / 640.0f;
+    float distance = isnan(gradient) ? 0.0f : FGB_DIV(gradient * static_cast<float>(k.spatial_width), 640.0f);
     if (distance < 0.0f) distance = 0.0f;
     Df transfer_df = colour_iter_df;  // kept in double-float for methods 0, 4 and 6's iteration branch
     bool exact_transfer = k.color_method == 0 || k.color_method == 4;
@@ -553,13 +572,15 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
             if (k.inverse_transition) f = 1.0f - f;
             const int upper = lower + 1 < k.lut_size ? lower + 1 : 0;  // (lower + 1) mod size, lower in [0, size)
             const float g = 1.0f - f;
-            o_r = (static_cast<float>(lut[lower * 3]) * g + static_cast<float>(lut[upper * 3]) * f) / 255.0f;
-            o_g = (static_cast<float>(lut[lower * 3 + 1]) * g + static_cast<float>(lut[upper * 3 + 1]) * f) / 255.0f;
-            o_b = (static_cast<float>(lut[lower * 3 + 2]) * g + static_cast<float>(lut[upper * 3 + 2]) * f) / 255.0f;
+            o_r = FGB_DIV(static_cast<float>(lut[lower * 3]) * g + static_cast<float>(lut[upper * 3]) * f, 255.0f);
+            o_g = FGB_DIV(static_cast<float>(lut[lower * 3 + 1]) * g + static_cast<float>(lut[upper * 3 + 1]) * f,
+                          255.0f);
+            o_b = FGB_DIV(static_cast<float>(lut[lower * 3 + 2]) * g + static_cast<float>(lut[upper * 3 + 2]) * f,
+                          255.0f);
         } else {
-            o_r = static_cast<float>(lut[lower * 3]) / 255.0f;
-            o_g = static_cast<float>(lut[lower * 3 + 1]) / 255.0f;
-            o_b = static_cast<float>(lut[lower * 3 + 2]) / 255.0f;
+            o_r = FGB_DIV(static_cast<float>(lut[lower * 3]), 255.0f);
+            o_g = FGB_DIV(static_cast<float>(lut[lower * 3 + 1]), 255.0f);
+            o_b = FGB_DIV(static_cast<float>(lut[lower * 3 + 2]), 255.0f);
         }
     };
     if (k.multi_color) {
@@ -640,9 +661,9 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     if (k.needs_slopes) {
         const float horizontal = analytic ? analytic_x : (x > 0 ? l - centre : centre - r);
         const float vertical = analytic ? analytic_y : (y == 0 ? centre - d : u - centre);
-        const float projected = (horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
-            * static_cast<float>(k.spatial_width) / 640.0f;
-        const float strength = atanf(fabsf(projected)) / (kPiF / 2.0f) * k.slope_ratio / 100.0f;
+        const float projected = FGB_DIV((horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
+                                            * static_cast<float>(k.spatial_width), 640.0f);
+        const float strength = FGB_DIV(FGB_DIV(atanf(fabsf(projected)), kHalfPiF) * k.slope_ratio, 100.0f);
         if (projected >= 0.0f) {
             red *= 1.0f - strength;
             green *= 1.0f - strength;
@@ -945,6 +966,32 @@ cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, con
         cudaFuncSetAttribute(kfp_atlas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
     }
     kfp_atlas_kernel<<<grid, block, shared, stream>>>(atlas, rgb, kp, kc, lut, mc_period, mc_type);
+    return cudaGetLastError();
+}
+
+namespace {
+
+// Every 32-bit pattern x: div_const(x, d, RN(1/d)) against the IEEE quotient
+// x / d, bit for bit (any two NaNs agree); mismatches are counted.
+__global__ void division_check_kernel(float d, unsigned long long* mismatches) {
+    const float r = 1.0f / d;
+    unsigned long long local = 0;
+    for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+         i < (1ull << 32); i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const float x = __uint_as_float(static_cast<unsigned>(i));
+        const float want = x / d, got = div_const(x, d, r);
+        const bool same = __float_as_uint(want) == __float_as_uint(got) || (isnan(want) && isnan(got));
+        local += same ? 0 : 1;
+    }
+    if (local) atomicAdd(mismatches, local);
+}
+
+}  // namespace
+
+cudaError_t launch_division_check(float divisor, unsigned long long* mismatches, cudaStream_t stream) {
+    cudaError_t status = cudaMemsetAsync(mismatches, 0, sizeof(unsigned long long), stream);
+    if (status != cudaSuccess) return status;
+    division_check_kernel<<<152 * 16, 256, 0, stream>>>(divisor, mismatches);
     return cudaGetLastError();
 }
 

@@ -276,6 +276,9 @@ struct KfpAtlasLaunch {
 cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, const KfpLaunch& parent_launch,
                              const std::uint8_t* lut, const double* mc_period, const int* mc_type,
                              cudaStream_t stream);
+// Counts the float inputs for which the colour pass's constant division
+// (div_const) differs from IEEE division by `divisor` (all 2^32 patterns).
+cudaError_t launch_division_check(float divisor, unsigned long long* mismatches, cudaStream_t stream);
 cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& launch, const std::uint8_t* lut,
                        const double* mc_period, const int* mc_type, cudaStream_t stream,
                        const KfpPlanesLaunch* planes = nullptr, const void* samples = nullptr,

@@ -387,6 +387,7 @@ _GB300_ABI = (
     ("fractal_gb300_device_count", ctypes.c_int, ()),
     ("fractal_gb300_set_table_builder", None, (ctypes.c_int,)),
     ("fractal_gb300_last_kernel_ms", ctypes.c_double, ()),
+    ("fractal_gb300_check_division", ctypes.c_int, (ctypes.c_float, ctypes.POINTER(ctypes.c_ulonglong))),
     ("fractal_gb300_render_reference_device", ctypes.c_int,
      (ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -457,6 +457,10 @@ void fractal_gb300_set_table_builder(int on_device);
 int fractal_gb300_device_count(void);
 /* Duration in ms of the last render/colour kernel issued by this thread,
  * measured with CUDA events on its stream (after a synchronous call). */
+/* Self-check: of all 2^32 float inputs, how many give a quotient by
+ * `divisor` through the KFP pass's constant division (a rounded-reciprocal
+ * product with one FMA correction) that differs from IEEE division. */
+int fractal_gb300_check_division(float divisor, unsigned long long *mismatches);
 double fractal_gb300_last_kernel_ms(void);
 
 /* Deep or direct render of one field from a prepared reference into device

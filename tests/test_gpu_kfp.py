@@ -43,3 +43,15 @@ def test_kfp_matches_reference_within_one_lsb(product, package, expected_rgb):
     bad = {k: v for k, v in worst.items() if v > 1}
     assert not bad, bad
     assert exact / total > 0.999, exact / total
+
+
+@pytest.mark.parametrize("divisor", [255.0, 640.0, 100.0, 6.0, float(np.float32(np.pi) / np.float32(2.0))])
+def test_constant_division_equals_ieee_division(product, divisor):
+    """The KFP pass divides by its constants with a rounded-reciprocal
+    product and one FMA correction; for every one of the 2^32 float inputs
+    the quotient equals IEEE division bit for bit."""
+    import ctypes
+
+    mismatches = ctypes.c_ulonglong(99)
+    assert product.fractal_gb300_check_division(divisor, ctypes.byref(mismatches)) == 0
+    assert mismatches.value == 0
