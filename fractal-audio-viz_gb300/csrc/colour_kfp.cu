@@ -679,12 +679,23 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     out[2] = dither_byte(blue, dither_x, dither_y, 2);
 }
 
+// Copies the palette into shared memory once per block: 4-byte words when
+// the table is word-aligned, then the tail bytes.
 __device__ __forceinline__ void stage_lut(unsigned char* lut, const unsigned char* __restrict__ lut_global, int size) {
-    for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < size * 3; i += blockDim.x * blockDim.y) {
-        lut[i] = lut_global[i];
+    const int bytes = size * 3;
+    const int thread = threadIdx.y * blockDim.x + threadIdx.x, threads = blockDim.x * blockDim.y;
+    int done = 0;
+    if ((reinterpret_cast<std::uintptr_t>(lut_global) & 3) == 0) {
+        const int words = bytes >> 2;
+        const unsigned* src = reinterpret_cast<const unsigned*>(lut_global);
+        unsigned* dst = reinterpret_cast<unsigned*>(lut);
+        for (int i = thread; i < words; i += threads) dst[i] = __ldg(src + i);
+        done = words << 2;
     }
+    for (int i = done + thread; i < bytes; i += threads) lut[i] = lut_global[i];
     __syncthreads();
 }
+
 
 template <bool Planes>
 __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
@@ -715,16 +726,10 @@ __device__ __forceinline__ float tile_ramp(int i, int size, int feather) {
 // interior child pixel of the owned region, the child or parent by
 // interior test without a feather band, else both tiles blended in FP64
 // and rounded half-even (rounded_colour_byte).
-__global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at, unsigned char* __restrict__ rgb,
-                                                        const KfpDevice kp, const KfpDevice kc,
-                                                        const unsigned char* __restrict__ lut_global,
-                                                        const double* __restrict__ mc_period,
-                                                        const int* __restrict__ mc_type) {
-    extern __shared__ unsigned char lut[];
-    stage_lut(lut, lut_global, kp.lut_size);
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= kp.width || y >= kp.height) return;
+__device__ __forceinline__ void kfp_atlas_pixel(const KfpAtlasLaunch& at, unsigned char* __restrict__ rgb,
+                                                const KfpDevice& kp, const KfpDevice& kc, const unsigned char* lut,
+                                                const double* __restrict__ mc_period,
+                                                const int* __restrict__ mc_type, int x, int y) {
     unsigned char* dst = rgb + 3 * (static_cast<long long>(y) * kp.width + x);
     const KfpPlanesLaunch none{};
     const int cx = x - at.child_left, cy = y - at.child_top;
@@ -766,6 +771,19 @@ __global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at,
         v = v < 0.0 ? 0.0 : (v > 255.0 ? 255.0 : v);
         dst[ch] = static_cast<unsigned char>(__double2int_rn(v));
     }
+}
+
+// fractal_atlas_colourise_kfp, one 32 x 8 tile per block.
+__global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at, unsigned char* __restrict__ rgb,
+                                                        const KfpDevice kp, const KfpDevice kc,
+                                                        const unsigned char* __restrict__ lut_global,
+                                                        const double* __restrict__ mc_period,
+                                                        const int* __restrict__ mc_type) {
+    extern __shared__ unsigned char lut[];
+    stage_lut(lut, lut_global, kp.lut_size);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < kp.width && y < kp.height) kfp_atlas_pixel(at, rgb, kp, kc, lut, mc_period, mc_type, x, y);
 }
 
 // ColorMethod 4 bounds: min/max of floor(sample) over escaped pixels below
@@ -960,11 +978,11 @@ cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, con
     child_launch.transfer_max = atlas.child_transfer_max;
     const KfpDevice kc = kfp_device(child_launch, parent_launch.width);
     const dim3 block(32, 8);
-    const dim3 grid((parent_launch.width + 31) / 32, (parent_launch.height + 7) / 8);
     const std::size_t shared = static_cast<std::size_t>(parent_launch.lut_size) * 3;
     if (shared > 48 * 1024) {
         cudaFuncSetAttribute(kfp_atlas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
     }
+    const dim3 grid((parent_launch.width + 31) / 32, (parent_launch.height + 7) / 8);
     kfp_atlas_kernel<<<grid, block, shared, stream>>>(atlas, rgb, kp, kc, lut, mc_period, mc_type);
     return cudaGetLastError();
 }
