@@ -7,8 +7,8 @@
 // interpolation, MultiColor HSV waves (:5580-5630), slopes (3D relief) and
 // Kalles' ordered dither (:5246-5258, 5314-5332).
 //
-// The kernel is HBM-bound by design (4 B of field in, 3 B of RGB out per
-// pixel; the stencil re-reads hit L1).  Precision: stencil differences are
+// Algorithmically HBM-bound (4 B of field in, 3 B of RGB out per pixel; the
+// stencil re-reads and the palette hit L1); in practice issue-bound.  Precision: stencil differences are
 // formed in FP32, which is exact for neighbouring values within a factor of
 // two (Sterbenz); the transcendentals (log, sqrt, pow, atan, sin) run in
 // FP32; the palette position (division by IterDiv, offset, modulo, floor) is
@@ -370,7 +370,9 @@ __global__ void kfp_plane_bounds_kernel(const float2* __restrict__ samples, cons
 
 // write_kfp_pixel (renderer.cpp:6696-7289) for source pixel (x, y) of a
 // k.width x k.height field, dithered at output position (dither_x,
-// dither_y); `lut` is the palette staged in shared memory.
+// dither_y); `lut` is the palette in global memory (3 KB at the usual 1024
+// entries: it stays in L1, which served it faster than a per-block copy into
+// shared memory).
 template <bool Planes>
 __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const KfpDevice& k,
                                           const unsigned char* lut, const double* __restrict__ mc_period,
@@ -679,36 +681,16 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     out[2] = dither_byte(blue, dither_x, dither_y, 2);
 }
 
-// Copies the palette into shared memory once per block: 4-byte words when
-// the table is word-aligned, then the tail bytes.
-__device__ __forceinline__ void stage_lut(unsigned char* lut, const unsigned char* __restrict__ lut_global, int size) {
-    const int bytes = size * 3;
-    const int thread = threadIdx.y * blockDim.x + threadIdx.x, threads = blockDim.x * blockDim.y;
-    int done = 0;
-    if ((reinterpret_cast<std::uintptr_t>(lut_global) & 3) == 0) {
-        const int words = bytes >> 2;
-        const unsigned* src = reinterpret_cast<const unsigned*>(lut_global);
-        unsigned* dst = reinterpret_cast<unsigned*>(lut);
-        for (int i = thread; i < words; i += threads) dst[i] = __ldg(src + i);
-        done = words << 2;
-    }
-    for (int i = done + thread; i < bytes; i += threads) lut[i] = lut_global[i];
-    __syncthreads();
-}
-
-
 template <bool Planes>
 __global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
                                                   const KfpDevice k, const unsigned char* __restrict__ lut_global,
                                                   const double* __restrict__ mc_period, const int* __restrict__ mc_type,
                                                   const KfpPlanesLaunch pl, const float2* __restrict__ psamples,
                                                   const unsigned char* __restrict__ pflags) {
-    extern __shared__ unsigned char lut[];
-    stage_lut(lut, lut_global, k.lut_size);
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= k.width || y >= k.height) return;
-    kfp_pixel<Planes>(field, k, lut, mc_period, mc_type, pl, psamples, pflags, x, y, x, y,
+    kfp_pixel<Planes>(field, k, lut_global, mc_period, mc_type, pl, psamples, pflags, x, y, x, y,
                       rgb + 3 * (static_cast<long long>(y) * k.width + x));
 }
 
@@ -779,11 +761,9 @@ __global__ void __launch_bounds__(256) kfp_atlas_kernel(const KfpAtlasLaunch at,
                                                         const unsigned char* __restrict__ lut_global,
                                                         const double* __restrict__ mc_period,
                                                         const int* __restrict__ mc_type) {
-    extern __shared__ unsigned char lut[];
-    stage_lut(lut, lut_global, kp.lut_size);
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x < kp.width && y < kp.height) kfp_atlas_pixel(at, rgb, kp, kc, lut, mc_period, mc_type, x, y);
+    if (x < kp.width && y < kp.height) kfp_atlas_pixel(at, rgb, kp, kc, lut_global, mc_period, mc_type, x, y);
 }
 
 // ColorMethod 4 bounds: min/max of floor(sample) over escaped pixels below
@@ -948,20 +928,11 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
     const KfpDevice k = kfp_device(launch, launch.width);
     const dim3 block(32, 8);
     const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
-    const std::size_t shared = static_cast<std::size_t>(launch.lut_size) * 3;
     if (planes != nullptr) {
-        if (shared > 48 * 1024) {
-            cudaFuncSetAttribute(kfp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(shared));
-        }
-        kfp_kernel<true><<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type, *planes,
+        kfp_kernel<true><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, *planes,
                                                           static_cast<const float2*>(samples), flags);
     } else {
-        if (shared > 48 * 1024) {
-            cudaFuncSetAttribute(kfp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(shared));
-        }
-        kfp_kernel<false><<<grid, block, shared, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
+        kfp_kernel<false><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
                                                            nullptr, nullptr);
     }
     return cudaGetLastError();
@@ -978,12 +949,8 @@ cudaError_t launch_kfp_atlas(const KfpAtlasLaunch& atlas, std::uint8_t* rgb, con
     child_launch.transfer_max = atlas.child_transfer_max;
     const KfpDevice kc = kfp_device(child_launch, parent_launch.width);
     const dim3 block(32, 8);
-    const std::size_t shared = static_cast<std::size_t>(parent_launch.lut_size) * 3;
-    if (shared > 48 * 1024) {
-        cudaFuncSetAttribute(kfp_atlas_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(shared));
-    }
     const dim3 grid((parent_launch.width + 31) / 32, (parent_launch.height + 7) / 8);
-    kfp_atlas_kernel<<<grid, block, shared, stream>>>(atlas, rgb, kp, kc, lut, mc_period, mc_type);
+    kfp_atlas_kernel<<<grid, block, 0, stream>>>(atlas, rgb, kp, kc, lut, mc_period, mc_type);
     return cudaGetLastError();
 }
 
