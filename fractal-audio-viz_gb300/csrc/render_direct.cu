@@ -729,17 +729,14 @@ cudaError_t launch_formula(const DirectBatch& b, int formula, int sms, int block
 }
 
 // Aurora palette lookup (write_colour_pixel, renderer.cpp:5210-5237): the
-// palette index is smooth * ((size-1)/max_iter) formed in double from a
-// float32 scale, truncated and clamped; interior and non-finite pixels are
-// black.  Four pixels per thread: 16 B of field in, 12 B of RGB out.
-__global__ void __launch_bounds__(1024) aurora_kernel(const float* __restrict__ field,
+// palette index is smooth * ((size-1)/max_iter), the reference's double
+// product of two floats, truncated and clamped; interior and non-finite
+// pixels take the interior colour.  Four pixels per thread: 16 B of field in, 12 B of RGB out.
+__global__ void __launch_bounds__(256) aurora_kernel(const float* __restrict__ field,
                                                      std::uint8_t* __restrict__ rgb, long long pixels,
                                                      const std::uint8_t* __restrict__ lut, int lut_size,
                                                      float index_scale, int max_iter, int vector_ok,
                                                      std::uint32_t interior) {
-    extern __shared__ std::uint8_t palette[];
-    for (int i = threadIdx.x; i < lut_size * 3; i += blockDim.x) palette[i] = lut[i];
-    __syncthreads();
     const float limit = static_cast<float>(max_iter);
     const long long quads = vector_ok ? pixels / 4 : 0;
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
@@ -750,13 +747,24 @@ __global__ void __launch_bounds__(1024) aurora_kernel(const float* __restrict__ 
             dst[2] = static_cast<std::uint8_t>(interior >> 16);
             return;
         }
-        const double scaled = static_cast<double>(smooth) * static_cast<double>(index_scale);
-        const int k = scaled >= static_cast<double>(lut_size - 1)
-            ? lut_size - 1
-            : (!(scaled > 0.0) ? 0 : static_cast<int>(scaled));
-        dst[0] = palette[3 * k];
-        dst[1] = palette[3 * k + 1];
-        dst[2] = palette[3 * k + 2];
+        // trunc(double(smooth) * double(index_scale)), clamped: the product
+        // of two floats is exact as p + e (FMA two-product), so it is
+        // compared and truncated without FP64 (smooth is finite here).
+        const float p = smooth * index_scale;
+        const float e = __fmaf_rn(smooth, index_scale, -p);
+        const float last_f = static_cast<float>(lut_size - 1);
+        int k;
+        if (p > last_f || (p == last_f && e >= 0.0f)) {
+            k = lut_size - 1;
+        } else if (!(p > 0.0f)) {
+            k = 0;
+        } else {
+            const float f = floorf(p);
+            k = static_cast<int>(f) - (p == f && e < 0.0f ? 1 : 0);
+        }
+        dst[0] = __ldg(lut + 3 * k);
+        dst[1] = __ldg(lut + 3 * k + 1);
+        dst[2] = __ldg(lut + 3 * k + 2);
     };
     for (long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < quads; q += stride) {
         const float4 v = __ldcs(reinterpret_cast<const float4*>(field) + q);
@@ -871,23 +879,17 @@ cudaError_t launch_aurora(const float* field, std::uint8_t* rgb, long long pixel
     int device = 0, sms = 152;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const std::size_t shared = static_cast<std::size_t>(lut_size) * 3;
+    // The palette (up to 192 KiB) is read through L1: neighbouring pixels
+    // take neighbouring entries.
     const long long quads = (pixels + 3) / 4;
-    // The palette is copied into shared memory by every block: with a large
-    // palette (up to 192 KiB) run one 1024-thread block per SM so the copy is
-    // made once per SM, not once per 256 pixels.
-    const int threads = shared > 48 * 1024 ? 1024 : 256;
+    const int threads = 256;
     long long blocks = (quads + threads - 1) / threads;
-    const long long cap = static_cast<long long>(sms) * (shared > 48 * 1024 ? 1 : 8);
+    const long long cap = static_cast<long long>(sms) * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    if (shared > 48 * 1024) {
-        cudaFuncSetAttribute(aurora_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(shared));
-    }
     const int vector_ok = (reinterpret_cast<std::uintptr_t>(field) % 16 == 0)
         && (reinterpret_cast<std::uintptr_t>(rgb) % 4 == 0);
-    aurora_kernel<<<static_cast<unsigned>(blocks), threads, shared, stream>>>(field, rgb, pixels, lut, lut_size,
+    aurora_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(field, rgb, pixels, lut, lut_size,
                                                                               index_scale, max_iter, vector_ok,
                                                                               interior);
     return cudaGetLastError();
