@@ -930,8 +930,10 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const unsigned quads_per_row = static_cast<unsigned>((a.out_width + 3) / 4);
     const unsigned total = quads_per_row * static_cast<unsigned>(a.out_height);
+    // One quad per thread: blocks retire as they finish, so uneven pixels
+    // (the seam band's second sample, the child rectangle) balance
+    // themselves.
     long long blocks = (static_cast<long long>(total) + 255) / 256;
-    if (blocks > static_cast<long long>(sms) * 8) blocks = static_cast<long long>(sms) * 8;
     atlas_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, stream>>>(a, quads_per_row, total);
     status = cudaGetLastError();
     if (status != cudaSuccess) return status;
