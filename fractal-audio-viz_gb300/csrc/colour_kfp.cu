@@ -682,7 +682,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
 }
 
 template <bool Planes>
-__global__ void __launch_bounds__(256) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
+__global__ void __launch_bounds__(256, 6) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
                                                   const KfpDevice k, const unsigned char* __restrict__ lut_global,
                                                   const double* __restrict__ mc_period, const int* __restrict__ mc_type,
                                                   const KfpPlanesLaunch pl, const float2* __restrict__ psamples,
