@@ -318,7 +318,7 @@ __device__ __forceinline__ float plane_smooth_fast(const KfpPlanesLaunch& pl, lo
 // flags (bit 0 interior, bit 1 hidden glitch): kfp_plane_orbit_sample
 // (renderer.cpp:5844-5866) from orbit_iteration + the smoothing part, else
 // stored iteration + 1 - transition (kfp_plane_colour_sample, 5868-5911).
-__global__ void kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter, long long pixels, float2* samples,
+__global__ void __launch_bounds__(256, 6) kfp_plane_samples_kernel(const KfpPlanesLaunch pl, int max_iter, long long pixels, float2* samples,
                                          unsigned char* flags) {
     for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < pixels;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
