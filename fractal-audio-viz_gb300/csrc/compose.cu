@@ -632,7 +632,7 @@ __device__ __forceinline__ void queue_exact(const AtlasLaunch& a, bool undecided
 // 12 bytes (RGB, three aligned words); everything else stores per pixel.  A
 // pixel whose sample could not be decided in double-float is written with a
 // placeholder and queued for atlas_exact_kernel, which rewrites it.
-__global__ void __launch_bounds__(256) atlas_kernel(const AtlasLaunch a, unsigned quads_per_row,
+__global__ void __launch_bounds__(256, 8) atlas_kernel(const AtlasLaunch a, unsigned quads_per_row,
                                                     unsigned total_quads) {
     const bool vector_rows = (a.out_width & 3) == 0;
     const SourceView parent = parent_view(a), child = child_view(a);
