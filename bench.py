@@ -617,6 +617,7 @@ def run_frame_passes(args) -> int:
     lut = torch.from_numpy(kfp.palette_lut(profile)).cuda()
     options = kfp.options(profile)
     h = ctypes.c_void_p(stream.cuda_stream)
+    packed = torch.empty(pixels * 4, dtype=torch.uint8, device="cuda")
     passes = {
         "atlas_colourise": (lambda: library.fractal_gb300_atlas_colourise_device(
             fields[0].data_ptr(), width, height, caps[0], fields[1].data_ptr(), width, height, caps[1],
@@ -637,6 +638,14 @@ def run_frame_passes(args) -> int:
         "kfp_colour": (lambda: library.fractal_gb300_colourise_kfp_device(
             ctypes.c_void_p(fields[0].data_ptr()), ctypes.c_void_p(rgb.data_ptr()), width, height, caps[0],
             ctypes.byref(options), ctypes.c_void_p(lut.data_ptr()), lut.shape[0], h), pixels * 7),
+        # Frame packing for the encoder pipe: RGB8 in (3 B), NV12 out (1.5 B)
+        # or RGBA out (4 B) per pixel.
+        "pack_nv12": (lambda: library.fractal_gb300_pack_frame_device(
+            ctypes.c_void_p(rgb.data_ptr()), width, height, 4, ctypes.c_void_p(packed.data_ptr()), h),
+            pixels * 3 + pixels * 3 // 2),
+        "pack_rgba": (lambda: library.fractal_gb300_pack_frame_device(
+            ctypes.c_void_p(rgb.data_ptr()), width, height, 2, ctypes.c_void_p(packed.data_ptr()), h),
+            pixels * 7),
     }
     peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"), encoding="ascii"))["hbm_gbs"]
     results = []
