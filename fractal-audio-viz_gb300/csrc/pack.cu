@@ -16,8 +16,8 @@
 // (coefficients: the BT.709 matrix scaled to 8-bit studio swing, x 256,
 // rounded so that each chroma row sums to zero: greys map to 128), chroma
 // taken from the rounded mean of the 2x2 block's R, G, B.
-// One thread per 2x2 block: its four Y samples and one chroma pair; HBM-bound
-// (3 B in, 1.5 B out per pixel for YUV).
+// One thread per 2x2 block (any shape) or per 4x2 pixels with word accesses
+// (the common shape); HBM-bound (3 B in, 1.5 B out per pixel for YUV).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -80,6 +80,63 @@ __global__ void pack_yuv_kernel(const std::uint8_t* __restrict__ rgb, std::uint8
     }
 }
 
+// The same conversion for the common frame shape (width a multiple of 4,
+// even height, 4-byte aligned buffers): one thread per 4x2 pixels, i.e. two
+// chroma blocks side by side, with 4-byte loads and stores (three words of
+// RGB per row in, one word of Y per row, one word of interleaved U/V or two
+// half-words of U and V out).
+__global__ void pack_yuv_wide_kernel(const std::uint8_t* __restrict__ rgb, std::uint8_t* __restrict__ out,
+                                     int width, int height, int interleaved) {
+    const int quads = width >> 2, rows = height >> 1;
+    const long long units = static_cast<long long>(quads) * rows;
+    const long long chroma_blocks = static_cast<long long>(width >> 1) * rows;
+    std::uint8_t* y_plane = out;
+    std::uint8_t* u_plane = out + static_cast<long long>(width) * height;
+    std::uint8_t* v_plane = u_plane + chroma_blocks;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < units;
+         t += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int by = static_cast<int>(t / quads), qx = static_cast<int>(t - static_cast<long long>(by) * quads);
+        const int x0 = qx << 2;
+        int sr[2] = {0, 0}, sg[2] = {0, 0}, sb[2] = {0, 0};
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            const long long i = static_cast<long long>(2 * by + dy) * width + x0;
+            const std::uint32_t* src = reinterpret_cast<const std::uint32_t*>(rgb + 3 * i);
+            const std::uint32_t w0 = __ldg(src), w1 = __ldg(src + 1), w2 = __ldg(src + 2);
+            // Bytes r0 g0 b0 r1 | g1 b1 r2 g2 | b2 r3 g3 b3.
+            const int r[4] = {static_cast<int>(w0 & 255), static_cast<int>(w0 >> 24), static_cast<int>((w1 >> 16) & 255),
+                              static_cast<int>((w2 >> 8) & 255)};
+            const int g[4] = {static_cast<int>((w0 >> 8) & 255), static_cast<int>(w1 & 255),
+                              static_cast<int>(w1 >> 24), static_cast<int>((w2 >> 16) & 255)};
+            const int b[4] = {static_cast<int>((w0 >> 16) & 255), static_cast<int>((w1 >> 8) & 255),
+                              static_cast<int>(w2 & 255), static_cast<int>(w2 >> 24)};
+            std::uint32_t luma_word = 0;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                luma_word |= static_cast<std::uint32_t>(luma(r[p], g[p], b[p])) << (8 * p);
+                sr[p >> 1] += r[p];
+                sg[p >> 1] += g[p];
+                sb[p >> 1] += b[p];
+            }
+            *reinterpret_cast<std::uint32_t*>(y_plane + i) = luma_word;
+        }
+        std::uint32_t u[2], v[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int r = (sr[c] + 2) >> 2, g = (sg[c] + 2) >> 2, b = (sb[c] + 2) >> 2;
+            u[c] = static_cast<std::uint32_t>(chroma_u(r, g, b));
+            v[c] = static_cast<std::uint32_t>(chroma_v(r, g, b));
+        }
+        const long long k = static_cast<long long>(by) * (width >> 1) + (qx << 1);  // first of the two blocks
+        if (interleaved) {
+            *reinterpret_cast<std::uint32_t*>(u_plane + 2 * k) = u[0] | (v[0] << 8) | (u[1] << 16) | (v[1] << 24);
+        } else {
+            *reinterpret_cast<std::uint16_t*>(u_plane + k) = static_cast<std::uint16_t>(u[0] | (u[1] << 8));
+            *reinterpret_cast<std::uint16_t*>(v_plane + k) = static_cast<std::uint16_t>(v[0] | (v[1] << 8));
+        }
+    }
+}
+
 }  // namespace
 
 std::size_t packed_frame_bytes(int width, int height, int format) {
@@ -106,6 +163,11 @@ cudaError_t launch_pack_frame(const std::uint8_t* rgb, int width, int height, in
     if (format == 1 || format == 2) {
         pack_rgbx_kernel<<<blocks, 256, 0, stream>>>(rgb, reinterpret_cast<std::uint32_t*>(out), pixels,
                                                      format == 2 ? 255u : 0u);
+    } else if (width % 4 == 0 && height % 2 == 0 && (reinterpret_cast<std::uintptr_t>(rgb) & 3) == 0
+               && (reinterpret_cast<std::uintptr_t>(out) & 3) == 0) {
+        const long long units = static_cast<long long>(width / 4) * (height / 2);
+        const unsigned wide = static_cast<unsigned>((units + 255) / 256 < blocks ? (units + 255) / 256 : blocks);
+        pack_yuv_wide_kernel<<<wide > 0 ? wide : 1, 256, 0, stream>>>(rgb, out, width, height, format == 4 ? 1 : 0);
     } else {
         pack_yuv_kernel<<<blocks, 256, 0, stream>>>(rgb, out, width, height, format == 4 ? 1 : 0);
     }

@@ -27,7 +27,7 @@ def _oracle():
     return module
 
 
-@pytest.mark.parametrize("size", [(3840, 2160), (1921, 1081), (7, 5)])
+@pytest.mark.parametrize("size", [(3840, 2160), (1924, 1082), (4, 2), (1922, 1080), (1921, 1081), (7, 5)])
 @pytest.mark.parametrize("fmt", ["rgb24", "rgb0", "rgba", "yuv420p", "nv12"])
 def test_pack_matches_oracle(product, size, fmt):
     import torch
