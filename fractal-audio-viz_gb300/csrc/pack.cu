@@ -41,6 +41,26 @@ __global__ void pack_rgbx_kernel(const std::uint8_t* __restrict__ rgb, std::uint
     }
 }
 
+// Four pixels per thread for 4-byte aligned RGB and 16-byte aligned output:
+// three word loads, one 16-byte store; `quads` = pixels / 4 (the caller packs
+// any remainder with pack_rgbx_kernel).
+__global__ void pack_rgbx_wide_kernel(const std::uint8_t* __restrict__ rgb, uint4* __restrict__ out, long long quads,
+                                      std::uint32_t alpha) {
+    const std::uint32_t a = alpha << 24;
+    for (long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < quads;
+         q += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const std::uint32_t* src = reinterpret_cast<const std::uint32_t*>(rgb + 12 * q);
+        const std::uint32_t w0 = __ldg(src), w1 = __ldg(src + 1), w2 = __ldg(src + 2);
+        // Bytes r0 g0 b0 r1 | g1 b1 r2 g2 | b2 r3 g3 b3.
+        uint4 o;
+        o.x = (w0 & 0xffffffu) | a;
+        o.y = (w0 >> 24) | ((w1 & 0xffffu) << 8) | a;
+        o.z = (w1 >> 16) | ((w2 & 0xffu) << 16) | a;
+        o.w = (w2 >> 8) | a;
+        out[q] = o;
+    }
+}
+
 __global__ void pack_yuv_kernel(const std::uint8_t* __restrict__ rgb, std::uint8_t* __restrict__ out, int width,
                                 int height, int interleaved) {
     const int cw = (width + 1) / 2, ch = (height + 1) / 2;
@@ -161,8 +181,20 @@ cudaError_t launch_pack_frame(const std::uint8_t* rgb, int width, int height, in
     if (format == 0) return cudaMemcpyAsync(out, rgb, pixels * 3, cudaMemcpyDeviceToDevice, stream);
     const unsigned blocks = static_cast<unsigned>(sms) * 8;
     if (format == 1 || format == 2) {
-        pack_rgbx_kernel<<<blocks, 256, 0, stream>>>(rgb, reinterpret_cast<std::uint32_t*>(out), pixels,
-                                                     format == 2 ? 255u : 0u);
+        const std::uint32_t alpha = format == 2 ? 255u : 0u;
+        if ((reinterpret_cast<std::uintptr_t>(rgb) & 3) == 0 && (reinterpret_cast<std::uintptr_t>(out) & 15) == 0
+            && pixels >= 4) {
+            const long long quads = pixels / 4;
+            const unsigned wide = static_cast<unsigned>((quads + 255) / 256 < blocks ? (quads + 255) / 256 : blocks);
+            pack_rgbx_wide_kernel<<<wide, 256, 0, stream>>>(rgb, reinterpret_cast<uint4*>(out), quads, alpha);
+            const long long done = quads * 4;
+            if (done < pixels) {
+                pack_rgbx_kernel<<<1, 32, 0, stream>>>(rgb + 3 * done, reinterpret_cast<std::uint32_t*>(out) + done,
+                                                       pixels - done, alpha);
+            }
+        } else {
+            pack_rgbx_kernel<<<blocks, 256, 0, stream>>>(rgb, reinterpret_cast<std::uint32_t*>(out), pixels, alpha);
+        }
     } else if (width % 4 == 0 && height % 2 == 0 && (reinterpret_cast<std::uintptr_t>(rgb) & 3) == 0
                && (reinterpret_cast<std::uintptr_t>(out) & 3) == 0) {
         const long long units = static_cast<long long>(width / 4) * (height / 2);
