@@ -373,13 +373,23 @@ __global__ void kfp_plane_bounds_kernel(const float2* __restrict__ samples, cons
 // dither_y); `lut` is the palette in global memory (3 KB at the usual 1024
 // entries: it stays in L1, which served it faster than a per-block copy into
 // shared memory).
-template <bool Planes>
+template <bool Planes, bool Kalles = false>
 __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const KfpDevice& k,
                                           const unsigned char* lut, const double* __restrict__ mc_period,
                                           const int* __restrict__ mc_type, const KfpPlanesLaunch& pl,
                                           const float2* __restrict__ psamples, const unsigned char* __restrict__ pflags,
                                           int x, int y, int dither_x, int dither_y, unsigned char* out) {
     const long long index = static_cast<long long>(y) * k.width + x;
+    // The Kalles default family (ColorMethod 7, Differences 3, smooth
+    // palette, no flat, inverse or multi-colour transfer) is a compile-time
+    // variant: its option switches and dead branches fold away.
+    const int color_method = Kalles ? 7 : k.color_method;
+    const int differences = Kalles ? 3 : k.differences;
+    const int smooth = Kalles ? 1 : k.smooth;
+    const int flat = Kalles ? 0 : k.flat;
+    const int inverse_transition = Kalles ? 0 : k.inverse_transition;
+    const int multi_color = Kalles ? 0 : k.multi_color;
+    const int needs_difference = Kalles ? 1 : k.needs_difference;
     // Plane samples (when the planes carry iterations) are double-float
     // values; the stencil then works on their differences from the centre,
     // so `centre` is 0 and each neighbour is its difference.
@@ -426,7 +436,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         centre = sample(field, k, x, y);
         centre_value = df_add(Df{centre, 0.0f}, Df{k.shift_hi, k.shift_lo});
     }
-    const Df colour_iter_df = k.flat ? df_floor(centre_value) : centre_value;
+    const Df colour_iter_df = flat ? df_floor(centre_value) : centre_value;
     const float colour_iter = df_value(colour_iter_df);
     auto plane_difference_df = [&](int dx, int dy) -> Df {
         const int sx = x + dx, sy = y + dy;
@@ -449,11 +459,11 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         return reflected(field, k, x, y, dx, dy, centre);
     };
     float l = centre, r = centre, u = centre, d = centre, tl = centre, tr = centre, bl = centre, br = centre;
-    if (k.needs_difference || k.needs_slopes || texture) {
+    if (needs_difference || k.needs_slopes || texture) {
         l = neighbour(-1, 0);
         u = neighbour(0, -1);
-        if (k.needs_difference) {
-            switch (k.differences) {
+        if (needs_difference) {
+            switch (differences) {
                 case 0:
                     tl = neighbour(-1, -1);
                     bl = neighbour(-1, 1);
@@ -486,7 +496,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     if constexpr (Planes) {
         // Differences 7 with DE planes: Kalles' float reciprocal norm of the
         // analytic derivative (renderer.cpp:6942-6962).
-        if ((k.needs_difference || k.needs_slopes) && pl.analytic) {
+        if ((needs_difference || k.needs_slopes) && pl.analytic) {
             analytic = true;
             const double ex = pl.de_x[index], ey = pl.de_y[index];
             const float de_x = static_cast<float>(isfinite(ex) ? ex : 0.0);
@@ -499,13 +509,13 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
             }
         }
     }
-    if (!analytic && k.needs_difference) gradient = difference_magnitude(k.differences, centre, l, r, u, d, tl, tr, bl, br);
+    if (!analytic && needs_difference) gradient = difference_magnitude(differences, centre, l, r, u, d, tl, tr, bl, br);
     float distance = isnan(gradient) ? 0.0f : FGB_DIV(gradient * static_cast<float>(k.spatial_width), 640.0f);
     if (distance < 0.0f) distance = 0.0f;
     Df transfer_df = colour_iter_df;  // kept in double-float for methods 0, 4 and 6's iteration branch
-    bool exact_transfer = k.color_method == 0 || k.color_method == 4;
+    bool exact_transfer = color_method == 0 || color_method == 4;
     float transfer = colour_iter;
-    switch (k.color_method) {
+    switch (color_method) {
         case 1: transfer = sqrtf(fmaxf(0.0f, colour_iter)); break;
         case 2: transfer = powf(fmaxf(0.0f, colour_iter), 1.0f / 3.0f); break;
         case 3: transfer = logf(fmaxf(1.0f, colour_iter)); break;
@@ -535,7 +545,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     }
     Df palette_value = exact_transfer ? transfer_df : Df{transfer, 0.0f};
     if (isnan(palette_value.hi) || isnan(palette_value.lo) || df_negative(palette_value)) palette_value = Df{0.0f, 0.0f};
-    if ((k.color_method == 5 || k.color_method == 7 || k.color_method == 8) && palette_value.hi > 1024.0f) {
+    if ((color_method == 5 || color_method == 7 || color_method == 8) && palette_value.hi > 1024.0f) {
         palette_value = Df{1024.0f, 0.0f};
     }
     if (k.has_div) palette_value = df_mul(palette_value, Df{k.inv_div_hi, k.inv_div_lo});
@@ -569,9 +579,9 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         const Df lower_position = df_floor(position);
         int lower = static_cast<int>(lower_position.hi) + static_cast<int>(lower_position.lo);
         lower = lower < 0 ? 0 : (lower > k.lut_size - 1 ? k.lut_size - 1 : lower);
-        if (k.smooth) {
+        if (smooth) {
             float f = df_value(df_add(position, df_neg(lower_position)));
-            if (k.inverse_transition) f = 1.0f - f;
+            if (inverse_transition) f = 1.0f - f;
             const int upper = lower + 1 < k.lut_size ? lower + 1 : 0;  // (lower + 1) mod size, lower in [0, size)
             const float g = 1.0f - f;
             o_r = FGB_DIV(static_cast<float>(lut[lower * 3]) * g + static_cast<float>(lut[upper * 3]) * f, 255.0f);
@@ -585,8 +595,8 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
             o_b = FGB_DIV(static_cast<float>(lut[lower * 3 + 2]), 255.0f);
         }
     };
-    if (k.multi_color) {
-        const double wave_input = static_cast<double>(df_value(k.smooth ? base : df_floor(base)));
+    if (multi_color) {
+        const double wave_input = static_cast<double>(df_value(smooth ? base : df_floor(base)));
         float hs = 0.0f, ss = 0.0f, vs = 0.0f;
         int hc = 0, sc = 0, vc = 0;
         for (int i = 0; i < k.multi_count; ++i) {
@@ -681,7 +691,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     out[2] = dither_byte(blue, dither_x, dither_y, 2);
 }
 
-template <bool Planes>
+template <bool Planes, bool Kalles>
 __global__ void __launch_bounds__(256, 6) kfp_kernel(const float* __restrict__ field, unsigned char* __restrict__ rgb,
                                                   const KfpDevice k, const unsigned char* __restrict__ lut_global,
                                                   const double* __restrict__ mc_period, const int* __restrict__ mc_type,
@@ -690,7 +700,7 @@ __global__ void __launch_bounds__(256, 6) kfp_kernel(const float* __restrict__ f
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= k.width || y >= k.height) return;
-    kfp_pixel<Planes>(field, k, lut_global, mc_period, mc_type, pl, psamples, pflags, x, y, x, y,
+    kfp_pixel<Planes, Kalles>(field, k, lut_global, mc_period, mc_type, pl, psamples, pflags, x, y, x, y,
                       rgb + 3 * (static_cast<long long>(y) * k.width + x));
 }
 
@@ -929,10 +939,17 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
     const dim3 block(32, 8);
     const dim3 grid((launch.width + 31) / 32, (launch.height + 7) / 8);
     if (planes != nullptr) {
-        kfp_kernel<true><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, *planes,
+        kfp_kernel<true, false><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, *planes,
                                                           static_cast<const float2*>(samples), flags);
     } else {
-        kfp_kernel<false><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
+        const bool kalles = k.color_method == 7 && k.differences == 3 && k.smooth && !k.flat && !k.inverse_transition
+            && !k.multi_color;
+        if (kalles) {
+            kfp_kernel<false, true><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type,
+                                                                KfpPlanesLaunch{}, nullptr, nullptr);
+            return cudaGetLastError();
+        }
+        kfp_kernel<false, false><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type, KfpPlanesLaunch{},
                                                            nullptr, nullptr);
     }
     return cudaGetLastError();
