@@ -599,10 +599,10 @@ __device__ __forceinline__ void crop_aurora_pixel(bool& undecided, const AtlasLa
 
 // One output pixel of any mode: a float (field_out modes) into *value or
 // three bytes into rgb.
-template <bool Exact>
+template <bool Exact, int Mode>
 __device__ __forceinline__ void atlas_pixel(const AtlasLaunch& a, const SourceView& parent, const SourceView& child,
                                             int x, int y, bool& undecided, float* value, std::uint8_t* rgb) {
-    switch (a.mode) {
+    switch (Mode) {
         case kAtlasKfpSurface: *value = surface_pixel<Exact>(undecided, a, parent, child, x, y); break;
         case kAtlasKfpPlanes: *value = planes_surface_pixel<Exact>(undecided, a, parent, child, x, y); break;
         case kAtlasCropField: *value = crop_pixel(a, x, y); break;
@@ -632,7 +632,9 @@ __device__ __forceinline__ void queue_exact(const AtlasLaunch& a, bool undecided
 // 12 bytes (RGB, three aligned words); everything else stores per pixel.  A
 // pixel whose sample could not be decided in double-float is written with a
 // placeholder and queued for atlas_exact_kernel, which rewrites it.
-__global__ void __launch_bounds__(256, 8) atlas_kernel(const AtlasLaunch a, unsigned quads_per_row,
+template <int Mode>
+__global__ void __launch_bounds__(256, (Mode == kAtlasRgb || Mode == kAtlasCropAurora) ? 6 : 8)
+    atlas_kernel(const AtlasLaunch a, unsigned quads_per_row,
                                                     unsigned total_quads) {
     const bool vector_rows = (a.out_width & 3) == 0;
     const SourceView parent = parent_view(a), child = child_view(a);
@@ -646,7 +648,7 @@ __global__ void __launch_bounds__(256, 8) atlas_kernel(const AtlasLaunch a, unsi
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             bool undecided = false;
-            if (k < n) atlas_pixel<false>(a, parent, child, x0 + k, y, undecided, v + k, out + 3 * k);
+            if (k < n) atlas_pixel<false, Mode>(a, parent, child, x0 + k, y, undecided, v + k, out + 3 * k);
             queue_exact(a, undecided, static_cast<unsigned>(row + x0 + k));
         }
         if (a.field_out) {
@@ -675,6 +677,7 @@ __global__ void __launch_bounds__(256, 8) atlas_kernel(const AtlasLaunch a, unsi
 // reference's FP64 form.  Dense warps, so the FP64 pipe runs with all lanes
 // active; the list is usually a few hundred pixels, up to a few percent of a
 // frame whose axes fall on exact halves (2:1 resampling).
+template <int Mode>
 __global__ void __launch_bounds__(256) atlas_exact_kernel(const AtlasLaunch a) {
     const SourceView parent = parent_view(a), child = child_view(a);
     const unsigned count = *a.exact_count;
@@ -685,7 +688,7 @@ __global__ void __launch_bounds__(256) atlas_exact_kernel(const AtlasLaunch a) {
         bool undecided = false;
         float value = 0.0f;
         std::uint8_t rgb[3];
-        atlas_pixel<true>(a, parent, child, x, y, undecided, &value, rgb);
+        atlas_pixel<true, Mode>(a, parent, child, x, y, undecided, &value, rgb);
         if (a.field_out) {
             a.field_out[index] = value;
         } else {
@@ -934,11 +937,28 @@ cudaError_t launch_atlas(AtlasLaunch& a, void* tables, cudaStream_t stream) {
     // (the seam band's second sample, the child rectangle) balance
     // themselves.
     long long blocks = (static_cast<long long>(total) + 255) / 256;
-    atlas_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, stream>>>(a, quads_per_row, total);
-    status = cudaGetLastError();
-    if (status != cudaSuccess) return status;
-    atlas_exact_kernel<<<static_cast<unsigned>(sms) * 2, 256, 0, stream>>>(a);
-    return cudaGetLastError();
+    const unsigned grid = static_cast<unsigned>(blocks < 1 ? 1 : blocks), exact_grid = static_cast<unsigned>(sms) * 2;
+    // One instantiation per mode: each gets its own register allocation and
+    // no per-pixel mode switch.
+    switch (a.mode) {
+#define FGB_ATLAS_MODE(M)                                                                    \
+        case M:                                                                              \
+            atlas_kernel<M><<<grid, 256, 0, stream>>>(a, quads_per_row, total);              \
+            status = cudaGetLastError();                                                     \
+            if (status != cudaSuccess) return status;                                        \
+            atlas_exact_kernel<M><<<exact_grid, 256, 0, stream>>>(a);                         \
+            return cudaGetLastError();
+        FGB_ATLAS_MODE(kAtlasField)
+        FGB_ATLAS_MODE(kAtlasAurora)
+        FGB_ATLAS_MODE(kAtlasKfpSurface)
+        FGB_ATLAS_MODE(kAtlasCropField)
+        FGB_ATLAS_MODE(kAtlasRgb)
+        FGB_ATLAS_MODE(kAtlasCropAurora)
+        FGB_ATLAS_MODE(kAtlasKfpPlanes)
+#undef FGB_ATLAS_MODE
+        default:
+            return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace fgb
