@@ -381,8 +381,9 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
                                           int x, int y, int dither_x, int dither_y, unsigned char* out) {
     const long long index = static_cast<long long>(y) * k.width + x;
     // The Kalles default family (ColorMethod 7, Differences 3, smooth
-    // palette, no flat, inverse or multi-colour transfer) is a compile-time
-    // variant: its option switches and dead branches fold away.
+    // palette, slopes, a power-of-two palette, no flat, inverse or
+    // multi-colour transfer) is a compile-time variant: its option switches
+    // and dead branches fold away.
     const int color_method = Kalles ? 7 : k.color_method;
     const int differences = Kalles ? 3 : k.differences;
     const int smooth = Kalles ? 1 : k.smooth;
@@ -390,6 +391,8 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     const int inverse_transition = Kalles ? 0 : k.inverse_transition;
     const int multi_color = Kalles ? 0 : k.multi_color;
     const int needs_difference = Kalles ? 1 : k.needs_difference;
+    const int needs_slopes = Kalles ? 1 : k.needs_slopes;
+    const bool lut_pow2 = Kalles || k.lut_shift >= 0;
     // Plane samples (when the planes carry iterations) are double-float
     // values; the stencil then works on their differences from the centre,
     // so `centre` is 0 and each neighbour is its difference.
@@ -459,7 +462,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
         return reflected(field, k, x, y, dx, dy, centre);
     };
     float l = centre, r = centre, u = centre, d = centre, tl = centre, tr = centre, bl = centre, br = centre;
-    if (needs_difference || k.needs_slopes || texture) {
+    if (needs_difference || needs_slopes || texture) {
         l = neighbour(-1, 0);
         u = neighbour(0, -1);
         if (needs_difference) {
@@ -485,7 +488,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
                     break;
             }
         }
-        if (k.needs_slopes || texture) {
+        if (needs_slopes || texture) {
             if (x == 0) r = neighbour(1, 0);
             if (y == 0) d = neighbour(0, 1);
         }
@@ -496,7 +499,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     if constexpr (Planes) {
         // Differences 7 with DE planes: Kalles' float reciprocal norm of the
         // analytic derivative (renderer.cpp:6942-6962).
-        if ((needs_difference || k.needs_slopes) && pl.analytic) {
+        if ((needs_difference || needs_slopes) && pl.analytic) {
             analytic = true;
             const double ex = pl.de_x[index], ey = pl.de_y[index];
             const float de_x = static_cast<float>(isfinite(ex) ? ex : 0.0);
@@ -563,7 +566,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
     float red, green, blue;
     auto palette_rgb = [&](Df input, float& o_r, float& o_g, float& o_b) {
         Df position;
-        if (k.lut_shift >= 0) {
+        if (lut_pow2) {
             // input - size * floor(input / size): power-of-two scalings are
             // exact, so this is the cyclic position in [0, size).
             const float size = static_cast<float>(k.lut_size);
@@ -670,7 +673,7 @@ __device__ __forceinline__ void kfp_pixel(const float* __restrict__ field, const
                                       + merge * static_cast<double>(t[2]) / 255.0);
         }
     }
-    if (k.needs_slopes) {
+    if (needs_slopes) {
         const float horizontal = analytic ? analytic_x : (x > 0 ? l - centre : centre - r);
         const float vertical = analytic ? analytic_y : (y == 0 ? centre - d : u - centre);
         const float projected = FGB_DIV((horizontal * k.slope_cos + vertical * k.slope_sin) * k.slope_power
@@ -943,7 +946,7 @@ cudaError_t launch_kfp(const float* field, std::uint8_t* rgb, const KfpLaunch& l
                                                           static_cast<const float2*>(samples), flags);
     } else {
         const bool kalles = k.color_method == 7 && k.differences == 3 && k.smooth && !k.flat && !k.inverse_transition
-            && !k.multi_color;
+            && !k.multi_color && k.needs_slopes && k.lut_shift >= 0;
         if (kalles) {
             kfp_kernel<false, true><<<grid, block, 0, stream>>>(field, rgb, k, lut, mc_period, mc_type,
                                                                 KfpPlanesLaunch{}, nullptr, nullptr);
