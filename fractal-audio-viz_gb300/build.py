@@ -27,7 +27,7 @@ LIBRARY = os.path.join(BUILD, "libfractal_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units compiled with contraction allowed (FP32 floatexp, colour).
-FMA_UNITS = {"render_fe.cu", "colour_kfp.cu", "mlp.cu", "queue.cu"}
+FMA_UNITS = {"render_fe.cu", "colour_kfp.cu", "mlp.cu"}
 
 
 def _cuda_home() -> str:

@@ -7,7 +7,7 @@ claims the heaviest tiles first (FRACTAL_GB300_BATCH_LEARNED).  It orders
 work only: every pixel is the same as with the static order.
 
 Training data are fields the renderer itself produces: seeded Misiurewicz
-centres (costnet_centres.json, made by make_costnet_centres.py), each
+centres (costnet_centres.json, made by tests/golden/make_costnet_centres.py), each
 rendered as one 1920x1080 atlas keyframe at a seeded level of the FHD ladder
 (zoom 8^level, cap 2000 + 3000 per decade) through the tile queue in static
 order with the probe on.  Labels are the measured per-tile costs (SM cycles)

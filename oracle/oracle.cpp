@@ -58,6 +58,30 @@ struct Oops : std::runtime_error {
 };
 
 // ------------------------------------------------------------ numbers
+// frexp / ldexp with the library's exact results, decided on the bit
+// pattern for normal doubles (a multiply by an exact power of two rounds
+// once, as ldexp does); zeros, subnormals, infinities, NaNs and extreme
+// scales go to the library.  They keep the hot loops free of libm calls.
+inline double frexp2(double v, int* e) {
+    std::uint64_t b;
+    std::memcpy(&b, &v, sizeof b);
+    const int biased = static_cast<int>((b >> 52) & 0x7ff);
+    if (biased == 0 || biased == 0x7ff) return std::frexp(v, e);
+    *e = biased - 1022;
+    b = (b & ~(0x7ffULL << 52)) | (1022ULL << 52);
+    double r;
+    std::memcpy(&r, &b, sizeof r);
+    return r;
+}
+
+inline double ldexp2(double v, int k) {
+    if (k < -1022 || k > 1023) return std::ldexp(v, k);
+    const std::uint64_t b = static_cast<std::uint64_t>(k + 1023) << 52;
+    double scale;
+    std::memcpy(&scale, &b, sizeof scale);
+    return v * scale;
+}
+
 int clamp_exp(long long v) {
     return v > INT_MAX ? INT_MAX : (v < INT_MIN ? INT_MIN : static_cast<int>(v));
 }
@@ -70,7 +94,7 @@ struct FE {  // mantissa in [0.5,1) times 2^e
 FE fe(double value, int exponent) {
     if (value == 0.0 || std::isnan(value)) return {value, 0};
     int s = 0;
-    double n = std::frexp(value, &s);
+    double n = frexp2(value, &s);
     return {n, clamp_exp(static_cast<long long>(exponent) + s)};
 }
 
@@ -86,13 +110,13 @@ FE add(const FE& a, const FE& b) {
     const FE& small = b.e > a.e ? a : b;
     long long gap = static_cast<long long>(big.e) - small.e;
     if (gap > 60) return big;
-    double m = big.m + std::ldexp(small.m, -static_cast<int>(gap));
+    double m = big.m + ldexp2(small.m, -static_cast<int>(gap));
     if (m == 0.0 || !std::isfinite(m)) return fe(m, big.e);
     double am = std::fabs(m);
     if (am >= 1.0) return {m * 0.5, clamp_exp(static_cast<long long>(big.e) + 1)};
     if (am >= 0.5) return {m, big.e};
     int s = 0;
-    double n = std::frexp(m, &s);
+    double n = frexp2(m, &s);
     return {n, clamp_exp(static_cast<long long>(big.e) + s)};
 }
 
@@ -179,9 +203,9 @@ void fix(SC& v) {
     }
     int s = 0;
     if (big >= 2.0 || big < 0.25) {
-        std::frexp(big, &s);
-        v.x = std::ldexp(v.x, -s);
-        v.y = std::ldexp(v.y, -s);
+        frexp2(big, &s);
+        v.x = ldexp2(v.x, -s);
+        v.y = ldexp2(v.y, -s);
         v.e = clamp_exp(static_cast<long long>(v.e) + s);
     } else if (big >= 1.0) {
         v.x *= 0.5;
@@ -198,8 +222,8 @@ SC from_fc(const FE& r, const FE& i) {
     if (r.m == 0.0 && i.m == 0.0) return {};
     int top = std::max(r.e, i.e);
     long long dr = static_cast<long long>(r.e) - top, di = static_cast<long long>(i.e) - top;
-    SC v{dr < -1074 ? 0.0 : std::ldexp(r.m, static_cast<int>(dr)),
-         di < -1074 ? 0.0 : std::ldexp(i.m, static_cast<int>(di)), top};
+    SC v{dr < -1074 ? 0.0 : ldexp2(r.m, static_cast<int>(dr)),
+         di < -1074 ? 0.0 : ldexp2(i.m, static_cast<int>(di)), top};
     fix(v);
     return v;
 }
@@ -214,7 +238,7 @@ SC sadd(const SC& a, const SC& b) {
     const SC& small = b.e > a.e ? a : b;
     long long gap = static_cast<long long>(big.e) - small.e;
     if (gap > 60) return big;
-    SC v{big.x + std::ldexp(small.x, -static_cast<int>(gap)), big.y + std::ldexp(small.y, -static_cast<int>(gap)),
+    SC v{big.x + ldexp2(small.x, -static_cast<int>(gap)), big.y + ldexp2(small.y, -static_cast<int>(gap)),
          big.e};
     fix(v);
     return v;
@@ -272,8 +296,8 @@ bool escaped_norm(const NM& n, int mode) {
     return ncmp(n, NM{t.m, t.e}) > 0;
 }
 
-double sx(const SC& a) { return std::ldexp(a.x, a.e); }
-double sy(const SC& a) { return std::ldexp(a.y, a.e); }
+double sx(const SC& a) { return ldexp2(a.x, a.e); }
+double sy(const SC& a) { return ldexp2(a.y, a.e); }
 
 FC to_fc(const SC& a) { return {fe(a.x, a.e), fe(a.y, a.e)}; }
 
@@ -287,14 +311,14 @@ NM norm_with_margin(const FE& margin, int mode) {
 double norm_double(const NM& n) {
     if (n.m == 0.0) return 0.0;
     if (!std::isfinite(n.m)) return std::numeric_limits<double>::max();
-    double v = std::ldexp(n.m, n.e);
+    double v = ldexp2(n.m, n.e);
     return std::isfinite(v) ? std::max(0.0, v) : std::numeric_limits<double>::max();
 }
 
 NM norm_of_double(double v) {
     if (!(v > 0.0) || !std::isfinite(v)) return v > 0.0 ? NM{std::numeric_limits<double>::max(), 0} : NM{};
     int e = 0;
-    double m = std::frexp(v, &e);
+    double m = frexp2(v, &e);
     return {m, e};
 }
 
@@ -445,8 +469,8 @@ void orbit(Reference& R, const char* xs, const char* ys, const char* zs, int max
     R.zi.resize(n);
     for (std::size_t i = 0; i < n; ++i) {
         R.z[i] = from_fc(R.builder[i].r, R.builder[i].i);
-        R.zr[i] = std::ldexp(R.z[i].x, R.z[i].e);
-        R.zi[i] = std::ldexp(R.z[i].y, R.z[i].e);
+        R.zr[i] = ldexp2(R.z[i].x, R.z[i].e);
+        R.zi[i] = ldexp2(R.z[i].y, R.z[i].e);
     }
 }
 
@@ -473,7 +497,7 @@ void image_series(Reference& R, const std::vector<FC>& orb) {
                            {mul(in, 0.63), in}, {mul(in, 0.63), neg(in)}};
     std::vector<FC> k(static_cast<std::size_t>(order + 1)), nk(k.size()), keep;
     FC exact[12] = {};
-    const FE two = fe(2.0, 0), tol = fe(std::ldexp(1.0, -38), 0), floor2 = sq(pr);
+    const FE two = fe(2.0, 0), tol = fe(ldexp2(1.0, -38), 0), floor2 = sq(pr);
     int best = 1;
     for (int it = 0; it < last; ++it) {
         const FC& Z = orb[static_cast<std::size_t>(it)];
@@ -555,7 +579,7 @@ BCubic compose(const BCubic& y, const BCubic& x, const FE& in) {
 }
 
 std::vector<std::vector<Linear>> linear_levels(const Reference& R, int count, const FE& in) {
-    const FE tol = fe(std::ldexp(1.0, -38), 0), two = fe(2.0, 0);
+    const FE tol = fe(ldexp2(1.0, -38), 0), two = fe(2.0, 0);
     std::vector<std::vector<BLinear>> lv(1, std::vector<BLinear>(static_cast<std::size_t>(count)));
     for (int s = 1; s <= count; ++s) {
         const FC& Z = R.builder[static_cast<std::size_t>(s)];
@@ -597,7 +621,7 @@ void tables(Reference& R) {
     R.linear.clear();
     R.deep.clear();
     if (count == 0) return;
-    const FE tol = fe(std::ldexp(1.0, -38), 0), two = fe(2.0, 0);
+    const FE tol = fe(ldexp2(1.0, -38), 0), two = fe(2.0, 0);
     std::vector<std::vector<BCubic>> lv(1, std::vector<BCubic>(static_cast<std::size_t>(count)));
     for (int s = 1; s <= count; ++s) {
         const FC& Z = R.builder[static_cast<std::size_t>(s)];
@@ -640,7 +664,7 @@ void tables(Reference& R) {
 FE retarget(const FE& xr2, const FE& yr2, const SC& xa, const SC& xb, const FE& in) {
     NM na = norm(xa), nb = norm(xb);
     FE r = composed_radius(xr2, yr2, root(FE{na.m, na.e}), root(FE{nb.m, nb.e}), in);
-    return sq(mul(r, 1.0 - std::ldexp(1.0, -40)));
+    return sq(mul(r, 1.0 - ldexp2(1.0, -40)));
 }
 
 // ------------------------------------------------------------ deep render
@@ -804,9 +828,9 @@ struct Pixel {
 
     // Plain-double tail (renderer.cpp:12451-12669); true = pathological.
     bool tail(int& it, int& ref, SC delta, const NM& start_norm, bool& unresolved) {
-        double cr = sx(dc), ci = std::ldexp(dc.y, dc.e);
+        double cr = sx(dc), ci = ldexp2(dc.y, dc.e);
         double esc = static_cast<double>(o.escape_radius_mode == 1 ? 1.0e8L : 4.0L), safe = esc + 1.0e-7;
-        double dr = sx(delta), di = std::ldexp(delta.y, delta.e);
+        double dr = sx(delta), di = ldexp2(delta.y, delta.e);
         out = encode(max_iter, o.output_bias);
         double tr0 = 0, ti0 = 0;
         int power = 1, length = 0, steps = 0, iters = 0, rebases = 0;

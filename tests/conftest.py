@@ -19,7 +19,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PACKAGE_DIR = os.path.join(ROOT, "fractal-audio-viz_gb300")
 FIXTURES = os.path.join(ROOT, "tests", "golden", "fixtures")
-REFERENCE_SOURCES = "/root/reference"  # present only where the fixtures are made
+# The reference checkout (read-only; present only where the fixtures are made).
+REFERENCE_SOURCES = os.environ.get("REFERENCE_DIR", "/root/reference")
 
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)

@@ -4,10 +4,10 @@
 half-plane), found by the same seeded Newton method as the parity centres
 (tests/golden/make_centres.py: double-precision Newton, polished with mpmath
 at 400 bits, exact preperiod/period checked) and written as 120-digit
-decimals to costnet_centres.json beside this file.  Needs mpmath; the GPU
-host only reads the JSON.
+decimals to fractal-audio-viz_gb300/costnet_centres.json, which the package
+reads.  Needs mpmath; the GPU host only reads the JSON.
 
-Run:  python fractal-audio-viz_gb300/make_costnet_centres.py
+Run:  python tests/golden/make_costnet_centres.py
 """
 
 from __future__ import annotations
@@ -17,7 +17,8 @@ import json
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-MAKER = os.path.join(os.path.dirname(HERE), "tests", "golden", "make_centres.py")
+MAKER = os.path.join(HERE, "make_centres.py")
+OUTPUT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "fractal-audio-viz_gb300", "costnet_centres.json")
 
 
 def main(count: int = 200, first_seed: int = 50_000) -> None:
@@ -25,7 +26,7 @@ def main(count: int = 200, first_seed: int = 50_000) -> None:
     maker = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(maker)
     centres = [maker.misiurewicz_centre(first_seed + i, 400, 120) for i in range(count)]
-    with open(os.path.join(HERE, "costnet_centres.json"), "w", encoding="ascii") as handle:
+    with open(OUTPUT, "w", encoding="ascii") as handle:
         json.dump({"method": "seeded Misiurewicz Newton, 400 bits, 120 digits", "centres": centres}, handle,
                   indent=1)
 

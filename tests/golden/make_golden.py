@@ -29,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 FIXTURES = os.path.join(HERE, "fixtures")
 REFERENCE_LIBRARY = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
-REFERENCE_SOURCES = "/root/reference"
+REFERENCE_SOURCES = os.environ.get("REFERENCE_DIR", "/root/reference")
 
 
 def _package_kfp():
