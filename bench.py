@@ -1,24 +1,41 @@
-"""Benchmark: Gpixel-iter/s of the FHD atlas keyframe stack on one GB300.
+"""Benchmark: Gpixel-iter/s of the 1e100 FHD atlas on one GB300.
 
-Workload (one step): the 55 atlas keyframes of a 1920x1080 field with
-keyframe factor 8 from zoom 1e0 to ~1e48.8 (levels i = 0..54, log10 zoom
-i*log10(8)), iteration cap 2000 + 3000 per decade up to 200k, centred on a
-seeded Misiurewicz point (tests/golden/centres.json "fhd_stack_e50", 1200-bit
-Newton, 360 digits).  Levels below 1e12 take the direct path, deeper ones
-render from the shared MPFR reference and its BLA tiers, as the reference
-pipeline does.  Work unit: a pixel-iteration, i.e. the sum of uint32
-iteration counts (escape index, or the cap for interior pixels); iterations
-skipped by the image series or BLA count as done (the reference's
-logical_iterations + series_jumps).
+Workload (one step, `fhd_atlas_e100`): every keyframe of a 1920x1080 atlas
+with keyframe factor 8 from zoom 1e0 to 1e100 -- the reference's
+_atlas_geometry([0, 100], 8) ladder (visualizer.py:7628-7661): levels
+i = 0..111, log10 zoom i*log10(8) -- with the reference's per-tile caps
+max_iterations(min(100, (i+1)*log10(8)), 2000, 3000, 200000)
+(visualizer.py:6958-6979, 11567-11580), centred on a seeded Misiurewicz
+point (tests/golden/centres.json "fhd_stack_e50", 1200-bit Newton, 360
+digits).  Levels below 1e12 are direct-path levels, deeper ones render from
+the shared MPFR reference and its BLA tiers, as the reference pipeline does.
+configs[1]'s 55-keyframe stack (levels 0..54, to 1e48.8, caps up to 151k,
+`fhd_keyframe_stack`) is measured beside it.  Work unit: a pixel-iteration,
+i.e. the sum of uint32 iteration counts (escape index, or the cap for
+interior pixels); iterations skipped by the image series or BLA count as
+done (the reference's logical_iterations + series_jumps).
+
+Forms
+  chosen   floatexp form: deep levels and the direct-path levels between 1e1
+           and 1e10 by FP32 perturbation in one persistent queue; the levels
+           that keep the FP64 direct iteration (the whole-set view, 1e10 and
+           deeper) in the FP64 lane-refill queue on a second stream
+  plain    the FP64 form, bit-identical to the reference
 
 Arms
   ours (default)      the GB300 library; `value` is device throughput with
                       the tables resident in HBM, `e2e` goes through the
-                      renderer.h ABI into host memory (field copied back).
+                      renderer.h ABI into host memory (fields copied back).
   --impl reference    the reference's CPU implementation of the path on the
                       host cores: the reference build in oracle/_ref when it
                       exists, else the oracle port (a restatement pinned
-                      bit-exact to it), on a bounded sample of the workload.
+                      bit-exact to it).  The K timed steps together render
+                      the whole workload once at full size (keyframes dealt
+                      round-robin over the steps).
+
+--gpus N without a launcher starts N replica processes (one per GPU, NCCL
+only for the barrier and the max-over-ranks time); under torchrun each
+process is one rank.
 """
 
 from __future__ import annotations
@@ -28,6 +45,7 @@ import ctypes
 import json
 import math
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -43,17 +61,25 @@ import __graft_entry__  # noqa: E402
 
 WIDTH, HEIGHT = 1920, 1080
 FACTOR = 8.0
-LEVELS = 55
-SAMPLE_DIVISOR = 4  # CPU sample: every keyframe at 480x270 (1/16 of the pixels)
+SAMPLE_DIVISOR = 4  # cpu_baseline sample: every keyframe at 480x270 (1/16 of the pixels)
 E2E_THREADS = 4     # host threads calling the renderer.h ABI in the end-to-end leg
 METRIC = "Gpixel-iter/s on 1e100 FHD atlas, chosen vs plain GPU at ≤1e-4 pixel mismatch"
+WORKLOADS = {
+    # name: (max log10 zoom of the camera path, keyframe count)
+    "fhd_atlas_e100": (100.0, 112),
+    "fhd_keyframe_stack": (50.0, 55),
+}
+HEADLINE = "fhd_atlas_e100"
 
 
-def workload_levels():
+def workload_levels(name: str = "fhd_keyframe_stack"):
+    """(level, log10 zoom, cap) of every keyframe of a workload, and the
+    ladder step log10(8)."""
+    maximum, count = WORKLOADS[name]
     step = math.log10(FACTOR)
     levels = []
-    for i in range(LEVELS):
-        cap = min(200_000, max(64, int(2000 + 3000 * max(0.0, min(50.0, (i + 1) * step)))))
+    for i in range(count):
+        cap = min(200_000, max(64, int(2000 + 3000 * max(0.0, min(maximum, (i + 1) * step)))))
         levels.append((i, i * step, cap))
     return levels, step
 
@@ -139,49 +165,83 @@ def max_over_ranks(value: float) -> float:
     return float(t.item())
 
 
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_replicas(argv: list[str], gpus: int) -> int:
+    """Start one bench process per GPU (RANK / LOCAL_RANK / WORLD_SIZE and a
+    127.0.0.1 rendezvous in the environment), as torchrun would; rank 0's
+    line is the job's.  Returns the first non-zero exit code, else 0."""
+    port = _free_port()
+    children = []
+    for rank in range(gpus):
+        env = dict(os.environ, RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE=str(gpus),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        children.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + argv, env=env))
+    codes = [child.wait() for child in children]
+    return next((code for code in codes if code != 0), 0)
+
+
+def cpu_library(native):
+    """The reference build when present (kind "reference"), else the oracle
+    port (kind "port"), built on demand."""
+    ref_path = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
+    if os.path.exists(ref_path):
+        return native.load(ref_path), "reference", ref_path
+    ref_path = os.path.join(ROOT, "oracle", "_ref", "liboracle.so")
+    if not os.path.exists(ref_path):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "port"], check=True, capture_output=True)
+    return native.load(ref_path), "port", ref_path
+
+
+def cpu_render(native, stack, keyframe, width, height, cores) -> int:
+    field, planes = stack.render_host(keyframe, width, height, threads=cores, planes=True)
+    return int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
+               .astype(np.uint64).sum())
+
+
 def run_reference_arm(args) -> int:
+    """The reference's CPU path on all host cores, on the headline workload
+    at full size: the keyframes are dealt round-robin over the K timed steps,
+    so the K steps together render every keyframe once (K below the keyframe
+    count) and value = their pixel-iterations / their time.  Warm-up steps
+    render one keyframe each at 240x135."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     package = __graft_entry__._package()
     native = package.native
     atlas = package.atlas
-    ref_path = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
-    kind = "reference"
-    if not os.path.exists(ref_path):
-        ref_path = os.path.join(ROOT, "oracle", "_ref", "liboracle.so")
-        kind = "port"
-        if not os.path.exists(ref_path):
-            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "port"], check=True,
-                           capture_output=True)
-    library = native.load(ref_path)
+    library, kind, ref_path = cpu_library(native)
     cores = os.cpu_count() or 1
-    levels, step = workload_levels()
+    levels, step = workload_levels(args.workload)
     x, y = centre()
-    w, h = WIDTH // SAMPLE_DIVISOR, HEIGHT // SAMPLE_DIVISOR
     t0 = time.perf_counter()
     stack = atlas.KeyframeStack(library, x, y, levels, step=step)
     setup_s = time.perf_counter() - t0
-
-    def one_step():
-        total = 0
-        for keyframe in stack.keyframes:
-            field, planes = stack.render_host(keyframe, w, h, threads=cores, planes=True)
-            total += int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
-                         .astype(np.uint64).sum())
-        return total
-
-    for _ in range(args.warmup):
-        one_step()
-    t0 = time.perf_counter()
+    keyframes = stack.keyframes
+    steps = max(1, args.steps)
+    # Deal the keyframes costliest-first so the steps carry similar work.
+    deal = sorted(range(len(keyframes)), key=lambda i: -keyframes[i].max_iter)
+    shares = [deal[k::steps] for k in range(steps)] if steps <= len(keyframes) else \
+        [[deal[k % len(keyframes)]] for k in range(steps)]
+    for k in range(args.warmup):
+        cpu_render(native, stack, keyframes[deal[k % len(deal)]], 240, 135, cores)
     work = 0
-    for _ in range(args.steps):
-        work += one_step()
-    elapsed = time.perf_counter() - t0
+    elapsed = 0.0
+    for share in shares:
+        t0 = time.perf_counter()
+        for i in share:
+            work += cpu_render(native, stack, keyframes[i], WIDTH, HEIGHT, cores)
+        elapsed += time.perf_counter() - t0
     stack.close()
     value = work / elapsed / 1e9
-    sample = (f"all {LEVELS} keyframes of the FHD stack at {w}x{h} (1/{SAMPLE_DIVISOR**2} of the pixels), "
-              f"same views and caps")
+    covered = len({i for share in shares for i in share})
+    sample = (f"full size: {covered} of {len(keyframes)} keyframes at {WIDTH}x{HEIGHT} over the {steps} timed steps "
+              f"(keyframes dealt round-robin), {elapsed:.1f} s")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -190,17 +250,18 @@ def run_reference_arm(args) -> int:
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": elapsed / args.steps * 1e3,
+        "ms_per_step": elapsed / steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded Misiurewicz centre)",
-        "config": {"workload": "fhd_keyframe_stack", "keyframes": LEVELS, "width": w, "height": h,
-                   "keyframe_factor": FACTOR, "max_log10_zoom": levels[-1][1], "threads": cores,
-                   "library": os.path.relpath(ref_path, ROOT), "reference_setup_s": setup_s},
-        "cpu_baseline": {"value": value, "unit": "Gpixel-iter/s", "cores": cores, "kind": kind,
-                         "sample": sample},
+        "data": "synthetic (seeded Misiurewicz centre, tests/golden/centres.json)",
+        "config": {"workload": args.workload, "keyframes": len(keyframes), "width": WIDTH, "height": HEIGHT,
+                   "keyframe_factor": FACTOR, "max_log10_zoom": levels[-1][1],
+                   "max_cap": max(c for _, _, c in levels), "threads": cores,
+                   "library": os.path.relpath(ref_path, ROOT), "reference_setup_s": setup_s,
+                   "pixel_iterations": work},
+        "cpu_baseline": {"value": value, "unit": "Gpixel-iter/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -208,16 +269,9 @@ def run_reference_arm(args) -> int:
 
 
 def cpu_baseline_sample(native, atlas, levels, step, x, y) -> dict:
-    """Time the CPU implementation on a bounded sample (rank 0, N=1 only)."""
-    ref_path = os.path.join(ROOT, "oracle", "_ref", "mandelbrot.so")
-    kind = "reference"
-    if not os.path.exists(ref_path):
-        ref_path = os.path.join(ROOT, "oracle", "_ref", "liboracle.so")
-        kind = "port"
-        if not os.path.exists(ref_path):
-            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "port"], check=True,
-                           capture_output=True)
-    library = native.load(ref_path)
+    """Time the CPU implementation on a bounded sample (rank 0, N=1 only):
+    every keyframe of the workload at 480x270."""
+    library, kind, _ = cpu_library(native)
     cores = os.cpu_count() or 1
     w, h = WIDTH // SAMPLE_DIVISOR, HEIGHT // SAMPLE_DIVISOR
     stack = atlas.KeyframeStack(library, x, y, levels, step=step)
@@ -225,14 +279,103 @@ def cpu_baseline_sample(native, atlas, levels, step, x, y) -> dict:
         work = 0
         t0 = time.perf_counter()
         for keyframe in stack.keyframes:
-            field, planes = stack.render_host(keyframe, w, h, threads=cores, planes=True)
-            work += int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
-                        .astype(np.uint64).sum())
+            work += cpu_render(native, stack, keyframe, w, h, cores)
         elapsed = time.perf_counter() - t0
     finally:
         stack.close()
     return {"value": work / elapsed / 1e9, "unit": "Gpixel-iter/s", "cores": cores, "kind": kind,
-            "sample": f"all {LEVELS} keyframes at {w}x{h} (1/{SAMPLE_DIVISOR**2} of the pixels), {elapsed:.1f} s"}
+            "sample": f"all {len(levels)} keyframes at {w}x{h} (1/{SAMPLE_DIVISOR**2} of the pixels), "
+                      f"{elapsed:.1f} s"}
+
+
+class StackBench:
+    """One workload's keyframe stack on the GPU: device outputs, the claim
+    order and the timed batched step."""
+
+    def __init__(self, package, library, name, stream, world):
+        import torch
+
+        self.package, self.library, self.name, self.world = package, library, name, world
+        self.native = package.native
+        self.levels, self.step = workload_levels(name)
+        x, y = centre()
+        t0 = time.perf_counter()
+        self.stack = package.atlas.KeyframeStack(library, x, y, self.levels, step=self.step)
+        self.setup_s = time.perf_counter() - t0
+        n = len(self.stack.keyframes)
+        self.pixels = WIDTH * HEIGHT
+        self.fields = torch.empty((n, self.pixels), dtype=torch.float32, device="cuda")
+        self.counts = torch.empty((n, self.pixels), dtype=torch.int32, device="cuda")
+        self.stream = stream
+        self.handle = stream.cuda_stream
+        self.targets = [(self.fields[i].data_ptr(), self.counts[i].data_ptr()) for i in range(n)]
+        keyframes = self.stack.keyframes
+        self.fp64_direct = [i for i, k in enumerate(keyframes) if k.reference is None and k.shallow_reference is None]
+        self.shallow = [i for i, k in enumerate(keyframes) if k.shallow_reference is not None]
+        self.direct = [i for i, k in enumerate(keyframes) if k.reference is None]
+        self.deep = [i for i, k in enumerate(keyframes) if k.reference is not None]
+        # Claim order: the direct levels first in the direct queue, the
+        # deepest levels first in the perturbation queue.
+        self.order = self.direct + self.deep[::-1]
+        self.floatexp = self.shallow + self.deep[::-1]
+
+    def step_device(self, form, subset=None, autotune=False, tiles=0):
+        self.stack.render_batch_device(self.targets, WIDTH, HEIGHT, form=form, stream=self.handle, graph=True,
+                                       autotune=autotune, order=subset if subset is not None else self.order,
+                                       tiles=tiles if form == 1 else 0)
+
+    def timed(self, form, steps, warmup, subset=None, tiles=0):
+        import torch
+
+        for _ in range(warmup):
+            self.step_device(form, subset, tiles=tiles)
+        torch.cuda.synchronize()
+        if self.world > 1:
+            torch.distributed.barrier()
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(self.stream)
+        for _ in range(steps):
+            self.step_device(form, subset, tiles=tiles)
+        stop.record(self.stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(start.elapsed_time(stop))
+
+    def compare_forms(self, form):
+        """Counts of both forms on the same views: work, mismatch (all and
+        per keyframe) and smooth-value error where the counts agree."""
+        import torch
+
+        self.step_device(form)
+        torch.cuda.synchronize()
+        chosen_counts = self.counts.clone()
+        chosen_field = self.fields.clone()
+        work = int(self.counts.to(torch.int64).sum().item())
+        per_level_work = self.counts.to(torch.int64).sum(dim=1).cpu().numpy()
+        self.step_device(0)
+        torch.cuda.synchronize()
+        plain_work = int(self.counts.to(torch.int64).sum().item())
+        differ = self.counts != chosen_counts
+        per_field = (differ.sum(dim=1).to(torch.float64) / self.pixels).cpu().numpy()
+        mismatch = int(differ.sum().item())
+        both = torch.isfinite(self.fields) & torch.isfinite(chosen_field) & ~differ
+        err = (self.fields - chosen_field).abs()
+        per_field_p99 = []
+        for i in range(err.shape[0]):
+            e = err[i][both[i]]
+            sample = e[torch.randperm(e.numel(), device="cuda")[:200_000]].float()
+            per_field_p99.append(float(torch.quantile(sample, 0.99).item()) if sample.numel() else 0.0)
+        e = err[both]
+        sample = e[torch.randperm(e.numel(), device="cuda")[:1_000_000]].float()
+        smooth = {"median": float(sample.median().item()), "p99": float(torch.quantile(sample, 0.99).item()),
+                  "max": float(e.max().item())}
+        del chosen_counts, chosen_field, differ, both, err
+        return {"work": work, "plain_work": plain_work, "mismatch": mismatch / (self.fields.shape[0] * self.pixels),
+                "per_field_mismatch": per_field, "per_field_smooth_p99": per_field_p99, "smooth": smooth,
+                "per_level_work": per_level_work}
+
+    def close(self):
+        self.stack.close()
 
 
 def run_gpu_arm(args) -> int:
@@ -246,182 +389,141 @@ def run_gpu_arm(args) -> int:
     torch.cuda.set_device(local_rank)
     package = __graft_entry__._package()
     native = package.native
-    atlas = package.atlas
     library = package.load_library()
-    levels, step = workload_levels()
-    x, y = centre()
-    t0 = time.perf_counter()
-    stack = atlas.KeyframeStack(library, x, y, levels, step=step)
-    setup_s = time.perf_counter() - t0
-    n_levels = len(stack.keyframes)
-    pixels = WIDTH * HEIGHT
-    fields = torch.empty((n_levels, pixels), dtype=torch.float32, device="cuda")
-    counts = torch.empty((n_levels, pixels), dtype=torch.int32, device="cuda")
-    # A dedicated stream: the library enqueues on the handle it is given, and
-    # the timing events are recorded on the same stream.
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    handle = stream.cuda_stream
-    assert handle != 0
-    forms = {"plain": 0, "chosen": 1 if args.form == "chosen" else 0}
-    targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(n_levels)]
-    direct_levels = [i for i, k in enumerate(stack.keyframes) if k.reference is None]
-    deep_levels = [i for i, k in enumerate(stack.keyframes) if k.reference is not None]
-    # Claim order: the shallow levels with interior (largest per-pixel cost)
-    # first in the direct queue, the deepest levels first in the deep queue.
-    order = direct_levels + deep_levels[::-1]
-    schedules = {"chunks": 0, "tiles": native.BATCH_TILES, "learned": native.BATCH_TILES | native.BATCH_LEARNED}
-    net = None
-    if forms["chosen"] == 1:
-        net = package.costnet.load_default(library)
-        net.attach()
+    assert stream.cuda_stream != 0
+    chosen = 1 if args.form == "chosen" else 0
+    run = StackBench(package, library, args.workload, stream, world)
+    n_levels = len(run.stack.keyframes)
 
-    def step_device(form, subset=None, autotune=False, schedule="chunks"):
-        stack.render_batch_device(targets, WIDTH, HEIGHT, form=form, stream=handle, graph=True, autotune=autotune,
-                                  order=subset if subset is not None else order,
-                                  tiles=schedules[schedule] if form == 1 else 0)
-
-    def timed(form, steps, warmup, subset=None, schedule="chunks"):
-        for _ in range(warmup):
-            step_device(form, subset, schedule=schedule)
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        start = torch.cuda.Event(enable_timing=True)
-        stop = torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        for _ in range(steps):
-            step_device(form, subset, schedule=schedule)
-        stop.record(stream)
-        torch.cuda.synchronize()
-        return max_over_ranks(start.elapsed_time(stop))
-
-    # Launch shapes tuned once per schedule on this batch (graph replay; the
+    # Launch shapes tuned once per form on this batch (graph replay; the
     # shapes change the schedule only, never a pixel).
-    for name in (schedules if forms["chosen"] == 1 else ["chunks"]):
-        step_device(forms["chosen"], autotune=True, schedule=name)
-    if forms["chosen"] != 0:
-        step_device(0, autotune=True)
-
-    # Work per step (sum of counts) for the chosen form, verified against the
-    # plain form (the parity form) on the same views.
-    step_device(forms["chosen"])
+    run.step_device(chosen, autotune=True)
+    if chosen:
+        run.step_device(0, autotune=True)
+    compared = run.compare_forms(chosen)
+    work = compared["work"]
+    run.step_device(chosen)
     torch.cuda.synchronize()
-    chosen_counts = counts.clone()
-    chosen_field = fields.clone()
-    work = int(counts.to(torch.int64).sum().item())
-    direct_work = int(counts[direct_levels].to(torch.int64).sum().item())
-    step_device(0)
-    torch.cuda.synchronize()
-    plain_work = int(counts.to(torch.int64).sum().item())
-    mismatch = int((counts != chosen_counts).sum().item())
-    both = torch.isfinite(fields) & torch.isfinite(chosen_field) & (counts == chosen_counts)
-    smooth_err = (fields[both] - chosen_field[both]).abs()
-    smooth_stats = {"median": float(smooth_err.median().item()), "p99": float(torch.quantile(
-        smooth_err[torch.randperm(smooth_err.numel(), device="cuda")[:1_000_000]].float(), 0.99).item()),
-        "max": float(smooth_err.max().item())}
-    del chosen_counts, chosen_field, both, smooth_err
-
-    # The chosen schedule: the fastest of the three, each timed the same way.
-    schedule_ms = {}
-    if forms["chosen"] == 1:
-        for name in schedules:
-            schedule_ms[name] = timed(1, max(2, args.steps // 2), 1, schedule=name) / max(2, args.steps // 2)
-        chosen_schedule = min(schedule_ms, key=schedule_ms.get)
-    else:
-        chosen_schedule = "chunks"
-    step_device(forms["chosen"], schedule=chosen_schedule)
-    torch.cuda.synchronize()
-    shapes = stack.queue_shapes()
+    shapes = run.stack.queue_shapes()
 
     sampler = ClockSampler(local_rank)
     sampler.start()
-    ms = timed(forms["chosen"], args.steps, args.warmup, schedule=chosen_schedule)
+    ms = run.timed(chosen, args.steps, args.warmup)
     clocks = sampler.stop()
     ms_per_step = ms / args.steps
     value = world * work * args.steps / (ms * 1e-3) / 1e9
+    plain_steps = max(1, args.steps // 4)
+    plain_ms = run.timed(0, plain_steps, 1) if chosen else ms
+    plain_value = compared["plain_work"] * plain_steps / (plain_ms * 1e-3) / 1e9 if chosen else value
 
-    plain_ms = timed(0, max(1, args.steps // 2), 1) if forms["chosen"] != 0 else ms
-    plain_value = plain_work * max(1, args.steps // 2) / (plain_ms * 1e-3) / 1e9 if forms["chosen"] != 0 else value
-
-    # Each queue timed alone with the step's own launch shapes (same
-    # launches, one part of the batch).
+    # Each queue alone with the step's own launch shapes: the FP32
+    # perturbation queue (deep + shallow-mode levels) and the FP64 direct
+    # queue (levels that keep the direct iteration).
     pinned = (ctypes.c_int * 4)(*shapes)
     library.fractal_gb300_set_queue_shapes(pinned, 4)
-    direct_ms = timed(forms["chosen"], 2, 1, subset=direct_levels) / 2
-    steps_done = ctypes.c_ulonglong(0)
-    library.fractal_gb300_last_direct_steps(ctypes.byref(steps_done))
-    deep_ms = timed(forms["chosen"], 2, 1, subset=deep_levels[::-1], schedule=chosen_schedule) / 2
+    queue_ms = run.timed(chosen, 3, 1, subset=run.floatexp if chosen else run.deep[::-1]) / 3
+    direct_subset = run.fp64_direct if chosen else run.direct
+    direct_ms = run.timed(chosen, 3, 1, subset=direct_subset) / 3 if direct_subset else 0.0
     library.fractal_gb300_set_queue_shapes(None, 0)
-    fp64 = ctypes.c_double(0.0)
-    library.fractal_gb300_fma_peak(64, ctypes.byref(fp64))
     fp32 = ctypes.c_double(0.0)
     library.fractal_gb300_fma_peak(32, ctypes.byref(fp32))
-    # Direct queue: 7 FP64 mul/add per iteration actually computed; a mul or
-    # add issues at the FMA instruction rate, i.e. half the FMA flop peak.
-    direct_achieved = 7.0 * steps_done.value / (direct_ms * 1e-3) / 1e12
-    direct_peak = fp64.value / 2.0
-    deep = [stack.keyframes[i] for i in deep_levels]
+    fp64 = ctypes.c_double(0.0)
+    library.fractal_gb300_fma_peak(64, ctypes.byref(fp64))
+    # Algorithmic flops of the perturbation queue: the deep levels' counters
+    # (22 per exact step, 14 per linear block, 60 per cubic block, 8 per
+    # series term and pixel; the reference's own counters, taken from the
+    # plain form's render of the same views), plus 22 per iteration of the
+    # shallow-mode levels (every iteration there is an exact perturbation
+    # step: no series, no BLA, no culled pixel in those views).
     flops = 0.0
     library.fractal_set_stats_enabled(1)
-    for keyframe in deep:
-        stack.render_host(keyframe, WIDTH, HEIGHT)
+    for i in run.deep:
+        run.stack.render_host(run.stack.keyframes[i], WIDTH, HEIGHT)
         flops += algorithmic_flops(native.stats(library), 32)
     library.fractal_set_stats_enabled(0)
-    deep_achieved = flops / (deep_ms * 1e-3) / 1e12
-    deep_roofline = {"bound": "fp32-fma" if forms["chosen"] == 1 else "fp64-fma", "achieved": deep_achieved,
-                     "peak": fp32.value if forms["chosen"] == 1 else fp64.value, "unit": "TFLOP/s",
-                     "frac": deep_achieved / (fp32.value if forms["chosen"] == 1 else fp64.value),
-                     "launch_ms": deep_ms, "kernel": "floatexp queue (41 deep keyframes)"}
+    shallow_steps = int(sum(compared["per_level_work"][i] for i in run.shallow)) if chosen else 0
+    flops += 22.0 * shallow_steps
+    achieved = flops / (queue_ms * 1e-3) / 1e12
+    peak = fp32.value if chosen else fp64.value
     roofline = {
-        "bound": "fp64",
-        "achieved": direct_achieved,
-        "peak": direct_peak,
+        "bound": "fp32-fma" if chosen else "fp64-fma",
+        "achieved": achieved,
+        "peak": peak,
         "unit": "TFLOP/s",
-        "frac": direct_achieved / direct_peak if direct_peak else None,
+        "frac": achieved / peak if peak else None,
         "traffic": None,
-        "peak_source": "FP64 FMA chains measured on this GPU by fractal_gb300_fma_peak, halved for mul/add "
-                       "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks)",
-        "kernel": "direct_queue_kernel (14 shallow keyframes, the step's critical path)",
-        "launch_ms": direct_ms,
-        "flops_per_unit": "7 FP64 mul/add per computed iteration",
-        "units": int(steps_done.value),
+        "peak_source": f"FP{'32' if chosen else '64'} FMA chains measured on this GPU by fractal_gb300_fma_peak "
+                       "(MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks); of measured",
+        "kernel": f"floatexp_queue_kernel ({len(run.floatexp)} keyframes: {len(run.deep)} deep, "
+                  f"{len(run.shallow)} shallow-mode)" if chosen else "plain_mandelbrot_kernel (deep levels)",
+        "launch_ms": queue_ms,
+        "flops_per_unit": "22 per exact step, 14 per linear BLA block, 60 per cubic block, 8 per series term",
+        "flops_per_launch": flops,
     }
 
     # End to end through the renderer.h ABI: host output buffers, the field
-    # copied back every keyframe.
-    # Backend 4 selects the same floatexp form through the ABI; backend 0 is
-    # the plain form.
-    # The calls come from E2E_THREADS host threads at once, as the reference
-    # pipeline's prefetch executor makes them (visualizer.py:11541); each
-    # thread has its own stream and scratch in the library, so one thread's
-    # copy-back overlaps another's render.
+    # copied back every keyframe, from E2E_THREADS host threads at once (the
+    # reference pipeline's prefetch executor calls the library from several
+    # threads, visualizer.py:11541).  Backend 4 selects the floatexp form.
     from concurrent.futures import ThreadPoolExecutor
 
-    e2e_options = native.RenderOptions(backend=4 if forms["chosen"] == 1 else 0)
-    e2e_steps = max(1, args.steps // 2)
-    e2e_order = [stack.keyframes[i] for i in order]
+    e2e_options = native.RenderOptions(backend=4 if chosen else 0)
+    e2e_steps = max(1, args.steps // 4)
+    e2e_order = [run.stack.keyframes[i] for i in run.order]
 
     def render_one(keyframe):
-        stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
+        run.stack.render_host(keyframe, WIDTH, HEIGHT, options=e2e_options)
 
     with ThreadPoolExecutor(E2E_THREADS) as pool:
         list(pool.map(render_one, e2e_order[:2 * E2E_THREADS]))
+        if world > 1:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             list(pool.map(render_one, e2e_order))
-        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * work * e2e_steps / e2e_s / 1e9
+
+    # configs[1]'s 55-keyframe stack beside the headline (N=1 replica 0 only).
+    second = None
+    if rank == 0 and args.workload == HEADLINE and not args.headline_only:
+        del run.fields, run.counts
+        torch.cuda.empty_cache()
+        stack50 = StackBench(package, library, "fhd_keyframe_stack", stream, 1)
+        stack50.step_device(chosen, autotune=True)
+        if chosen:
+            stack50.step_device(0, autotune=True)
+        c50 = stack50.compare_forms(chosen)
+        steps50 = max(2, args.steps // 2)
+        ms50 = stack50.timed(chosen, steps50, 2)
+        plain50 = stack50.timed(0, max(1, args.steps // 8), 1) if chosen else ms50
+        schedules = {}
+        if chosen:
+            net = package.costnet.load_default(library)
+            net.attach()
+            for name, flags in (("tiles", native.BATCH_TILES), ("learned", native.BATCH_TILES | native.BATCH_LEARNED)):
+                stack50.step_device(chosen, autotune=True, tiles=flags)
+                schedules[name] = stack50.timed(chosen, steps50, 1, tiles=flags) / steps50
+            library.fractal_gb300_set_cost_network(None)
+            net.close()
+        schedules["chunks"] = ms50 / steps50
+        second = {"workload": "fhd_keyframe_stack", "keyframes": len(stack50.stack.keyframes),
+                  "max_log10_zoom": stack50.levels[-1][1], "max_cap": max(c for _, _, c in stack50.levels),
+                  "value": c50["work"] * steps50 / (ms50 * 1e-3) / 1e9, "ms_per_step": ms50 / steps50,
+                  "plain_value": c50["plain_work"] * max(1, args.steps // 8) / (plain50 * 1e-3) / 1e9,
+                  "count_mismatch_vs_plain": c50["mismatch"], "smooth_error_vs_plain": c50["smooth"],
+                  "pixel_iterations_per_step": c50["work"], "schedule_ms_per_step": schedules}
+        stack50.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(native, atlas, levels, step, x, y)
-    if net is not None:
-        library.fractal_gb300_set_cost_network(None)
-        net.close()
-    stack.close()
+        cpu = cpu_baseline_sample(native, package.atlas, run.levels, run.step, *centre())
+    run.close()
 
     if rank == 0:
+        per_field = compared["per_field_mismatch"]
         line = {
             "metric": METRIC,
             "value": value,
@@ -433,41 +535,49 @@ def run_gpu_arm(args) -> int:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32-floatexp" if forms["chosen"] == 1 else "f64",
+            "dtype": "f32-floatexp" if chosen else "f64",
             "data": "synthetic (seeded Misiurewicz centre, tests/golden/centres.json)",
             "config": {
-                "workload": "fhd_keyframe_stack",
+                "workload": args.workload,
                 "keyframes": n_levels,
                 "width": WIDTH,
                 "height": HEIGHT,
                 "keyframe_factor": FACTOR,
-                "max_log10_zoom": levels[-1][1],
-                "max_cap": max(c for _, _, c in levels),
+                "max_log10_zoom": run.levels[-1][1],
+                "max_cap": max(c for _, _, c in run.levels),
                 "form": args.form,
                 "pixel_iterations_per_step": work,
-                "count_mismatch_vs_plain": mismatch / (n_levels * pixels),
+                "count_mismatch_vs_plain": compared["mismatch"],
                 "plain_value": plain_value,
-                "reference_setup_s": setup_s,
+                "chosen_vs_plain": value / plain_value if plain_value else None,
+                "per_field_count_mismatch": [round(float(v), 7) for v in per_field],
+                "per_field_smooth_p99_vs_plain": [round(v, 5) for v in compared["per_field_smooth_p99"]],
+                "max_field_count_mismatch": float(max(per_field)),
+                "smooth_error_vs_plain": compared["smooth"],
+                "reference_setup_s": run.setup_s,
+                "levels": {"fp64_direct": [run.stack.keyframes[i].level for i in run.fp64_direct],
+                           "shallow_mode": [run.stack.keyframes[i].level for i in run.shallow],
+                           "deep": len(run.deep)},
                 "queue_shapes": {"direct_chunk": shapes[0], "direct_blocks_per_sm": shapes[1],
                                  "floatexp_chunk": shapes[2], "floatexp_blocks_per_sm": shapes[3]},
-                "launch": "one batched call per step: direct FP64 lane-refill queue (second stream) + "
-                          "floatexp queue, replayed as a CUDA graph",
-                "schedule": chosen_schedule,
-                "schedule_ms_per_step": schedule_ms,
-                "smooth_error_vs_plain": smooth_stats,
-                "direct_pixel_iterations": direct_work,
-                "floatexp_roofline": deep_roofline,
-                "l2": "outputs larger than L2 (455 MB field + 455 MB counts per step)",
+                "queue_ms_alone": {"floatexp_queue": queue_ms, "fp64_direct_queue": direct_ms},
+                "launch": "one batched call per step replayed as a CUDA graph: FP32 perturbation queue "
+                          "(floatexp + shallow mode) on the caller's stream, FP64 direct queue on a second "
+                          "stream for the levels that keep it",
+                "schedule": "chunks",
+                "fhd_keyframe_stack": second,
+                "l2": "outputs larger than L2 (fields + counts: "
+                      f"{n_levels * WIDTH * HEIGHT * 8 / 1e6:.0f} MB per step)",
             },
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "Gpixel-iter/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": n_levels * pixels * 4,
-                    "path": f"fractal_render_reference_ex / render_fractal_ex into host memory, {E2E_THREADS} host threads"},
-            # Per step: direct coordinates + 4 queue phases; series prologue +
-            # the floatexp queue (learned adds probe, features, 2 GEMMs,
-            # output layer, order); the plain form launches per deep field.
-            "gpu_launches": args.steps * ((6 + (7 if chosen_schedule == "learned" else 1)) if forms["chosen"] == 1
-                                          else 5 + len(deep_levels)),
+                    "d2h_bytes_per_step": n_levels * WIDTH * HEIGHT * 4,
+                    "path": f"fractal_render_reference_ex (backend {4 if chosen else 0}) / render_fractal_ex "
+                            f"into host memory, {E2E_THREADS} host threads"},
+            # Per step: direct coordinates + direct queue (when the step has
+            # FP64 direct levels), series prologue + floatexp queue; the plain
+            # form launches the direct pair plus one kernel per deep field.
+            "gpu_launches": args.steps * ((2 if run.fp64_direct else 0) + 2 if chosen else 2 + len(run.deep)),
             "roofline": roofline,
             "cpu_baseline": cpu,
         }
@@ -914,6 +1024,9 @@ def main() -> int:
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", choices=["ours", "reference"], default="ours")
     parser.add_argument("--form", choices=["chosen", "plain"], default="chosen")
+    parser.add_argument("--workload", choices=sorted(WORKLOADS), default=HEADLINE)
+    parser.add_argument("--headline-only", action="store_true",
+                        help="skip the 55-keyframe stack measured beside the 1e100 atlas")
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--frame-passes", action="store_true",
                         help="time the per-frame 4K passes (atlas compositor, colour) and exit")
@@ -928,6 +1041,8 @@ def main() -> int:
                                  "aurora_colour_3840x2160", "atlas_colour_3840x2160"],
                         help="run one fixed piece of the workload for a profiler capture and exit")
     args = parser.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ and not (args.case or args.frame_passes or args.song):
+        return launch_replicas(sys.argv[1:], args.gpus)
     if args.case:
         return run_case(args.case)
     if args.frame_passes:

@@ -87,12 +87,45 @@ def zoom_text(log10_zoom: float) -> bytes:
     return native.zoom_text(log10_zoom)
 
 
+# Zoom (log10) from which a direct-path level keeps the FP64 direct
+# iteration in the floatexp form: there FP64's 2^-53 resolution leaves fewer
+# than about ten bits below a 1080-row pixel, so the FP64 counts are decided
+# by FP64 rounding and only FP64 reproduces them.
+SHALLOW_FP64_LOG10_ZOOM = 10.0
+
+
+def view_meets_interior(x: float, y: float, log10_zoom: float, aspect: float = 16.0 / 9.0) -> bool:
+    """Whether a view reaches the main cardioid's or period-2 bulb's bounding
+    box (0.05 margin), as the direct path's interior test decides it.  Near
+    those boundaries escape times grow without bound (parabolic points), so a
+    1e-4-pixel error in c moves many counts: such views keep the FP64 direct
+    iteration in the floatexp form."""
+    half_h = 0.5 * 2.8 / 10.0 ** log10_zoom + 0.05
+    half_w = 0.5 * 2.8 * aspect / 10.0 ** log10_zoom + 0.05
+    cardioid = x + half_w >= -0.80 and x - half_w <= 0.40 and y + half_h >= -0.70 and y - half_h <= 0.70
+    bulb = x + half_w >= -1.30 and x - half_w <= -0.70 and y + half_h >= -0.30 and y - half_h <= 0.30
+    return cardioid or bulb
+
+
+def shallow_perturbation(x: str, y: str, log10_zoom: float) -> bool:
+    """Whether the floatexp form renders a direct-path level (below 1e12) by
+    FP32 perturbation from the root reference (its shallow mode) rather than
+    by the FP64 direct iteration."""
+    if log10_zoom >= SHALLOW_FP64_LOG10_ZOOM:
+        return False
+    return not view_meets_interior(float(x), float(y), log10_zoom)
+
+
 @dataclass
 class Keyframe:
     level: int
     log10_zoom: float
     max_iter: int
     reference: Optional[int]  # handle for deep levels, None for direct ones
+    # Direct levels of a stack that has a root reference, where
+    # shallow_perturbation() holds: that handle, which the floatexp form
+    # (form 1) renders them from in its shallow mode.
+    shallow_reference: Optional[int] = None
 
 
 class KeyframeStack:
@@ -123,9 +156,11 @@ class KeyframeStack:
                 self.handles.append(clone)
                 references.append((tier, clone))
         self.keyframes = []
+        root = self.handles[0] if self.handles else None
         for level, log_zoom, max_iter in levels:
             reference = select_reference(references, log_zoom) if log_zoom >= 12.0 else None
-            self.keyframes.append(Keyframe(level, log_zoom, max_iter, reference))
+            shallow = root if reference is None and shallow_perturbation(x_center, y_center, log_zoom) else None
+            self.keyframes.append(Keyframe(level, log_zoom, max_iter, reference, shallow))
 
     def close(self) -> None:
         for handle in reversed(self.handles):
@@ -135,10 +170,19 @@ class KeyframeStack:
     def render_device(self, keyframe: Keyframe, field_ptr: int, counts_ptr: int, width: int, height: int,
                       *, form: int = 0, series_order: int = 3, series_block: int = 256,
                       options: Optional[native.RenderOptions] = None, stream: int = 0) -> None:
-        """Enqueue one keyframe into device buffers (GB300 extension ABI)."""
+        """Enqueue one keyframe into device buffers (GB300 extension ABI).
+
+        Direct levels take the FP64 direct path in form 0; in form 1 they
+        render from the root reference in the floatexp form's shallow mode
+        when the stack has one."""
         options = options or native.RenderOptions()
         zoom = zoom_text(keyframe.log10_zoom)
-        if keyframe.reference is None:
+        if keyframe.reference is None and form == 1 and keyframe.shallow_reference is not None:
+            status = self.library.fractal_gb300_render_reference_device(
+                ctypes.c_void_p(field_ptr), ctypes.c_void_p(counts_ptr), width, height, zoom,
+                ctypes.c_void_p(keyframe.shallow_reference), keyframe.max_iter, series_order, series_block,
+                ctypes.byref(options), form, ctypes.c_void_p(stream))
+        elif keyframe.reference is None:
             status = self.library.fractal_gb300_render_direct_device(
                 ctypes.c_void_p(field_ptr), ctypes.c_void_p(counts_ptr), width, height, zoom,
                 self.x.encode("ascii"), self.y.encode("ascii"), keyframe.max_iter, 0, 0.0, 0.0,
@@ -172,7 +216,11 @@ class KeyframeStack:
             frames[slot].field = field_ptr
             frames[slot].counts = counts_ptr
             frames[slot].zoom_text = zooms[-1]
-            frames[slot].reference = keyframe.reference
+            if keyframe.reference is None and keyframe.shallow_reference is not None:
+                frames[slot].reference = keyframe.shallow_reference
+                frames[slot].flags = native.KEYFRAME_SHALLOW
+            else:
+                frames[slot].reference = keyframe.reference
             frames[slot].max_iter = keyframe.max_iter
         flags = (native.BATCH_GRAPH if graph else 0) | (native.BATCH_AUTOTUNE if autotune else 0) | tiles
         status = self.library.fractal_gb300_render_keyframes_device(
@@ -190,8 +238,17 @@ class KeyframeStack:
     def render_host(self, keyframe: Keyframe, width: int, height: int, *, threads: int = 0,
                     series_order: int = 3, series_block: int = 256, planes: bool = False,
                     options: Optional[native.RenderOptions] = None):
-        """Render one keyframe through the renderer.h ABI into host memory."""
+        """Render one keyframe through the renderer.h ABI into host memory.
+
+        With the CUDA backend's floatexp form (options.backend 4) a direct
+        level renders from the root reference in the shallow mode."""
         zoom = zoom_text(keyframe.log10_zoom)
+        shallow = (keyframe.reference is None and keyframe.shallow_reference is not None
+                   and options is not None and options.backend == native.BACKEND_CUDA)
+        if shallow:
+            return native.render_reference(self.library, keyframe.shallow_reference, width, height, zoom,
+                                           keyframe.max_iter, threads=threads, series_order=series_order,
+                                           series_block=series_block, options=options, planes=planes)
         if keyframe.reference is None:
             return native.render_fractal(self.library, width, height, zoom, self.x, self.y, keyframe.max_iter,
                                          256, False, threads=threads, options=options, planes=planes)

@@ -30,6 +30,11 @@
 namespace fgb {
 
 thread_local std::string last_error;
+// Whether this thread has made its runtime (streams, scratch), and whether
+// its last direct launch was a no-allocation one (whose counters live in
+// the shared no-allocation array, not in the thread's scratch).
+thread_local bool runtime_made = false;
+thread_local bool last_direct_noalloc = false;
 
 void set_error(const std::string& message) { last_error = message; }
 
@@ -71,6 +76,7 @@ ThreadRuntime& thread_runtime() {
     if (rt.stream == nullptr || rt.device != device) {
         rt.~ThreadRuntime();
         new (&rt) ThreadRuntime();
+        runtime_made = true;
         rt.device = device;
         check_cuda(cudaStreamCreateWithFlags(&rt.stream, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaMalloc(&rt.stats, sizeof(unsigned long long) * kStatsSlots), "cudaMalloc (stats)");
@@ -429,6 +435,7 @@ void launch_direct_render(const Outputs& out, int width, int height, long double
     const long long spill = spill_entries(static_cast<long long>(width) * height);
     void* work = scratch(rt, kScratchDirect, direct_scratch_bytes(&p, 1, spill));
     check_cuda(launch_direct_batch(&p, 1, work, QueueShape{}, spill, stream), "direct kernel launch");
+    last_direct_noalloc = false;
 }
 
 // Dispatch of a reference render by zoom depth and formula
@@ -461,19 +468,54 @@ void render_from_reference(ReferenceContext& ctx, const Outputs& out, int width,
 // non-strict cycle detection and time budgets use the plain form.
 namespace {
 
+// Zoom below which the reference pipeline renders a field on the direct
+// path (visualizer.py:6152); the floatexp form renders such fields in its
+// shallow mode (FxParams::shallow).
+constexpr long double kShallowLog10Zoom = 12.0L;
+
 // Floatexp kernel parameters of one field, or false when the field is not
-// one the floatexp form covers (shallow, alternate formula, non-strict cycle
-// detection, time budget): those render in the plain form.
+// one the floatexp form covers (alternate formula, non-strict cycle
+// detection, time budget): those render in the plain form.  Fields below
+// 1e12 take the shallow mode: plain FP32 perturbation against the handle's
+// orbit with unlimited rebasing, no series and no BLA.
 bool make_floatexp_params(ReferenceContext& ctx, const Outputs& out, int width, int height, const char* zoom_text,
                           int max_iter, int series_order, int series_block, const FractalRenderOptions& o,
                           FxParams& p) {
     const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx.precision_bits);
     const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
-    if (fe_log10(zoom) < 6.0L || ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) return false;
+    if (ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) return false;
     std::shared_ptr<DeviceTables> dev = device_tables(ctx);
     floatexp_tables(ctx, *dev);
     const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
     std::memset(static_cast<void*>(&p), 0, sizeof p);  // padding too: the bytes key the graph cache
+    if (fe_log10(zoom) < kShallowLog10Zoom) {
+        if (dev->orbit_size < 2) return false;
+        const double half_h = 0.5 * fx::scale2(g.view_height.m, g.view_height.e) + 0.05;
+        const double half_w = 0.5 * fx::scale2(g.view_width.m, g.view_width.e) + 0.05;
+        const double x = static_cast<double>(ctx.x_center), y = static_cast<double>(ctx.y_center);
+        const bool cardioid = x + half_w >= -0.80 && x - half_w <= 0.40 && y + half_h >= -0.70 && y - half_h <= 0.70;
+        const bool bulb = x + half_w >= -1.30 && x - half_w <= -0.70 && y + half_h >= -0.30 && y - half_h <= 0.30;
+        p.orbit = dev->fx_orbit;
+        p.orbit_size = dev->orbit_size;
+        p.view_width = f32x::norm(static_cast<float>(g.view_width.m), 0.0f, g.view_width.e);
+        p.view_height = f32x::norm(static_cast<float>(g.view_height.m), 0.0f, g.view_height.e);
+        p.coordinate_mode = o.coordinate_mode;
+        p.width = width;
+        p.height = height;
+        p.max_iter = max_iter;
+        p.map_end = ctx.map_end;
+        p.disable_bla = 1;
+        p.strict = o.strict;
+        p.escape_mode = o.escape_radius_mode;
+        p.output_bias = static_cast<float>(o.output_bias);
+        p.out = out.field;
+        p.counts = out.counts;
+        p.shallow = 1;
+        p.interior_test = cardioid || bulb ? 1 : 0;
+        p.centre_re = static_cast<float>(x);
+        p.centre_im = static_cast<float>(y);
+        return true;
+    }
     const bool covers = fx::fe_cmp(g.current_input_radius, ctx.input_radius) <= 0;
     const bool use_deep = fx::fe_cmp(g.current_input_radius, ctx.deep_input_radius) <= 0;
     const bool use_ultra = fx::fe_cmp(g.current_input_radius, fx::fe_mul(ctx.input_radius, 1.0e-40)) <= 0;
@@ -1488,6 +1530,7 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
             const int n = static_cast<int>(std::min<std::size_t>(kMaxDirectFields, fields.size() - i));
             long long pixels = 0;
             for (int f = 0; f < n; ++f) pixels += static_cast<long long>(fields[i + f].width) * fields[i + f].height;
+            last_direct_noalloc = false;
             check_cuda(launch_direct_batch(fields.data() + i, n, direct_scratch, shapes.direct, spill_entries(pixels),
                                            direct_stream, plan.fast_smooth),
                        "direct batch launch");
@@ -2361,7 +2404,11 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
             Outputs out;
             out.field = frame.field;
             out.counts = frame.counts;
-            if (!frame.reference) {
+            const bool shallow = (frame.flags & FRACTAL_GB300_KEYFRAME_SHALLOW) != 0;
+            if ((frame.flags & ~FRACTAL_GB300_KEYFRAME_SHALLOW) != 0) {
+                throw Failure{"invalid native keyframe " + std::to_string(i) + " flags"};
+            }
+            if (!frame.reference || (shallow && form == 0)) {
                 if (!centre_parsed) {
                     if (!x_center || !y_center) throw Failure{"keyframe batch without a centre for direct frames"};
                     cx = parse_coordinate(x_center, "real");
@@ -2394,7 +2441,7 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
                 continue;
             }
             const fx::Fe zoom = parse_zoom_fe(frame.zoom_text, ctx->precision_bits);
-            if (fe_log10(zoom) < 6.0L) {
+            if (fe_log10(zoom) < 6.0L || shallow) {
                 plan.direct[ctx->formula].push_back(make_direct_params(
                     out, width, height, parse_zoom_direct(frame.zoom_text), ctx->x_center, ctx->y_center,
                     frame.max_iter, ctx->formula, ctx->julia_re, ctx->julia_im, o));
@@ -2556,6 +2603,11 @@ int fractal_gb300_last_tiles(int* tiles, float* cost, uint16_t* features, int ca
 int fractal_gb300_last_direct_steps(unsigned long long* steps) {
     return guarded("reading the direct queue's step count failed", [&] {
         if (!steps) throw Failure{"null step counter"};
+        if (!runtime_made) throw Failure{"no direct batch has run on this thread"};
+        if (last_direct_noalloc) {
+            throw Failure{"the calling thread's last direct launch was a no-allocation render, whose counters "
+                          "are not kept"};
+        }
         ThreadRuntime& rt = thread_runtime();
         if (!rt.scratch[kScratchDirect]) throw Failure{"no direct batch has run on this thread"};
         check_cuda(cudaStreamSynchronize(rt.batch_stream ? rt.batch_stream : rt.stream), "keyframe batch");
@@ -2599,6 +2651,7 @@ int fractal_gb300_render_direct_device_noalloc(float* field, uint32_t* counts, i
                                                   julia_real, julia_imag, o);
         std::string why;
         if (!launch_direct_noalloc(p, static_cast<cudaStream_t>(stream_handle), why)) throw Failure{why};
+        last_direct_noalloc = true;
     });
 }
 

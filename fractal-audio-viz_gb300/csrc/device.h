@@ -332,6 +332,15 @@ struct FxParams {
     float* out;
     std::uint32_t* counts;
     FxSeriesScaled* series_scaled;  // per-field slot filled by the series prologue (nullptr: F2e Horner)
+    // Shallow mode (a field the reference pipeline renders on the direct
+    // path, below 1e12): plain FP32 perturbation against the orbit from
+    // iteration 0 with unlimited rebasing, no series, no BLA; pixels that the
+    // cardioid / period-2 bulb test puts clearly inside are written as
+    // interior without iterating (interior_test: the view reaches either).
+    int shallow;
+    int interior_test;
+    float centre_re;  // the view centre rounded to float (interior test only)
+    float centre_im;
 };
 
 cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stream);

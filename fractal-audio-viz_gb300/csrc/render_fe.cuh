@@ -1,5 +1,5 @@
-// Floatexp form (shared by render_fe.cu and queue.cu): deep Mandelbrot perturbation with FP32-mantissa / int32-
-// exponent deltas, one thread per pixel.
+// Floatexp form (included by render_fe.cu): deep Mandelbrot perturbation with FP32-mantissa / int32-exponent
+// deltas, one thread per pixel, plus the shallow mode (plain FP32 perturbation below 1e12).
 //
 // The decision structure is the plain form's (render_bla_impl,
 // renderer.cpp:12673-13583): image-series jump, glitch sentinel, escape,
@@ -201,9 +201,78 @@ __device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration,
     return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
 }
 
+// Shallow mode: a field above 1e-12 of view height renders by plain FP32
+// perturbation against the reference orbit, z_n = Z_m + d, from d = 0 at
+// iteration 0 (Z_0 = 0), rebasing to the orbit's start (d <- z, m <- 0)
+// whenever |z| < |d| or the orbit's valid part ends, with no limit on the
+// number of rebases.  The deltas' rounding error is relative to |d|, which
+// starts at the pixel's offset from the centre, so the counts equal those
+// of the FP64 direct iteration except where FP64 rounding itself decides
+// them.  The step is d' = d (2Z + d) + dc written as
+//   re: dr (2Zr + dr) - di (2Zi + di) + dcr
+//   im: 2 (Zr di + dr (Zi + di)) + dci
+// (6 FMA-pipe operations), then |Z + d|^2 for the escape and rebase tests.
+__device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py) {
+    const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
+    const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
+    const float dcr = ldexpf_fast(p.view_width.x * xf, p.view_width.e);
+    const float dci = ldexpf_fast(p.view_height.x * yf, p.view_height.e);
+    const PixelOut inside{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    if (p.interior_test) {
+        // Main cardioid and period-2 bulb (renderer.cpp:10060-10066), taken
+        // only with a margin far above the float error of c = centre + dc,
+        // so a culled pixel is interior in FP64 as well; pixels near either
+        // boundary are iterated (an interior pixel then reaches the cap).
+        const float cx = p.centre_re + dcr, cy = p.centre_im + dci;
+        const float xq = cx - 0.25f;
+        const float q = fmaf(xq, xq, cy * cy);
+        const bool cardioid = q * (q + xq) <= fmaf(0.25f * cy, cy, -1.0e-4f);
+        const float xb = cx + 1.0f;
+        const bool bulb = fmaf(xb, xb, cy * cy) <= 0.0625f - 1.0e-4f;
+        if (cardioid || bulb) return inside;
+    }
+    const float escape2 = p.escape_mode == 1 ? 1.0e8f : 4.0f;
+    const float safe2 = escape2 + 1.0e-7f;
+    // Last orbit entry before the reference escapes (map_end) or ends; the
+    // host guarantees orbit_size >= 2.
+    const int valid = max(1, min(p.map_end, p.orbit_size - 1));
+    const float2* orbit = reinterpret_cast<const float2*>(p.orbit);
+    constexpr int kStride = sizeof(FxOrbitRec) / sizeof(float2);
+    float dr = 0.0f, di = 0.0f;
+    float zr = 0.0f, zi = 0.0f;  // Z_0
+    int ref = 0;
+    for (int iteration = 1; iteration <= p.max_iter; ++iteration) {
+        const float ar = fmaf(2.0f, zr, dr), ai = fmaf(2.0f, zi, di);
+        const float nr = fmaf(dr, ar, fmaf(-di, ai, dcr));
+        const float ni = fmaf(2.0f, fmaf(zr, di, dr * (zi + di)), dci);
+        dr = nr;
+        di = ni;
+        ++ref;
+        const float2 z = __ldg(orbit + static_cast<long long>(ref) * kStride);
+        zr = z.x;
+        zi = z.y;
+        const float tr = zr + dr, ti = zi + di;
+        const float m2 = fmaf(tr, tr, ti * ti);
+        if (m2 > escape2) {
+            const float mag = sqrtf(fmaxf(m2, safe2));
+            return PixelOut{(static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                            static_cast<std::uint32_t>(iteration)};
+        }
+        if (m2 < fmaf(dr, dr, di * di) || ref >= valid) {
+            dr = tr;
+            di = ti;
+            zr = 0.0f;
+            zi = 0.0f;
+            ref = 0;
+        }
+    }
+    return inside;
+}
+
 // One pixel of the floatexp form; shared by the per-field kernel and the
-// batched persistent queue (queue.cu).
+// batched persistent queues.
 __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int py) {
+    if (p.shallow) return shallow_pixel(p, px, py);
     const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
     const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
     const F2e dx = norm(p.view_width.x * xf, 0.0f, p.view_width.e);

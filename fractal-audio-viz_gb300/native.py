@@ -373,7 +373,7 @@ class Keyframe(ctypes.Structure):
         ("zoom_text", ctypes.c_char_p),
         ("reference", ctypes.c_void_p),
         ("max_iter", ctypes.c_int),
-        ("reserved", ctypes.c_int),
+        ("flags", ctypes.c_int),
     ]
 
 
@@ -382,6 +382,7 @@ BATCH_AUTOTUNE = 2
 BATCH_TILES = 4
 BATCH_LEARNED = 8
 BATCH_PROBE = 16
+KEYFRAME_SHALLOW = 1
 
 _GB300_ABI = (
     ("fractal_gb300_device_count", ctypes.c_int, ()),

@@ -555,15 +555,24 @@ int fractal_gb300_pack_frame_device(const uint8_t *rgb, int width, int height, i
 /* One keyframe of a batch: device outputs (`counts` may be NULL), its zoom,
  * the reference handle it renders from (NULL: the direct FP64 path at the
  * batch centre, which the reference pipeline takes below 1e12,
- * visualizer.py:6152) and its iteration cap. */
+ * visualizer.py:6152), its iteration cap and flags (0 or
+ * FRACTAL_GB300_KEYFRAME_SHALLOW). */
 typedef struct FractalGb300Keyframe {
     float *field;
     uint32_t *counts;
     const char *zoom_text;
     void *reference;
     int max_iter;
-    int reserved;
+    int flags;
 } FractalGb300Keyframe;
+
+/* Keyframe flag: a frame the reference pipeline renders on the direct path
+ * (below 1e12) that also names a reference handle at the batch centre.  In
+ * form 0 it takes the direct FP64 path at the batch centre (the handle is
+ * not used); in form 1 it renders by FP32 perturbation against the handle's
+ * orbit (shallow mode: from iteration 0, unlimited rebasing, no series or
+ * BLA), which removes the FP64 direct iteration from the floatexp form. */
+#define FRACTAL_GB300_KEYFRAME_SHALLOW 1
 
 /* Capture the batch's launches into a CUDA graph and replay the graph when
  * the same batch (same buffers, zooms, handles and options) comes again. */
@@ -621,7 +630,11 @@ int fractal_gb300_last_tiles(int *tiles, float *cost, uint16_t *features, int ca
 
 /* Iterations the direct queue actually computed in the calling thread's last
  * direct launch (escaped pixels count their escape index, pixels the cycle
- * probe settled count the steps taken before it did); synchronises. */
+ * probe settled count the steps taken before it did); synchronises.  Fails
+ * when that launch was a fractal_gb300_render_direct_device_noalloc call
+ * (its counters are not kept) and when the thread has made no direct launch;
+ * fails too, after the count is copied, when the launch's spill queue
+ * reported an unpublished entry (the render is then incomplete). */
 int fractal_gb300_last_direct_steps(unsigned long long *steps);
 
 /* Launch shapes the calling thread's last batch used: direct chunk, direct
@@ -634,7 +647,11 @@ int fractal_gb300_queue_shapes(int *values, int capacity);
  * reserve-everything-up-front memory policy, or in a real-time loop where an
  * allocation's implicit synchronisation is not acceptable.  It calls no
  * cudaMalloc/cudaFree and creates no stream: `stream` NULL means the legacy
- * default stream.  Its scratch is a fixed 128 KiB array inside the library,
+ * default stream (fractal_gb300_render_direct_device's NULL means the calling
+ * thread's own non-blocking stream, so NULL-stream calls of the two entry
+ * points are ordered differently).  It runs without the spill list (long
+ * pixels finish in their own lane), so its pixels are the same but its tail
+ * latency on interior-heavy views can be longer.  Its scratch is a fixed 128 KiB array inside the library,
  * so width + height must be at most 16352 (larger fields fail with an error,
  * before any launch).  All calls share that array: calls ordered on one
  * stream are independent (each call resets what it uses), calls that overlap

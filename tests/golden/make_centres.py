@@ -296,7 +296,22 @@ def julia_boundary_constant(seed: int):
     raise RuntimeError("no Julia boundary constant found")
 
 
+def add_deep_alternates(path: str) -> None:
+    """Add 130-digit burning-ship and tricorn boundary points (views to 1e100
+    need more than 100 digits) to an existing centres.json."""
+    with open(path, encoding="ascii") as handle:
+        centres = json.load(handle)
+    centres["burning_ship_boundary_deep"] = alternate_boundary("burning-ship", seed=8201, digits=130)
+    centres["tricorn_boundary_deep"] = alternate_boundary("tricorn", seed=8202, digits=130)
+    with open(path, "w", encoding="ascii") as handle:
+        json.dump(centres, handle, indent=1)
+        handle.write("\n")
+
+
 def main() -> int:
+    if "--deep-alternates" in sys.argv:
+        add_deep_alternates(os.path.join(HERE, "centres.json"))
+        return 0
     centres = {
         # 640x360 at 1e30: 400-bit Newton, 120-digit strings.
         "field_640x360_e30": misiurewicz_centre(seed=20240, bits=400, digits=120),

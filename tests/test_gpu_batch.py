@@ -69,16 +69,12 @@ def test_batch_equals_single_keyframe_renders(package, product, form):
         direct = np.array([k.reference is None for k in stack.keyframes])
     finally:
         stack.close()
+    # In form 1 the direct levels that shallow_perturbation() admits render
+    # from the root reference in the floatexp form's shallow mode, the others
+    # on the FP64 direct path, in the batch and alone alike.
+    assert direct.any() and any(k.shallow_reference is not None for k in stack.keyframes)
     np.testing.assert_array_equal(got_counts, want_counts)
-    if form == 0:
-        np.testing.assert_array_equal(got_field, want_field)
-        return
-    # The floatexp form's batch takes the direct frames' smooth logarithms in
-    # FP32: counts identical, smooth values within a few float ulps.
-    np.testing.assert_array_equal(got_field[~direct], want_field[~direct])
-    got = got_field[direct].view(np.float32).astype(np.float64)
-    want = want_field[direct].view(np.float32).astype(np.float64)
-    assert np.all(np.abs(got - want) <= 4e-6 * np.maximum(1.0, np.abs(want))), np.max(np.abs(got - want))
+    np.testing.assert_array_equal(got_field, want_field)
 
 
 def test_batch_graph_replay_order_and_autotune_keep_pixels(package, product):
