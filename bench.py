@@ -378,6 +378,118 @@ class StackBench:
         self.stack.close()
 
 
+def measure_batch_mix(package, library, stream, steps: int, local_rank: int) -> dict:
+    """configs[2]: 64 seeded fields mixing the four formulas and the four
+    sizes 720x480 .. 3840x2160, zooms log-uniform 1e10-1e100, caps
+    log-uniform 1e4-1e6, counts + smooth field + derivative planes, all in
+    one fractal_gb300_render_fields_device call (graph replay, launch
+    shapes autotuned on the batch).  Reports Gpixel-iter/s of both forms, the
+    count mismatch per formula and the derivative planes' error."""
+    import torch
+
+    from tests.golden import cases as case_defs
+
+    mix = case_defs.batch_mix(seed=2024, count=64)
+    # (The chosen form here is slow on the other formulas' FP64 fields: a
+    # batch takes tens of seconds, so the leg times few batches.)
+    specs = [package.fields.FieldSpec(m["formula"], m["re"], m["im"], m["log10_zoom"], m["width"], m["height"],
+                                      m["max_iter"], tuple(m["julia"])) for m in mix]
+    t0 = time.perf_counter()
+    fields = package.fields.FieldSet(library, specs, threads=os.cpu_count() or 8,
+                                     initializer=lambda: torch.cuda.set_device(local_rank))
+    setup_s = time.perf_counter() - t0
+    bufs = []
+    for m in mix:
+        n = m["width"] * m["height"]
+        bufs.append((torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda"),
+                     torch.empty(n, dtype=torch.float64, device="cuda"),
+                     torch.empty(n, dtype=torch.float64, device="cuda")))
+    targets = [tuple(t.data_ptr() for t in b) for b in bufs]
+    handle = stream.cuda_stream
+    try:
+        def timed(form, count, fp32=False):
+            torch.cuda.synchronize()
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            for _ in range(count):
+                fields.render_device(targets, form=form, stream=handle, graph=True, fp32_alternates=fp32)
+            stop.record(stream)
+            torch.cuda.synchronize()
+            return start.elapsed_time(stop) / count
+
+        def mismatch_vs(plain_counts):
+            per = {}
+            for m, b, pc in zip(mix, bufs, plain_counts):
+                d, t = per.get(m["formula"], (0, 0))
+                per[m["formula"]] = (d + int((b[1] != pc).sum().item()), t + pc.numel())
+            return {f: d / t for f, (d, t) in per.items()}
+
+        fields.render_device(targets, form=0, stream=handle, graph=True)
+        torch.cuda.synchronize()
+        plain = [(b[1].clone(), b[2].clone(), b[3].clone()) for b in bufs]
+        plain_counts = [p[0] for p in plain]
+        plain_work = sum(int(c.to(torch.int64).sum().item()) for c in plain_counts)
+        # The FP32 queue for all four formulas (opt-in): launch shapes tuned
+        # on it, its throughput and its drift from the FP64 counts.
+        fields.render_device(targets, form=1, stream=handle, graph=True, fp32_alternates=True, autotune=True)
+        torch.cuda.synchronize()
+        shapes = (ctypes.c_int * 4)()
+        library.fractal_gb300_queue_shapes(shapes, 4)
+        fp32_all_mismatch = mismatch_vs(plain_counts)
+        fp32_all_work = sum(int(b[1].to(torch.int64).sum().item()) for b in bufs)
+        fp32_all_ms = timed(1, 2, fp32=True)
+        # The chosen form: Mandelbrot in the FP32 queue, the rest in FP64.
+        fields.render_device(targets, form=1, stream=handle, graph=True)
+        torch.cuda.synchronize()
+        work = sum(int(b[1].to(torch.int64).sum().item()) for b in bufs)
+        per_formula = mismatch_vs(plain_counts)
+        de_err = []
+        for m, b, (pc, pdx, pdy) in zip(mix, bufs, plain):
+            same = (b[1] == pc) & (pc < m["max_iter"])
+            pd = torch.hypot(pdx, pdy)[same]
+            qd = torch.hypot(b[2], b[3])[same]
+            ok = pd > 0
+            if ok.any():
+                de_err.append(((qd[ok] - pd[ok]).abs() / pd[ok]).float())
+        de_err = torch.cat(de_err)
+        de_sample = de_err[torch.randperm(de_err.numel(), device="cuda")[:1_000_000]]
+        chosen_ms = timed(1, steps)
+        plain_ms = timed(0, 1)  # the FP64 form takes tens of seconds per batch
+        pixels = sum(m["width"] * m["height"] for m in mix)
+        return {
+            "workload": "batch64_mixed",
+            "fields": len(mix),
+            "formulas": {f: sum(1 for m in mix if m["formula"] == f) for f in
+                         ("mandelbrot", "julia", "burning-ship", "tricorn")},
+            "sizes": {f"{w}x{h}": sum(1 for m in mix if (m["width"], m["height"]) == (w, h))
+                      for w, h in case_defs.BATCH_SIZES},
+            "pixels": pixels,
+            "log10_zoom_range": [round(min(m["log10_zoom"] for m in mix), 2),
+                                 round(max(m["log10_zoom"] for m in mix), 2)],
+            "cap_range": [min(m["max_iter"] for m in mix), max(m["max_iter"] for m in mix)],
+            "outputs": "uint32 counts, float32 smooth field, float64 de_x / de_y",
+            "value": work / (chosen_ms * 1e-3) / 1e9,
+            "unit": "Gpixel-iter/s",
+            "ms_per_batch": chosen_ms,
+            "plain_value": plain_work / (plain_ms * 1e-3) / 1e9,
+            "plain_ms_per_batch": plain_ms,
+            "pixel_iterations": work,
+            "count_mismatch_vs_plain_per_formula": per_formula,
+            "form": "chosen: Mandelbrot fields in the FP32 queue, the other formulas in FP64 beside it",
+            "fp32_all_formulas": {"value": fp32_all_work / (fp32_all_ms * 1e-3) / 1e9, "ms_per_batch": fp32_all_ms,
+                                  "count_mismatch_vs_plain_per_formula": fp32_all_mismatch},
+            "de_relative_error_vs_plain": {"median": float(de_sample.median().item()),
+                                           "p99": float(torch.quantile(de_sample, 0.99).item())},
+            "autotuned_queue_shapes": {"direct_chunk": shapes[0], "direct_blocks_per_sm": shapes[1],
+                                       "floatexp_chunk": shapes[2], "floatexp_blocks_per_sm": shapes[3],
+                                       "tuned_on": "the FP32 queue of all four formulas"},
+            "reference_setup_s": setup_s,
+            "launch": "one fractal_gb300_render_fields_device call replayed as a CUDA graph",
+        }
+    finally:
+        fields.close()
+
+
 def run_gpu_arm(args) -> int:
     import torch
 
@@ -517,6 +629,10 @@ def run_gpu_arm(args) -> int:
                   "pixel_iterations_per_step": c50["work"], "schedule_ms_per_step": schedules}
         stack50.close()
 
+    batch = None
+    if rank == 0 and args.workload == HEADLINE and not args.headline_only and chosen:
+        batch = measure_batch_mix(package, library, stream, 1, local_rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(native, package.atlas, run.levels, run.step, *centre())
@@ -566,6 +682,7 @@ def run_gpu_arm(args) -> int:
                           "stream for the levels that keep it",
                 "schedule": "chunks",
                 "fhd_keyframe_stack": second,
+                "batch64_mixed": batch,
                 "l2": "outputs larger than L2 (fields + counts: "
                       f"{n_levels * WIDTH * HEIGHT * 8 / 1e6:.0f} MB per step)",
             },

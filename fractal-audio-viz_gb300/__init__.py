@@ -31,6 +31,7 @@ atlas = _load("atlas")
 kfp = _load("kfp")
 costnet = _load("costnet")
 frames = _load("frames")
+fields = _load("fields")
 _builder = _load("build")
 LIBRARY_PATH = _builder.LIBRARY
 

@@ -474,20 +474,66 @@ namespace {
 constexpr long double kShallowLog10Zoom = 12.0L;
 
 // Floatexp kernel parameters of one field, or false when the field is not
-// one the floatexp form covers (alternate formula, non-strict cycle
-// detection, time budget): those render in the plain form.  Fields below
-// 1e12 take the shallow mode: plain FP32 perturbation against the handle's
-// orbit with unlimited rebasing, no series and no BLA.
+// one the floatexp form covers (non-strict cycle detection, time budget,
+// render planes other than the derivative pair; the other formulas unless
+// `fp32_alternates`, and then from 1e6): those render in the plain form.
+// The other formulas stay FP64 by default because their deep views hold
+// long post-linear orbits (Julia near its parabolic-like points, burning
+// ship's folds) that FP32 deltas cannot follow: against a direct mpmath
+// iteration the FP64 form is right where the FP32 form is not.  Mandelbrot fields below 1e12 take
+// the shallow mode: plain FP32 perturbation against the handle's orbit with
+// unlimited rebasing, no series and no BLA.
 bool make_floatexp_params(ReferenceContext& ctx, const Outputs& out, int width, int height, const char* zoom_text,
                           int max_iter, int series_order, int series_block, const FractalRenderOptions& o,
-                          FxParams& p) {
+                          FxParams& p, bool fp32_alternates = false) {
     const fx::Fe zoom = parse_zoom_fe(zoom_text, ctx.precision_bits);
     const bool cycle = o.disable_cycle == 0 && (o.strict == 0 || o.strict_cycle != 0);
-    if (ctx.formula != kFormulaMandelbrot || cycle || o.time_budget_ms > 0) return false;
+    if (cycle || o.time_budget_ms > 0 || out.p_iter || out.p_phase || out.p_t1 || out.p_t2) return false;
+    if ((out.p_dex == nullptr) != (out.p_dey == nullptr)) return false;
+    if (ctx.formula != kFormulaMandelbrot && (!fp32_alternates || fe_log10(zoom) < 6.0L)) return false;
     std::shared_ptr<DeviceTables> dev = device_tables(ctx);
     floatexp_tables(ctx, *dev);
     const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
     std::memset(static_cast<void*>(&p), 0, sizeof p);  // padding too: the bytes key the graph cache
+    p.formula = ctx.formula;
+    p.de_x = out.p_dex;
+    p.de_y = out.p_dey;
+    p.pixel_spacing = f32x::n_norm(static_cast<float>(g.pixel_spacing.m), g.pixel_spacing.e);
+    if (ctx.formula != kFormulaMandelbrot) {
+        // Alternate-formula policy (render_alternate_reference_impl,
+        // renderer.cpp:12116-12137): the 2x2 table whenever it exists, the
+        // series only for Julia.
+        p.orbit = dev->fx_orbit;
+        p.orbit_size = dev->orbit_size;
+        p.alt = dev->fx_alt;
+        p.linear_index = dev->fx_index + 3;
+        p.alt_start = ctx.alt_start;
+        p.alt_input_radius2 = f32x::n_norm(static_cast<float>(ctx.alt_input_radius2.m), ctx.alt_input_radius2.e);
+        p.parameter = f32x::norm(static_cast<float>(ctx.parameter.re), static_cast<float>(ctx.parameter.im),
+                                 ctx.parameter.e);
+        p.series = dev->fx_series;
+        p.series_terms = dev->series_terms;
+        p.series_iteration = ctx.series.iteration;
+        p.series_on = ctx.formula == kFormulaJulia && ctx.series.enabled && ctx.series.iteration < max_iter
+            && dev->series_terms > 1;
+        p.series_r2 = f32x::n_norm(static_cast<float>(ctx.series.r2.m), ctx.series.r2.e);
+        p.view_width = f32x::norm(static_cast<float>(g.view_width.m), 0.0f, g.view_width.e);
+        p.view_height = f32x::norm(static_cast<float>(g.view_height.m), 0.0f, g.view_height.e);
+        p.coordinate_mode = o.coordinate_mode;
+        p.width = width;
+        p.height = height;
+        p.max_iter = max_iter;
+        p.map_end = ctx.map_end;
+        p.disable_bla = o.disable_bla != 0 || !p.alt ? 1 : 0;
+        p.strict = o.strict;
+        p.allow_recovery = o.allow_recovery;
+        p.escape_mode = o.escape_radius_mode;
+        p.max_lin_len = std::clamp(static_cast<int>(o.max_linear_bla_length), 2, kMaxSafeLinearBlaLength);
+        p.output_bias = static_cast<float>(o.output_bias);
+        p.out = out.field;
+        p.counts = out.counts;
+        return true;
+    }
     if (fe_log10(zoom) < kShallowLog10Zoom) {
         if (dev->orbit_size < 2) return false;
         const double half_h = 0.5 * fx::scale2(g.view_height.m, g.view_height.e) + 0.05;
@@ -522,9 +568,9 @@ bool make_floatexp_params(ReferenceContext& ctx, const Outputs& out, int width, 
     p.orbit = dev->fx_orbit;
     p.orbit_size = dev->orbit_size;
     p.cubic = dev->fx_cubic;
-    p.cubic_index = dev->cubic_index;
+    p.cubic_index = dev->fx_index;
     p.linear = use_deep ? dev->fx_deep_linear : dev->fx_linear;
-    p.linear_index = use_deep ? dev->deep_linear_index : dev->linear_index;
+    p.linear_index = dev->fx_index + (use_deep ? 2 : 1);
     p.series = dev->fx_series;
     p.series_terms = dev->series_terms;
     p.series_iteration = ctx.series.iteration;
@@ -1465,7 +1511,7 @@ std::map<std::string, BatchShapes> tuned_shapes;  // by batch class
 // Everything one batch enqueues, resolved on the host first (tables
 // uploaded, zooms parsed) so the enqueue itself can be captured in a graph.
 struct BatchPlan {
-    std::map<int, std::vector<DirectParams>> direct;  // by formula
+    std::map<int, std::vector<DirectParams>> direct;  // by formula, | 0x100 for fields with planes
     std::vector<FxParams> floatexp;
     std::vector<float> log_zoom;       // per floatexp field (tile features)
     unsigned tile_flags = 0;           // FRACTAL_GB300_BATCH_TILES / _LEARNED / _PROBE
@@ -1518,7 +1564,12 @@ TileBuffers tile_buffers(char* base, int tiles, int rows) {
 
 void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime& rt, cudaStream_t main,
                    void* direct_scratch, unsigned long long* counter) {
-    const bool fork = !plan.direct.empty() && (!plan.floatexp.empty() || !plan.plain.empty());
+    // The direct queue runs on the second stream beside the other launches;
+    // with an FP32 queue in the batch the plain-form (FP64) launches join it
+    // there, so the FP64 and FP32 pipes work at once.
+    const bool fork = (!plan.direct.empty() && (!plan.floatexp.empty() || !plan.plain.empty()))
+        || (!plan.plain.empty() && !plan.floatexp.empty());
+    cudaStream_t plain_stream = fork && !plan.floatexp.empty() ? rt.side : main;
     cudaStream_t direct_stream = fork ? rt.side : main;
     if (fork) {
         check_cuda(cudaEventRecord(rt.fork, main), "cudaEventRecord (fork)");
@@ -1573,7 +1624,7 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
                        "floatexp batch launch");
         }
     }
-    for (const auto& launch : plan.plain) launch(main);
+    for (const auto& launch : plan.plain) launch(plain_stream);
     if (fork) {
         check_cuda(cudaEventRecord(rt.join, rt.side), "cudaEventRecord (join)");
         check_cuda(cudaStreamWaitEvent(main, rt.join, 0), "cudaStreamWaitEvent (join)");
@@ -1640,20 +1691,21 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
     cudaEvent_t a = nullptr, b = nullptr;
     check_cuda(cudaEventCreate(&a), "cudaEventCreate");
     check_cuda(cudaEventCreate(&b), "cudaEventCreate");
+    int repeats = 3;  // median of three; one run each for batches of a second or more
     auto time = [&](const BatchShapes& shapes) {
         float runs[3];
-        for (float& ms : runs) {
+        for (int r = 0; r < repeats; ++r) {
             check_cuda(cudaEventRecord(a, stream), "cudaEventRecord");
             launch_plan(plan, shapes, rt, stream, graph);
             check_cuda(cudaEventRecord(b, stream), "cudaEventRecord");
             check_cuda(cudaEventSynchronize(b), "cudaEventSynchronize");
-            check_cuda(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+            check_cuda(cudaEventElapsedTime(&runs[r], a, b), "cudaEventElapsedTime");
         }
-        std::sort(runs, runs + 3);
-        return runs[1];
+        std::sort(runs, runs + repeats);
+        return runs[repeats / 2];
     };
     try {
-        time(best);  // warm-up (occupancy queries, graph capture, caches)
+        if (time(best) >= 1000.0f) repeats = 1;  // warm-up (occupancy queries, graph capture, caches)
         float best_ms = time(best);
         auto sweep = [&](const std::vector<BatchShapes>& candidates) {
             for (const BatchShapes& c : candidates) {
@@ -1723,11 +1775,262 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
     return best;
 }
 
+// Zoom (log10) from which a direct-path frame keeps the FP64 direct iteration
+// in the floatexp form: there FP64's 2^-53 resolution leaves fewer than about
+// ten bits below a 1080-row pixel, so the FP64 counts are decided by FP64
+// rounding and only FP64 reproduces them.
+constexpr long double kShallowFp64Log10Zoom = 10.0L;
+
+// Whether the floatexp form renders a direct-path frame (FRACTAL_GB300_
+// KEYFRAME_SHALLOW) by FP32 perturbation: Mandelbrot only, below 1e10, and
+// only where a 16:9 view does not reach the main cardioid's or period-2
+// bulb's bounding box (near those parabolic boundaries a 1e-4-pixel error in
+// c moves many escape counts).  atlas.shallow_perturbation is the same rule.
+bool shallow_perturbs(const ReferenceContext& ctx, const char* zoom_text, const FractalRenderOptions& o) {
+    if (ctx.formula != kFormulaMandelbrot) return false;
+    const long double zoom = parse_zoom_direct(zoom_text);
+    if (!(zoom > 0.0L) || std::log10(zoom) >= kShallowFp64Log10Zoom) return false;
+    const double span = viewport_height_factor(o.coordinate_mode) / static_cast<double>(zoom);
+    const double half_h = 0.5 * span + 0.05;
+    const double half_w = 0.5 * span * (16.0 / 9.0) + 0.05;
+    const double x = static_cast<double>(ctx.x_center), y = static_cast<double>(ctx.y_center);
+    const bool cardioid = x + half_w >= -0.80 && x - half_w <= 0.40 && y + half_h >= -0.70 && y - half_h <= 0.70;
+    const bool bulb = x + half_w >= -1.30 && x - half_w <= -0.70 && y + half_h >= -0.30 && y - half_h <= 0.30;
+    return !(cardioid || bulb);
+}
+
+// One field of a batch: device outputs (derivative planes optional), its
+// view and the reference handle it renders from.
+struct FieldRequest {
+    Outputs out;
+    const char* zoom_text = nullptr;
+    void* reference = nullptr;
+    int width = 0;
+    int height = 0;
+    int max_iter = 0;
+    int flags = 0;
+};
+
+// The batch behind fractal_gb300_render_keyframes_device and
+// fractal_gb300_render_fields_device: every field resolved on the host
+// (zooms parsed, tables uploaded), then one enqueue -- the direct fields in
+// the FP64 lane-refill queue on the second stream (one launch per formula and
+// plane set), the floatexp fields of every formula and size in one
+// persistent FP32 queue, plain-form deep fields one launch each -- optionally
+// captured into a CUDA graph and autotuned.
+void render_field_batch(const std::vector<FieldRequest>& fields, const char* x_center, const char* y_center,
+                        int series_order, int series_block, const FractalRenderOptions* supplied, int form,
+                        unsigned flags, void* stream_handle) {
+    if (fields.empty() || !valid_series(series_order, series_block) || (form != 0 && form != 1)) {
+        throw Failure{"invalid native keyframe batch"};
+    }
+    const FractalRenderOptions o = checked_options(supplied);
+    check_backend(o);
+    ThreadRuntime& rt = thread_runtime();
+    cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
+    BatchPlan plan;
+    plan.fast_smooth = form == 1;
+    append_bytes(plan.key, form);
+    std::size_t direct_doubles = 0;
+    bool centre_parsed = false;
+    long double cx = 0.0L, cy = 0.0L;
+    // Planes no caller asked for but the plain kernels write (they take all
+    // six or none): one shared discard region sized for the largest field.
+    long long plane_pixels = 0;
+    for (std::size_t i = 0; i < fields.size(); ++i) {
+        const FieldRequest& f = fields[i];
+        if (!f.out.field || !f.zoom_text || !valid_iterations(f.max_iter) || !valid_dims(f.width, f.height)) {
+            throw Failure{"invalid native keyframe " + std::to_string(i)};
+        }
+        if ((f.flags & ~FRACTAL_GB300_KEYFRAME_SHALLOW) != 0) {
+            throw Failure{"invalid native keyframe " + std::to_string(i) + " flags"};
+        }
+        if (f.out.p_dex) plane_pixels = std::max(plane_pixels, static_cast<long long>(f.width) * f.height);
+    }
+    Outputs discard;
+    if (plane_pixels > 0) {
+        auto* base = static_cast<char*>(scratch(rt, kScratchDiscard, static_cast<std::size_t>(plane_pixels) * 32));
+        discard.p_iter = reinterpret_cast<std::int64_t*>(base);
+        discard.p_phase = reinterpret_cast<double*>(base + plane_pixels * 8);
+        discard.p_t1 = reinterpret_cast<double*>(base + plane_pixels * 16);
+        discard.p_t2 = reinterpret_cast<double*>(base + plane_pixels * 24);
+    }
+    // All six planes for the plain kernels: the caller's derivative planes,
+    // the rest into the discard region.
+    auto plain_outputs = [&](const Outputs& out) {
+        Outputs full = out;
+        if (out.p_dex) {
+            full.p_iter = discard.p_iter;
+            full.p_phase = discard.p_phase;
+            full.p_t1 = discard.p_t1;
+            full.p_t2 = discard.p_t2;
+        }
+        return full;
+    };
+    auto direct_group = [](int formula, const Outputs& out) { return formula | (out.p_dex ? 0x100 : 0); };
+    for (std::size_t i = 0; i < fields.size(); ++i) {
+        const FieldRequest& frame = fields[i];
+        const int width = frame.width, height = frame.height;
+        const bool shallow = (frame.flags & FRACTAL_GB300_KEYFRAME_SHALLOW) != 0;
+        if (!frame.reference) {
+            if (!centre_parsed) {
+                if (!x_center || !y_center) throw Failure{"keyframe batch without a centre for direct frames"};
+                cx = parse_coordinate(x_center, "real");
+                cy = parse_coordinate(y_center, "imaginary");
+                centre_parsed = true;
+            }
+            const Outputs out = plain_outputs(frame.out);
+            auto& group = plan.direct[direct_group(kFormulaMandelbrot, out)];
+            group.push_back(make_direct_params(out, width, height, parse_zoom_direct(frame.zoom_text), cx, cy,
+                                               frame.max_iter, kFormulaMandelbrot, 0.0, 0.0, o));
+            direct_doubles += static_cast<std::size_t>(width) + height;
+            append_bytes(plan.key, group.back());
+            continue;
+        }
+        std::shared_ptr<ReferenceContext> ctx = acquire_reference(frame.reference);
+        if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
+        if (ctx->escape_mode != o.escape_radius_mode) {
+            throw Failure{"reference escape-radius mode does not match render options"};
+        }
+        if (frame.max_iter > ctx->requested_max_iter) {
+            throw Failure{"render iteration count exceeds prepared reference"};
+        }
+        plan.contexts.push_back(ctx);
+        // A shallow frame stays on the FP64 direct path (at its reference's
+        // centre) in form 0, and in form 1 wherever the shallow mode would
+        // not reproduce the FP64 counts within the floatexp budget.
+        const bool direct_path = shallow && (form == 0 || !shallow_perturbs(*ctx, frame.zoom_text, o));
+        FxParams fx;
+        if (form == 1 && !direct_path
+            && make_floatexp_params(*ctx, frame.out, width, height, frame.zoom_text, frame.max_iter, series_order,
+                                    series_block, o, fx, (flags & FRACTAL_GB300_BATCH_FP32_ALTERNATES) != 0)) {
+            plan.floatexp.push_back(fx);
+            plan.log_zoom.push_back(static_cast<float>(fe_log10(parse_zoom_fe(frame.zoom_text,
+                                                                              ctx->precision_bits))));
+            append_bytes(plan.key, fx);
+            continue;
+        }
+        const fx::Fe zoom = parse_zoom_fe(frame.zoom_text, ctx->precision_bits);
+        const Outputs out = plain_outputs(frame.out);
+        if (fe_log10(zoom) < 6.0L || direct_path) {
+            auto& group = plan.direct[direct_group(ctx->formula, out)];
+            group.push_back(make_direct_params(out, width, height, parse_zoom_direct(frame.zoom_text), ctx->x_center,
+                                               ctx->y_center, frame.max_iter, ctx->formula, ctx->julia_re,
+                                               ctx->julia_im, o));
+            direct_doubles += static_cast<std::size_t>(width) + height;
+            append_bytes(plan.key, group.back());
+            continue;
+        }
+        std::shared_ptr<DeviceTables> dev = device_tables(*ctx);
+        ReferenceContext* raw = ctx.get();
+        const int max_iter = frame.max_iter;
+        plan.plain.push_back([raw, dev, out, width, height, zoom, max_iter, series_order, series_block, o,
+                              &rt](cudaStream_t s) {
+            if (raw->formula != kFormulaMandelbrot) {
+                launch_deep_alternate(*raw, *dev, out, width, height, zoom, max_iter, o, false, rt, s);
+            } else {
+                launch_deep_mandelbrot(*raw, *dev, out, width, height, zoom, max_iter, series_order,
+                                       series_block, o, false, rt, s);
+            }
+        });
+        append_bytes(plan.key, raw);
+        append_bytes(plan.key, raw->generation);
+        append_bytes(plan.key, out);
+        append_bytes(plan.key, zoom);
+        append_bytes(plan.key, max_iter);
+        append_bytes(plan.key, width);
+        append_bytes(plan.key, height);
+        append_bytes(plan.key, series_order);
+        append_bytes(plan.key, series_block);
+        append_bytes(plan.key, o);
+    }
+    for (const auto& group : plan.direct) {
+        const std::vector<DirectParams>& direct = group.second;
+        for (std::size_t i = 0; i < direct.size(); i += kMaxDirectFields) {
+            const int n = static_cast<int>(std::min<std::size_t>(kMaxDirectFields, direct.size() - i));
+            long long pixels = 0;
+            for (int f = 0; f < n; ++f) pixels += static_cast<long long>(direct[i + f].width) * direct[i + f].height;
+            plan.direct_bytes = std::max(plan.direct_bytes,
+                                         direct_scratch_bytes(direct.data() + i, n, spill_entries(pixels)));
+        }
+    }
+    if (!plan.floatexp.empty()) {
+        auto* slots = static_cast<FxSeriesScaled*>(
+            scratch(rt, kScratchSeries, sizeof(FxSeriesScaled) * plan.floatexp.size()));
+        for (std::size_t f = 0; f < plan.floatexp.size(); ++f) plan.floatexp[f].series_scaled = slots + f;
+        append_bytes(plan.key, slots);
+    }
+    plan.tile_flags = flags & (FRACTAL_GB300_BATCH_TILES | FRACTAL_GB300_BATCH_LEARNED | FRACTAL_GB300_BATCH_PROBE);
+    if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
+        if (plan.floatexp.size() > static_cast<std::size_t>(kMaxFxFields)) {
+            throw Failure{"tile-scheduled batches take at most 64 floatexp keyframes"};
+        }
+        plan.tiles = batch_tiles(plan.floatexp.data(), static_cast<int>(plan.floatexp.size()));
+        plan.feature_rows = (plan.tiles + 127) / 128 * 128;
+        if (plan.tile_flags & FRACTAL_GB300_BATCH_LEARNED) {
+            if (!rt.costnet) throw Failure{"learned tile order requested but no cost network is attached"};
+            plan.net = static_cast<mlp::CostNet*>(rt.costnet);
+            std::string why;
+            if (!mlp::reserve_rows(plan.net, plan.feature_rows, why)) throw Failure{why};
+            append_bytes(plan.key, plan.net);
+        }
+        scratch(rt, kScratchTiles, tile_buffers(nullptr, plan.tiles, plan.feature_rows).bytes);
+        append_bytes(plan.key, plan.tile_flags);
+        rt.tile_stream = stream;
+        rt.last_tiles = plan.tiles;
+    }
+    long long total_pixels = 0;
+    for (const FieldRequest& f : fields) total_pixels += static_cast<long long>(f.width) * f.height;
+    std::string shape_key;
+    append_bytes(shape_key, plan.tile_flags);
+    append_bytes(shape_key, total_pixels);
+    append_bytes(shape_key, form);
+    append_bytes(shape_key, static_cast<int>(plan.floatexp.size()));
+    append_bytes(shape_key, static_cast<int>(plan.plain.size()));
+    append_bytes(shape_key, static_cast<int>(direct_doubles));
+    BatchShapes shapes;
+    bool tuned = false;
+    {
+        std::lock_guard<std::mutex> lock(tuned_mutex);
+        auto known = tuned_shapes.find(shape_key);
+        if (known != tuned_shapes.end()) {
+            shapes = known->second;
+            tuned = true;
+        }
+    }
+    if (!tuned && !plan.direct.empty() && !plan.floatexp.empty()) {
+        // Both queues resident at once: split the SM's blocks between them.
+        const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
+        shapes.direct.blocks_per_sm = std::max(1, capacity / 2);
+        shapes.floatexp.blocks_per_sm = std::max(1, capacity - shapes.direct.blocks_per_sm);
+    }
+    if (rt.shapes_pinned) {
+        if (rt.pinned_shapes[0] > 0) shapes.direct.chunk = rt.pinned_shapes[0];
+        shapes.direct.blocks_per_sm = rt.pinned_shapes[1];
+        if (rt.pinned_shapes[2] > 0) shapes.floatexp.chunk = rt.pinned_shapes[2];
+        shapes.floatexp.blocks_per_sm = rt.pinned_shapes[3];
+    }
+    wait_scratch(rt, stream);
+    if ((flags & FRACTAL_GB300_BATCH_AUTOTUNE) && !rt.shapes_pinned) {
+        shapes = autotune(plan, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
+        std::lock_guard<std::mutex> lock(tuned_mutex);
+        tuned_shapes[shape_key] = shapes;
+    }
+    rt.batch_stream = stream;
+    rt.last_shapes[0] = shapes.direct.chunk;
+    rt.last_shapes[1] = shapes.direct.blocks_per_sm;
+    rt.last_shapes[2] = shapes.floatexp.chunk;
+    rt.last_shapes[3] = shapes.floatexp.blocks_per_sm;
+    launch_plan(plan, shapes, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
+    release_scratch(rt, stream);
+}
+
 }  // namespace
 
 extern "C" {
 
 int fractal_abi_version(void) { return FRACTAL_ABI_VERSION; }
+
 int fractal_render_options_version(void) { return FRACTAL_RENDER_OPTIONS_VERSION; }
 void fractal_render_options_default(FractalRenderOptions* options) {
     if (options) *options = default_options();
@@ -2380,174 +2683,49 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe* frames, in
                                           int series_block, const FractalRenderOptions* supplied, int form,
                                           unsigned flags, void* stream_handle) {
     return guarded("keyframe batch render failed with an unknown exception", [&] {
-        if (!frames || count <= 0 || !valid_dims(width, height) || !valid_series(series_order, series_block)
-            || (form != 0 && form != 1)) {
-            throw Failure{"invalid native keyframe batch"};
-        }
-        const FractalRenderOptions o = checked_options(supplied);
-        check_backend(o);
-        ThreadRuntime& rt = thread_runtime();
-        cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
-        BatchPlan plan;
-        plan.fast_smooth = form == 1;
-        append_bytes(plan.key, width);
-        append_bytes(plan.key, height);
-        append_bytes(plan.key, form);
-        std::size_t direct_doubles = 0;
-        bool centre_parsed = false;
-        long double cx = 0.0L, cy = 0.0L;
+        if (!frames || count <= 0 || !valid_dims(width, height)) throw Failure{"invalid native keyframe batch"};
+        std::vector<FieldRequest> fields(static_cast<std::size_t>(count));
         for (int i = 0; i < count; ++i) {
-            const FractalGb300Keyframe& frame = frames[i];
-            if (!frame.field || !frame.zoom_text || !valid_iterations(frame.max_iter)) {
-                throw Failure{"invalid native keyframe " + std::to_string(i)};
-            }
-            Outputs out;
-            out.field = frame.field;
-            out.counts = frame.counts;
-            const bool shallow = (frame.flags & FRACTAL_GB300_KEYFRAME_SHALLOW) != 0;
-            if ((frame.flags & ~FRACTAL_GB300_KEYFRAME_SHALLOW) != 0) {
-                throw Failure{"invalid native keyframe " + std::to_string(i) + " flags"};
-            }
-            if (!frame.reference || (shallow && form == 0)) {
-                if (!centre_parsed) {
-                    if (!x_center || !y_center) throw Failure{"keyframe batch without a centre for direct frames"};
-                    cx = parse_coordinate(x_center, "real");
-                    cy = parse_coordinate(y_center, "imaginary");
-                    centre_parsed = true;
-                }
-                plan.direct[kFormulaMandelbrot].push_back(make_direct_params(
-                    out, width, height, parse_zoom_direct(frame.zoom_text), cx, cy, frame.max_iter,
-                    kFormulaMandelbrot, 0.0, 0.0, o));
-                direct_doubles += static_cast<std::size_t>(width) + height;
-                append_bytes(plan.key, plan.direct[kFormulaMandelbrot].back());
-                continue;
-            }
-            std::shared_ptr<ReferenceContext> ctx = acquire_reference(frame.reference);
-            if (!ctx) throw Failure{"invalid or already-destroyed reference handle"};
-            if (ctx->escape_mode != o.escape_radius_mode) {
-                throw Failure{"reference escape-radius mode does not match render options"};
-            }
-            if (frame.max_iter > ctx->requested_max_iter) {
-                throw Failure{"render iteration count exceeds prepared reference"};
-            }
-            plan.contexts.push_back(ctx);
-            FxParams fx;
-            if (form == 1 && make_floatexp_params(*ctx, out, width, height, frame.zoom_text, frame.max_iter,
-                                                  series_order, series_block, o, fx)) {
-                plan.floatexp.push_back(fx);
-                plan.log_zoom.push_back(static_cast<float>(fe_log10(parse_zoom_fe(frame.zoom_text,
-                                                                                  ctx->precision_bits))));
-                append_bytes(plan.key, fx);
-                continue;
-            }
-            const fx::Fe zoom = parse_zoom_fe(frame.zoom_text, ctx->precision_bits);
-            if (fe_log10(zoom) < 6.0L || shallow) {
-                plan.direct[ctx->formula].push_back(make_direct_params(
-                    out, width, height, parse_zoom_direct(frame.zoom_text), ctx->x_center, ctx->y_center,
-                    frame.max_iter, ctx->formula, ctx->julia_re, ctx->julia_im, o));
-                direct_doubles += static_cast<std::size_t>(width) + height;
-                append_bytes(plan.key, plan.direct[ctx->formula].back());
-                continue;
-            }
-            std::shared_ptr<DeviceTables> dev = device_tables(*ctx);
-            ReferenceContext* raw = ctx.get();
-            const int max_iter = frame.max_iter;
-            plan.plain.push_back([raw, dev, out, width, height, zoom, max_iter, series_order, series_block, o,
-                                  &rt](cudaStream_t s) {
-                if (raw->formula != kFormulaMandelbrot) {
-                    launch_deep_alternate(*raw, *dev, out, width, height, zoom, max_iter, o, false, rt, s);
-                } else {
-                    launch_deep_mandelbrot(*raw, *dev, out, width, height, zoom, max_iter, series_order,
-                                           series_block, o, false, rt, s);
-                }
-            });
-            append_bytes(plan.key, raw);
-            append_bytes(plan.key, raw->generation);
-            append_bytes(plan.key, out);
-            append_bytes(plan.key, zoom);
-            append_bytes(plan.key, max_iter);
-            append_bytes(plan.key, series_order);
-            append_bytes(plan.key, series_block);
-            append_bytes(plan.key, o);
+            FieldRequest& f = fields[static_cast<std::size_t>(i)];
+            f.out.field = frames[i].field;
+            f.out.counts = frames[i].counts;
+            f.zoom_text = frames[i].zoom_text;
+            f.reference = frames[i].reference;
+            f.width = width;
+            f.height = height;
+            f.max_iter = frames[i].max_iter;
+            f.flags = frames[i].flags;
         }
-        for (const auto& group : plan.direct) {
-            const std::vector<DirectParams>& fields = group.second;
-            for (std::size_t i = 0; i < fields.size(); i += kMaxDirectFields) {
-                const int n = static_cast<int>(std::min<std::size_t>(kMaxDirectFields, fields.size() - i));
-                long long pixels = 0;
-                for (int f = 0; f < n; ++f) pixels += static_cast<long long>(fields[i + f].width) * fields[i + f].height;
-                plan.direct_bytes = std::max(plan.direct_bytes,
-                                             direct_scratch_bytes(fields.data() + i, n, spill_entries(pixels)));
+        render_field_batch(fields, x_center, y_center, series_order, series_block, supplied, form, flags,
+                           stream_handle);
+    });
+}
+
+int fractal_gb300_render_fields_device(const FractalGb300Field* frames, int count, const char* x_center,
+                                       const char* y_center, int series_order, int series_block,
+                                       const FractalRenderOptions* supplied, int form, unsigned flags,
+                                       void* stream_handle) {
+    return guarded("field batch render failed with an unknown exception", [&] {
+        if (!frames || count <= 0) throw Failure{"invalid native field batch"};
+        std::vector<FieldRequest> fields(static_cast<std::size_t>(count));
+        for (int i = 0; i < count; ++i) {
+            FieldRequest& f = fields[static_cast<std::size_t>(i)];
+            if ((frames[i].de_x == nullptr) != (frames[i].de_y == nullptr)) {
+                throw Failure{"native field " + std::to_string(i) + " names one derivative plane without the other"};
             }
+            f.out.field = frames[i].field;
+            f.out.counts = frames[i].counts;
+            f.out.p_dex = frames[i].de_x;
+            f.out.p_dey = frames[i].de_y;
+            f.zoom_text = frames[i].zoom_text;
+            f.reference = frames[i].reference;
+            f.width = frames[i].width;
+            f.height = frames[i].height;
+            f.max_iter = frames[i].max_iter;
+            f.flags = frames[i].flags;
         }
-        if (!plan.floatexp.empty()) {
-            auto* slots = static_cast<FxSeriesScaled*>(
-                scratch(rt, kScratchSeries, sizeof(FxSeriesScaled) * plan.floatexp.size()));
-            for (std::size_t f = 0; f < plan.floatexp.size(); ++f) plan.floatexp[f].series_scaled = slots + f;
-            append_bytes(plan.key, slots);
-        }
-        plan.tile_flags = flags & (FRACTAL_GB300_BATCH_TILES | FRACTAL_GB300_BATCH_LEARNED | FRACTAL_GB300_BATCH_PROBE);
-        if (plan.tile_flags != 0 && !plan.floatexp.empty()) {
-            if (plan.floatexp.size() > static_cast<std::size_t>(kMaxFxFields)) {
-                throw Failure{"tile-scheduled batches take at most 64 floatexp keyframes"};
-            }
-            plan.tiles = batch_tiles(plan.floatexp.data(), static_cast<int>(plan.floatexp.size()));
-            plan.feature_rows = (plan.tiles + 127) / 128 * 128;
-            if (plan.tile_flags & FRACTAL_GB300_BATCH_LEARNED) {
-                if (!rt.costnet) throw Failure{"learned tile order requested but no cost network is attached"};
-                plan.net = static_cast<mlp::CostNet*>(rt.costnet);
-                std::string why;
-                if (!mlp::reserve_rows(plan.net, plan.feature_rows, why)) throw Failure{why};
-                append_bytes(plan.key, plan.net);
-            }
-            scratch(rt, kScratchTiles, tile_buffers(nullptr, plan.tiles, plan.feature_rows).bytes);
-            append_bytes(plan.key, plan.tile_flags);
-            rt.tile_stream = stream;
-            rt.last_tiles = plan.tiles;
-        }
-        std::string shape_key;
-        append_bytes(shape_key, plan.tile_flags);
-        append_bytes(shape_key, width);
-        append_bytes(shape_key, height);
-        append_bytes(shape_key, form);
-        append_bytes(shape_key, static_cast<int>(plan.floatexp.size()));
-        append_bytes(shape_key, static_cast<int>(plan.plain.size()));
-        append_bytes(shape_key, static_cast<int>(direct_doubles));
-        BatchShapes shapes;
-        bool tuned = false;
-        {
-            std::lock_guard<std::mutex> lock(tuned_mutex);
-            auto known = tuned_shapes.find(shape_key);
-            if (known != tuned_shapes.end()) {
-                shapes = known->second;
-                tuned = true;
-            }
-        }
-        if (!tuned && !plan.direct.empty() && !plan.floatexp.empty()) {
-            // Both queues resident at once: split the SM's blocks between them.
-            const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
-            shapes.direct.blocks_per_sm = std::max(1, capacity / 2);
-            shapes.floatexp.blocks_per_sm = std::max(1, capacity - shapes.direct.blocks_per_sm);
-        }
-        if (rt.shapes_pinned) {
-            if (rt.pinned_shapes[0] > 0) shapes.direct.chunk = rt.pinned_shapes[0];
-            shapes.direct.blocks_per_sm = rt.pinned_shapes[1];
-            if (rt.pinned_shapes[2] > 0) shapes.floatexp.chunk = rt.pinned_shapes[2];
-            shapes.floatexp.blocks_per_sm = rt.pinned_shapes[3];
-        }
-        wait_scratch(rt, stream);
-        if ((flags & FRACTAL_GB300_BATCH_AUTOTUNE) && !rt.shapes_pinned) {
-            shapes = autotune(plan, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
-            std::lock_guard<std::mutex> lock(tuned_mutex);
-            tuned_shapes[shape_key] = shapes;
-        }
-        rt.batch_stream = stream;
-        rt.last_shapes[0] = shapes.direct.chunk;
-        rt.last_shapes[1] = shapes.direct.blocks_per_sm;
-        rt.last_shapes[2] = shapes.floatexp.chunk;
-        rt.last_shapes[3] = shapes.floatexp.blocks_per_sm;
-        launch_plan(plan, shapes, rt, stream, (flags & FRACTAL_GB300_BATCH_GRAPH) != 0);
-        release_scratch(rt, stream);
+        render_field_batch(fields, x_center, y_center, series_order, series_block, supplied, form, flags,
+                           stream_handle);
     });
 }
 
@@ -2619,6 +2797,15 @@ int fractal_gb300_last_direct_steps(unsigned long long* steps) {
         check_cuda(cudaMemcpy(&error, counters + kQueueError, sizeof error, cudaMemcpyDeviceToHost),
                    "direct queue status");
         if (error) throw Failure{"direct queue: a spilled pixel was never published (render incomplete)"};
+    });
+}
+
+int fractal_gb300_set_direct_fault_injection(int spin_limit, int withhold_publish) {
+    return guarded("setting the direct queue's fault injection failed", [&] {
+        if (spin_limit < 0 || spin_limit > (1 << 22) || (withhold_publish != 0 && withhold_publish != 1)) {
+            throw Failure{"direct queue fault injection out of range"};
+        }
+        set_direct_fault_injection(spin_limit, withhold_publish);
     });
 }
 

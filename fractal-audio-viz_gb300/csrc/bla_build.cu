@@ -136,6 +136,21 @@ __global__ void fx_linear_kernel(const LinearStep* in, FxLinear* out, int count)
     out[i] = l;
 }
 
+__global__ void fx_alt_kernel(const AltStep* in, FxAltStep* out, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    FxAltStep a;
+    for (int k = 0; k < 8; ++k) {
+        const fx::Fe v = in[i].c[k];
+        a.c[k] = fx::fe_finite(v) ? f32x::r_norm(static_cast<float>(v.m), v.e)
+                                  : f32x::r_make(v.m < 0.0 ? -3.0e38f : 3.0e38f, 0x3fffffff);
+    }
+    a.r2 = fe_to_n1e(in[i].r2);
+    a.len = in[i].len;
+    a.pad = 0;
+    out[i] = a;
+}
+
 template <typename T>
 T* device_alloc(std::size_t count, const char* what) {
     T* p = nullptr;
@@ -332,12 +347,17 @@ void convert_fx_levels(DeviceTables& dev, cudaStream_t stream) {
     const int nc = total(dev.cubic_index);
     const int nl = total(dev.linear_index);
     const int nd = total(dev.deep_linear_index);
+    const int na = total(dev.alt_index);
     dev.fx_cubic = device_alloc<FxCubic>(static_cast<std::size_t>(nc), "cudaMalloc (FP32 cubic BLA)");
     dev.fx_linear = device_alloc<FxLinear>(static_cast<std::size_t>(nl), "cudaMalloc (FP32 linear BLA)");
     dev.fx_deep_linear = device_alloc<FxLinear>(static_cast<std::size_t>(nd), "cudaMalloc (FP32 linear BLA)");
     if (nc) fx_cubic_kernel<<<blocks_for(nc), kThreads, 0, stream>>>(dev.cubic, dev.fx_cubic, nc);
     if (nl) fx_linear_kernel<<<blocks_for(nl), kThreads, 0, stream>>>(dev.linear, dev.fx_linear, nl);
     if (nd) fx_linear_kernel<<<blocks_for(nd), kThreads, 0, stream>>>(dev.deep_linear, dev.fx_deep_linear, nd);
+    if (na) {
+        dev.fx_alt = device_alloc<FxAltStep>(static_cast<std::size_t>(na), "cudaMalloc (FP32 alternate BLA)");
+        fx_alt_kernel<<<blocks_for(na), kThreads, 0, stream>>>(dev.alt, dev.fx_alt, na);
+    }
     check_cuda(cudaGetLastError(), "FP32 table conversion");
     check_cuda(cudaStreamSynchronize(stream), "FP32 table conversion");
 }

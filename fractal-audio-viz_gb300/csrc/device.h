@@ -32,7 +32,18 @@ struct LevelIndex {
 struct FxOrbitRec {
     float zr, zi;  // Z_i as plain float (0 below the float range)
     f32x::F2e z;   // Z_i as floatexp
-    f32x::N1e z2;  // |Z_i|^2
+    // Mandelbrot references: |Z_i|^2.  Other formulas: the signed escape
+    // margin |Z_i|^2 - R^2 from the MPFR orbit (read as an f32x::R1e).
+    f32x::N1e z2;
+    int pad;
+};
+
+// FP32 mirror of AltStep: the real 2x2 maps d' = M d + P c, coefficients
+// c[0..3] = M (row-major), c[4..7] = P, and the squared validity radius.
+struct FxAltStep {
+    f32x::R1e c[8];
+    f32x::N1e r2;
+    int len;
     int pad;
 };
 
@@ -71,7 +82,12 @@ struct DeviceTables {
     FxCubic* fx_cubic = nullptr;
     FxLinear* fx_linear = nullptr;
     FxLinear* fx_deep_linear = nullptr;
+    FxAltStep* fx_alt = nullptr;
     f32x::F2e* fx_series = nullptr;
+    // Device copies of the level indexes for the floatexp kernels, which
+    // take them by pointer (the batched queue's parameters hold 64 fields):
+    // [0] cubic, [1] linear, [2] deep linear, [3] alternate.
+    LevelIndex* fx_index = nullptr;
     ~DeviceTables();
 };
 
@@ -306,9 +322,9 @@ struct FxParams {
     const FxOrbitRec* orbit;
     int orbit_size;
     const FxCubic* cubic;
-    LevelIndex cubic_index;
+    const LevelIndex* cubic_index;   // device copies (DeviceTables::fx_index)
     const FxLinear* linear;
-    LevelIndex linear_index;
+    const LevelIndex* linear_index;
     const f32x::F2e* series;
     int series_terms;
     int series_iteration;
@@ -341,6 +357,21 @@ struct FxParams {
     int interior_test;
     float centre_re;  // the view centre rounded to float (interior test only)
     float centre_im;
+    // Other formulas (kFormulaJulia / BurningShip / Tricorn): the FP32 2x2
+    // hierarchy `alt` (its levels indexed by linear_index), the reference
+    // index its level 0 starts at, the bound on |c|^2 for using it, and the
+    // parameter (Julia's c; the reference's c for the parameter planes).
+    int formula;
+    const FxAltStep* alt;
+    int alt_start;
+    f32x::N1e alt_input_radius2;
+    f32x::F2e parameter;
+    // Derivative planes (optional, both or neither): the analytic distance
+    // estimate (render_plane_de, renderer.cpp:7844-7990) per pixel, and the
+    // pixel spacing it is measured in.
+    double* de_x;
+    double* de_y;
+    f32x::N1e pixel_spacing;
 };
 
 cudaError_t launch_floatexp_mandelbrot(const FxParams& params, cudaStream_t stream);
@@ -452,7 +483,16 @@ struct DirectBatch {
     int fast_smooth;                        // smooth value in FP32 (floatexp form's direct levels)
     DirectSpill* spill;
     long long spill_capacity;
+    // Bound on a consumer's wait for a spilled entry's generation mark (then
+    // kQueueError is set and the entry is dropped), and a fault-injection
+    // switch for tests: spilled entries are written but never published.
+    int spin_limit;
+    int withhold_publish;
 };
+// Spill-wait bound and publish suppression of the calling thread's next
+// direct launches (tests of the queue's error path); 0, 0 restores the
+// defaults (1 << 22 spins, publish).
+void set_direct_fault_injection(int spin_limit, int withhold_publish);
 // Device scratch for one batch: counters, coordinate tables and a spill list
 // of `spill_entries` (0: no spilling).
 std::size_t direct_scratch_bytes(const DirectParams* fields, int count, long long spill_entries);

@@ -31,7 +31,9 @@ DeviceTables::~DeviceTables() {
     cudaFree(fx_cubic);
     cudaFree(fx_linear);
     cudaFree(fx_deep_linear);
+    cudaFree(fx_alt);
     cudaFree(fx_series);
+    cudaFree(fx_index);
     if (device >= 0 && current >= 0 && current != device) cudaSetDevice(current);
 }
 
@@ -78,6 +80,11 @@ f32x::N1e to_n1e(const fx::Fe& v) {
     return f32x::n_norm(static_cast<float>(v.m), v.e);
 }
 
+f32x::R1e to_r1e(const fx::Fe& v) {
+    if (!fx::fe_finite(v)) return f32x::r_make(v.m < 0.0 ? -3.0e38f : 3.0e38f, 0x3fffffff);
+    return f32x::r_norm(static_cast<float>(v.m), v.e);
+}
+
 float plain_float(double mantissa, int exponent) {
     const double v = fx::scale2(mantissa, exponent);
     const double a = v < 0 ? -v : v;
@@ -103,8 +110,12 @@ void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
         r.zr = plain_float(z.re, z.e);
         r.zi = plain_float(z.im, z.e);
         r.z = to_f2e(z);
-        const fx::Nrm n = fx::sc_norm2(z);
-        r.z2 = to_n1e(fx::fe_make(n.m, n.e));
+        if (ctx.formula == kFormulaMandelbrot) {
+            const fx::Nrm n = fx::sc_norm2(z);
+            r.z2 = to_n1e(fx::fe_make(n.m, n.e));
+        } else {
+            r.z2 = f32x::n_from_r(to_r1e(i < orbit.escape_margin.size() ? orbit.escape_margin[i] : fx::Fe{0.0, 0}));
+        }
     }
     dev.fx_orbit = upload(records);
     auto cubic_levels = [&](const std::vector<std::vector<CubicStep>>& levels) {
@@ -136,6 +147,20 @@ void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
         }
         return out;
     };
+    auto alt_levels = [&](const std::vector<std::vector<AltStep>>& levels) {
+        std::vector<std::vector<FxAltStep>> out;
+        for (const auto& level : levels) {
+            auto& dst = out.emplace_back();
+            for (const AltStep& s : level) {
+                FxAltStep a{};
+                for (int k = 0; k < 8; ++k) a.c[k] = to_r1e(s.c[k]);
+                a.r2 = to_n1e(s.r2);
+                a.len = s.len;
+                dst.push_back(a);
+            }
+        }
+        return out;
+    };
     if (ctx.bla_on_device) {
         convert_fx_levels(dev, thread_runtime().stream);
     } else {
@@ -143,7 +168,11 @@ void floatexp_tables(ReferenceContext& ctx, DeviceTables& dev) {
         dev.fx_cubic = upload_levels(cubic_levels(ctx.cubic), unused);
         dev.fx_linear = upload_levels(linear_levels(ctx.linear), unused);
         dev.fx_deep_linear = upload_levels(linear_levels(ctx.deep_linear), unused);
+        dev.fx_alt = upload_levels(alt_levels(ctx.alt), unused);
     }
+    const std::vector<LevelIndex> indexes = {dev.cubic_index, dev.linear_index, dev.deep_linear_index,
+                                             dev.alt_index};
+    dev.fx_index = upload(indexes);
     std::vector<f32x::F2e> series;
     for (const fx::Sc& c : ctx.series.coeff) series.push_back(to_f2e(c));
     dev.fx_series = upload(series);

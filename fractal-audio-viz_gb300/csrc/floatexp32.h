@@ -170,6 +170,94 @@ F32_HD int n_cmp(const N1e& a, const N1e& b) {
     return (a.m > b.m) - (a.m < b.m);
 }
 
+// Signed real (m * 2^e, |m| in [0.5, 1), or zero): the components of the
+// alternate formulas' 2x2 maps, escape margins and Jacobians.
+struct R1e {
+    float m;
+    int e;
+};
+
+F32_HD R1e r_make(float m, int e) {
+    R1e r;
+    r.m = m;
+    r.e = e;
+    return r;
+}
+
+F32_HD R1e r_zero() { return r_make(0.0f, 0); }
+
+F32_HD R1e r_norm(float m, int e) {
+    if (m == 0.0f) return r_zero();
+    int b = f_bits(m) & 0x7fffffff;
+    if (b >= 0x7f800000) return r_make(m, 0x3fffffff);
+    int be = b >> 23;
+    if (be == 0) {  // subnormal: lift by 2^24 first
+        m *= 16777216.0f;
+        e -= 24;
+        b = f_bits(m) & 0x7fffffff;
+        be = b >> 23;
+    }
+    const int shift = be - 126;
+    return shift == 0 ? r_make(m, e) : r_make(m * pow2f(-shift), e + shift);
+}
+
+F32_HD bool r_finite(const R1e& a) { return (f_bits(a.m) & 0x7f800000) != 0x7f800000; }
+F32_HD R1e r_neg(const R1e& a) { return r_make(-a.m, a.e); }
+F32_HD R1e r_abs(const R1e& a) { return r_make(a.m < 0.0f ? -a.m : a.m, a.e); }
+
+F32_HD R1e r_add(const R1e& a, const R1e& b) {
+    if (a.m == 0.0f) return b;
+    if (b.m == 0.0f) return a;
+    const R1e& hi = b.e > a.e ? b : a;
+    const R1e& lo = b.e > a.e ? a : b;
+    const int d = hi.e - lo.e;
+    if (d > 40) return hi;
+    return r_norm(hi.m + lo.m * pow2f(-d), hi.e);
+}
+
+F32_HD R1e r_sub(const R1e& a, const R1e& b) { return r_add(a, r_neg(b)); }
+
+F32_HD R1e r_mul(const R1e& a, const R1e& b) {
+    if (a.m == 0.0f || b.m == 0.0f) return r_zero();
+    return r_norm(a.m * b.m, a.e + b.e);
+}
+
+// a * s for a small constant s (2, -2, +-1).
+F32_HD R1e r_scale(const R1e& a, float s) { return a.m == 0.0f ? a : r_norm(a.m * s, a.e); }
+
+F32_HD int r_sign(const R1e& a) { return (a.m > 0.0f) - (a.m < 0.0f); }
+
+// Signed comparison.
+F32_HD int r_cmp(const R1e& a, const R1e& b) {
+    const int sa = r_sign(a), sb = r_sign(b);
+    if (sa != sb) return sa < sb ? -1 : 1;
+    if (sa == 0) return 0;
+    if (a.e != b.e) return (a.e < b.e ? -1 : 1) * sa;
+    return (a.m > b.m) - (a.m < b.m);
+}
+
+F32_HD R1e r_re(const F2e& z) { return r_norm(z.x, z.e); }
+F32_HD R1e r_im(const F2e& z) { return r_norm(z.y, z.e); }
+
+// Complex value from two reals (shared exponent, then normalised).
+F32_HD F2e from_r(const R1e& re, const R1e& im) {
+    if (re.m == 0.0f && im.m == 0.0f) return zero();
+    if (re.m == 0.0f) return norm(0.0f, im.m, im.e);
+    if (im.m == 0.0f) return norm(re.m, 0.0f, re.e);
+    const int e = re.e > im.e ? re.e : im.e;
+    const int dr = re.e - e, di = im.e - e;
+    return norm(dr < -126 ? 0.0f : re.m * pow2f(dr), di < -126 ? 0.0f : im.m * pow2f(di), e);
+}
+
+F32_HD N1e n_from_r(const R1e& a) {
+    N1e r;
+    r.m = a.m;
+    r.e = a.e;
+    return r;
+}
+
+F32_HD F2e conj(const F2e& a) { return make(a.x, -a.y, a.e); }
+
 // Plain float value of a (0 when below the float range, +-inf above).
 F32_HD float to_float_x(const F2e& a) { return ldexpf_fast(a.x, a.e); }
 F32_HD float to_float_y(const F2e& a) { return ldexpf_fast(a.y, a.e); }

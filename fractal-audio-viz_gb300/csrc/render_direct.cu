@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                 // (bounded) for its generation mark.
                 const DirectSpill& e = b.spill[base + rank];
                 bool ready = false;
-                for (int spin = 0; spin < (1 << 22); ++spin) {
+                for (int spin = 0; spin < b.spin_limit; ++spin) {
                     if (*reinterpret_cast<const volatile unsigned long long*>(&e.ready) == generation) {
                         ready = true;
                         break;
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant
                     e.field = l.field;
                     e.local = l.local;
                     __threadfence();
-                    *reinterpret_cast<volatile unsigned long long*>(&e.ready) = generation;
+                    if (!b.withhold_publish) *reinterpret_cast<volatile unsigned long long*>(&e.ready) = generation;
                     active = false;
                 } else {
                     l.stop_at = l.max_iter;
@@ -833,10 +833,23 @@ static bool view_meets_interior(const DirectParams& p) {
     return cardioid || bulb;
 }
 
+namespace {
+constexpr int kDefaultSpinLimit = 1 << 22;
+thread_local int fault_spin_limit = kDefaultSpinLimit;
+thread_local int fault_withhold_publish = 0;
+}  // namespace
+
+void set_direct_fault_injection(int spin_limit, int withhold_publish) {
+    fault_spin_limit = spin_limit > 0 ? spin_limit : kDefaultSpinLimit;
+    fault_withhold_publish = withhold_publish ? 1 : 0;
+}
+
 cudaError_t launch_direct_batch(const DirectParams* fields, int count, void* scratch, const QueueShape& shape,
                                 long long spill_entries, cudaStream_t stream, bool fast_smooth) {
     if (count < 1 || count > kMaxDirectFields || !scratch) return cudaErrorInvalidValue;
     DirectBatch b{};
+    b.spin_limit = fault_spin_limit;
+    b.withhold_publish = fault_withhold_publish;
     b.count = count;
     b.fast_smooth = fast_smooth ? 1 : 0;
     b.counter = static_cast<unsigned long long*>(scratch);

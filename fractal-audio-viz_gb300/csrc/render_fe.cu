@@ -1,5 +1,5 @@
-// Floatexp form kernels: one deep Mandelbrot field per launch (the
-// per-field entry point), the batched persistent queue over many fields, the
+// Floatexp form kernels: one field per launch (the per-field entry point),
+// the batched persistent queue over many fields of any formula and size, the
 // tile-scheduled queue (64x64 tiles claimed in a given order, per-tile cost
 // and tail timing recorded), the coarse tile probe with the cost network's
 // features, and the heaviest-first ordering of tiles.  All run the same
@@ -9,7 +9,7 @@
 #include <cstdint>
 
 #include "mlp.h"
-#include "render_fe.cuh"
+#include "render_fe_alt.cuh"
 
 namespace fgb {
 namespace {
@@ -20,9 +20,7 @@ __global__ void __launch_bounds__(128) floatexp_kernel(const FxParams p) {
     if (index >= pixels) return;
     const int py = static_cast<int>(index / p.width);
     const int px = static_cast<int>(index - static_cast<long long>(py) * p.width);
-    const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
-    p.out[index] = result.value;
-    if (p.counts) p.counts[index] = result.count;
+    fxk::render_pixel(p, px, py);
 }
 
 // Batched persistent form: every warp claims chunks of pixels from one
@@ -31,7 +29,7 @@ __global__ void __launch_bounds__(128) floatexp_kernel(const FxParams p) {
 // per-pixel code above.  Lanes of a warp stay on neighbouring pixels, whose
 // paths through the series/BLA/tail code coincide (31.5 of 32 lanes active
 // per instruction on the 1920x1080 keyframes), so no lane refill is needed.
-__global__ void __launch_bounds__(128) floatexp_queue_kernel(const __grid_constant__ FxBatch b) {
+__global__ void __launch_bounds__(128, 8) floatexp_queue_kernel(const __grid_constant__ FxBatch b) {
     constexpr unsigned kFull = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const long long total = b.first[b.count];
@@ -49,9 +47,7 @@ __global__ void __launch_bounds__(128) floatexp_queue_kernel(const __grid_consta
             const int local = static_cast<int>(g - b.first[f]);
             const int py = local / p.width;
             const int px = local - py * p.width;
-            const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
-            p.out[local] = result.value;
-            if (p.counts) p.counts[local] = result.count;
+            fxk::render_pixel(p, px, py);
         }
     }
 }
@@ -107,7 +103,7 @@ __device__ __forceinline__ int tile_field(const FxBatch& b, int tile) {
 
 // Tile-scheduled persistent queue: a warp claims one band (tile_rows rows)
 // of a 64x64 tile at a time, tiles in `order`.
-__global__ void __launch_bounds__(128) floatexp_tile_kernel(const __grid_constant__ FxBatch b) {
+__global__ void __launch_bounds__(128, 8) floatexp_tile_kernel(const __grid_constant__ FxBatch b) {
     constexpr unsigned kFull = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const int bands = kTileSide / b.tile_rows;
@@ -137,10 +133,7 @@ __global__ void __launch_bounds__(128) floatexp_tile_kernel(const __grid_constan
             const int px = x0 + (i & (kTileSide - 1));
             const int py = y0 + i / kTileSide;
             if (px >= p.width || py >= p.height) continue;
-            const fxk::PixelOut result = fxk::floatexp_pixel(p, px, py);
-            const long long local = static_cast<long long>(py) * p.width + px;
-            p.out[local] = result.value;
-            if (p.counts) p.counts[local] = result.count;
+            fxk::render_pixel(p, px, py);
         }
         __syncwarp();
         if (lane == 0) {
@@ -168,7 +161,7 @@ __global__ void __launch_bounds__(128) tile_probe_kernel(const __grid_constant__
         int py = ty * kTileSide + (k / mlp::kProbeSide) * kProbeStride + kProbeStride / 2;
         px = px < p.width ? px : p.width - 1;
         py = py < p.height ? py : p.height - 1;
-        probe[s] = fxk::floatexp_pixel(p, px, py).count;
+        probe[s] = fxk::pixel_count(p, px, py);
     }
 }
 

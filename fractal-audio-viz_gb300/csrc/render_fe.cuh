@@ -75,40 +75,36 @@ __device__ __forceinline__ N1e reference_norm(const N1e& n, int mode) {
     return n_norm(units, place);
 }
 
-__device__ const FxCubic* find_cubic(const FxParams& p, int start, const N1e& dn, int max_length) {
+// The aligned power-of-two lookup over a level index in device memory
+// (BlaLevels::lookup, renderer.cpp:8645-8684): the longest block starting at
+// `start` whose squared radius exceeds |d|^2.
+template <typename Step>
+__device__ const Step* find_block(const Step* table, const LevelIndex* index, int start, const N1e& dn,
+                                  int max_length) {
     if (start <= 0 || max_length <= 0) return nullptr;
-    const int levels = p.cubic_index.levels;
-    if (levels == 0 || start > p.cubic_index.count[0]) return nullptr;
+    const int levels = __ldg(&index->levels);
+    if (levels == 0 || start > __ldg(&index->count[0])) return nullptr;
     int top = 31 - __clz(max_length);
     top = top < levels - 1 ? top : levels - 1;
     const int offset = start - 1;
     for (int level = top; level >= 1; --level) {
         if ((offset & ((1 << level) - 1)) != 0) continue;
-        const int index = offset >> level;
-        if (index >= p.cubic_index.count[level]) continue;
-        const FxCubic* c = p.cubic + p.cubic_index.offset[level] + index;
+        const int at = offset >> level;
+        if (at >= __ldg(&index->count[level])) continue;
+        const Step* c = table + __ldg(&index->offset[level]) + at;
         const N1e r2 = ld_n1e(&c->r2);
         if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
     }
     return nullptr;
 }
 
-__device__ const FxLinear* find_linear(const FxParams& p, int start, const N1e& dn, int max_length) {
-    if (start <= 0 || max_length <= 0) return nullptr;
-    const int levels = p.linear_index.levels;
-    if (levels == 0 || start > p.linear_index.count[0]) return nullptr;
-    int top = 31 - __clz(max_length);
-    top = top < levels - 1 ? top : levels - 1;
-    const int offset = start - 1;
-    for (int level = top; level >= 1; --level) {
-        if ((offset & ((1 << level) - 1)) != 0) continue;
-        const int index = offset >> level;
-        if (index >= p.linear_index.count[level]) continue;
-        const FxLinear* c = p.linear + p.linear_index.offset[level] + index;
-        const N1e r2 = ld_n1e(&c->r2);
-        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
-    }
-    return nullptr;
+__device__ __forceinline__ const FxCubic* find_cubic(const FxParams& p, int start, const N1e& dn, int max_length) {
+    return find_block(p.cubic, p.cubic_index, start, dn, max_length);
+}
+
+__device__ __forceinline__ const FxLinear* find_linear(const FxParams& p, int start, const N1e& dn,
+                                                       int max_length) {
+    return find_block(p.linear, p.linear_index, start, dn, max_length);
 }
 
 // Cubic bivariate map in Horner form (renderer.cpp:8686-8730).
@@ -132,18 +128,92 @@ __device__ F2e apply_cubic(const FxCubic* s, const F2e& d, const F2e& c, int ord
 struct PixelOut {
     float value;
     std::uint32_t count;
+    float de_x;  // analytic distance estimate (derivative planes only)
+    float de_y;
 };
 
+__device__ __forceinline__ PixelOut out_of(float value, std::uint32_t count) {
+    return PixelOut{value, count, 0.0f, 0.0f};
+}
+
+__device__ __forceinline__ F2e one_f2e() { return make(0.5f, 0.0f, 1); }
+
+// d(z^2 + c)/dc = 2 z dz/dc + 1 for the pixel's total z.
+__device__ __forceinline__ F2e derivative_step(const F2e& total, const F2e& derivative) {
+    return add(twice(mul(total, derivative)), one_f2e());
+}
+
+// render_plane_de (renderer.cpp:7844-7890) in FP32 floatexp: the distance
+// estimate |z| ln|z| / (u conj(dz/dc) spacing) with u = z/|z|, as (re, im)
+// in pixel-spacing units; zero where it is undefined.
+__device__ void plane_de(const F2e& total, const F2e& derivative, const N1e& spacing, float& out_x,
+                         float& out_y) {
+    out_x = 0.0f;
+    out_y = 0.0f;
+    if (is_zero(total) || !finite(total) || is_zero(derivative) || !finite(derivative)) return;
+    const float mag = hypotf(total.x, total.y);
+    const float log_mag = __logf(mag) + static_cast<float>(total.e) * kLn2;
+    if (!(log_mag > 0.0f) || !isfinite(log_mag)) return;
+    const F2e unit = make(total.x / mag, total.y / mag, 0);
+    const F2e den = mul(mul(unit, conj(derivative)), make(spacing.m, 0.0f, spacing.e));
+    const float den2 = fmaf(den.x, den.x, den.y * den.y);
+    if (!(den2 > 0.0f) || !isfinite(den2)) return;
+    const float num = mag * log_mag;
+    const int e = total.e - den.e;
+    const float rx = ldexpf_fast(num * den.x / den2, e);
+    const float ry = ldexpf_fast(-num * den.y / den2, e);
+    if (isfinite(rx) && isfinite(ry)) {
+        out_x = rx;
+        out_y = ry;
+    }
+}
+
+template <bool Planes>
+__device__ __forceinline__ PixelOut escaped(float value, std::uint32_t count, const F2e& total, const F2e& derivative,
+                                            const FxParams& p) {
+    PixelOut r = out_of(value, count);
+    if constexpr (Planes) plane_de(total, derivative, p.pixel_spacing, r.de_x, r.de_y);
+    return r;
+}
+
+// apply_bla_series_derivative (renderer.cpp:8732-8795): the derivative with
+// respect to c through a cubic block, given dd = dd/dc on entry.
+__device__ F2e apply_cubic_derivative(const FxCubic* s, const F2e& d, const F2e& c, const F2e& dd, int order) {
+    const F2e k0 = ld_f2e(&s->c[0]);
+    const F2e k1 = ld_f2e(&s->c[1]);
+    if (order <= 1) return add(mul(k0, dd), k1);
+    const F2e k2 = ld_f2e(&s->c[2]);
+    const F2e k3 = ld_f2e(&s->c[3]);
+    const F2e k4 = ld_f2e(&s->c[4]);
+    F2e pd = add(k0, add(twice(mul(k2, d)), mul(k3, c)));
+    F2e pc = add(k1, add(mul(k3, d), twice(mul(k4, c))));
+    if (order >= 3) {
+        const F2e k5 = ld_f2e(&s->c[5]);
+        const F2e k6 = ld_f2e(&s->c[6]);
+        const F2e k7 = ld_f2e(&s->c[7]);
+        const F2e k8 = ld_f2e(&s->c[8]);
+        const F2e d2 = mul(d, d);
+        const F2e c2 = mul(c, c);
+        pd = add(pd, add(mul(add(twice(mul(k5, d)), mul(k5, d)), d), add(twice(mul(k6, mul(d, c))), mul(k7, c2))));
+        pc = add(pc, add(mul(k6, d2), add(twice(mul(k7, mul(d, c))), mul(add(twice(mul(k8, c)), mul(k8, c)), c))));
+    }
+    return add(mul(pd, dd), pc);
+}
+
 // Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).
-__device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc) {
+template <bool Planes>
+__device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc,
+                               F2e derivative) {
     const float dcr = to_float_x(dc), dci = to_float_y(dc);
     float dr = to_float_x(delta), di = to_float_y(delta);
     const float escape2 = p.escape_mode == 1 ? 1.0e8f : 4.0f;
     const float safe2 = escape2 + 1.0e-7f;
     int steps = 0, rebases = 0;
     const bool strict = p.strict != 0;
+    const PixelOut unresolved_out = out_of(nan32(), 0u);
     float zr = __ldg(&p.orbit[ref].zr), zi = __ldg(&p.orbit[ref].zi);
     while (iteration < p.max_iter && ref + 1 < p.orbit_size) {
+        if constexpr (Planes) derivative = derivative_step(norm(zr + dr, zi + di, 0), derivative);
         const float lr = 2.0f * (zr * dr - zi * di);
         const float li = 2.0f * (zr * di + zi * dr);
         const float sr = dr * dr - di * di;
@@ -152,20 +222,22 @@ __device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const 
         di = li + si + dci;
         ++ref;
         ++iteration;
-        if (++steps > 65536) return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                                             strict ? 0u : static_cast<std::uint32_t>(iteration)};
+        if (++steps > 65536) {
+            return strict ? unresolved_out
+                          : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
+        }
         zr = __ldg(&p.orbit[ref].zr);
         zi = __ldg(&p.orbit[ref].zi);
         const float tr = zr + dr, ti = zi + di;
         const float m2 = tr * tr + ti * ti;
         if (!isfinite(m2)) {
-            return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                            strict ? 0u : static_cast<std::uint32_t>(iteration)};
+            return strict ? unresolved_out
+                          : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
         }
         if (m2 > escape2) {
             const float mag = sqrtf(fmaxf(m2, safe2));
-            return PixelOut{(static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
-                            static_cast<std::uint32_t>(iteration)};
+            return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                                   static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
         }
         if (m2 < dr * dr + di * di) {
             dr = tr;
@@ -174,31 +246,35 @@ __device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const 
             zr = __ldg(&p.orbit[0].zr);
             zi = __ldg(&p.orbit[0].zi);
             if (++rebases > 64) {
-                return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                                strict ? 0u : static_cast<std::uint32_t>(iteration)};
+                return strict ? unresolved_out
+                              : out_of(static_cast<float>(iteration) - p.output_bias,
+                                       static_cast<std::uint32_t>(iteration));
             }
         }
     }
     if (iteration < p.max_iter) {
-        return PixelOut{strict ? nan32() : static_cast<float>(iteration) - p.output_bias,
-                        strict ? 0u : static_cast<std::uint32_t>(iteration)};
+        return strict ? unresolved_out
+                      : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
     }
-    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    return out_of(static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter));
 }
 
 // Direct recurrence from the total once the pixel has left the reference.
-__device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc) {
+template <bool Planes>
+__device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc, F2e derivative) {
     const F2e parameter = add(ld_f2e(&p.orbit[1].z), dc);
     const N1e limit = bailout(p.escape_mode);
     while (iteration < p.max_iter) {
+        if constexpr (Planes) derivative = derivative_step(total, derivative);
         total = add(mul(total, total), parameter);
         ++iteration;
         const N1e n = norm2(total);
         if (n_cmp(n, limit) > 0) {
-            return PixelOut{smooth_from_norm(iteration, n, p.output_bias), static_cast<std::uint32_t>(iteration)};
+            return escaped<Planes>(smooth_from_norm(iteration, n, p.output_bias), static_cast<std::uint32_t>(iteration),
+                                   total, derivative, p);
         }
     }
-    return PixelOut{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    return out_of(static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter));
 }
 
 // Shallow mode: a field above 1e-12 of view height renders by plain FP32
@@ -212,12 +288,14 @@ __device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration,
 //   re: dr (2Zr + dr) - di (2Zi + di) + dcr
 //   im: 2 (Zr di + dr (Zi + di)) + dci
 // (6 FMA-pipe operations), then |Z + d|^2 for the escape and rebase tests.
+template <bool Planes>
 __device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py) {
     const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
     const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
     const float dcr = ldexpf_fast(p.view_width.x * xf, p.view_width.e);
     const float dci = ldexpf_fast(p.view_height.x * yf, p.view_height.e);
-    const PixelOut inside{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    const PixelOut inside = out_of(static_cast<float>(p.max_iter) - p.output_bias,
+                                   static_cast<std::uint32_t>(p.max_iter));
     if (p.interior_test) {
         // Main cardioid and period-2 bulb (renderer.cpp:10060-10066), taken
         // only with a margin far above the float error of c = centre + dc,
@@ -240,8 +318,10 @@ __device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py
     constexpr int kStride = sizeof(FxOrbitRec) / sizeof(float2);
     float dr = 0.0f, di = 0.0f;
     float zr = 0.0f, zi = 0.0f;  // Z_0
+    F2e derivative = zero();
     int ref = 0;
     for (int iteration = 1; iteration <= p.max_iter; ++iteration) {
+        if constexpr (Planes) derivative = derivative_step(norm(zr + dr, zi + di, 0), derivative);
         const float ar = fmaf(2.0f, zr, dr), ai = fmaf(2.0f, zi, di);
         const float nr = fmaf(dr, ar, fmaf(-di, ai, dcr));
         const float ni = fmaf(2.0f, fmaf(zr, di, dr * (zi + di)), dci);
@@ -255,8 +335,8 @@ __device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py
         const float m2 = fmaf(tr, tr, ti * ti);
         if (m2 > escape2) {
             const float mag = sqrtf(fmaxf(m2, safe2));
-            return PixelOut{(static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
-                            static_cast<std::uint32_t>(iteration)};
+            return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                                   static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
         }
         if (m2 < fmaf(dr, dr, di * di) || ref >= valid) {
             dr = tr;
@@ -269,10 +349,11 @@ __device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py
     return inside;
 }
 
-// One pixel of the floatexp form; shared by the per-field kernel and the
-// batched persistent queues.
+// One Mandelbrot pixel of the floatexp form; shared by the per-field kernel
+// and the batched persistent queues.
+template <bool Planes>
 __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int py) {
-    if (p.shallow) return shallow_pixel(p, px, py);
+    if (p.shallow) return shallow_pixel<Planes>(p, px, py);
     const float xf = axis_offset(px, p.width, p.coordinate_mode) / static_cast<float>(p.width);
     const float yf = -axis_offset(py, p.height, p.coordinate_mode) / static_cast<float>(p.height);
     const F2e dx = norm(p.view_width.x * xf, 0.0f, p.view_width.e);
@@ -280,12 +361,14 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
     const F2e dc = add(make(dx.x, 0.0f, dx.e), make(0.0f, dy.x, dy.e));
 
     F2e delta = dc;
+    F2e derivative = one_f2e();
     int ref = 1;
     int iteration = 1;
     if (p.series_on && n_cmp(norm2(dc), p.series_r2) <= 0) {
         if (p.series_scaled) {
             // Plain-float Horner on u = dc 2^-scale with the field's
-            // prescaled coefficients (|u| <= 1), rescaled once at the end.
+            // prescaled coefficients (|u| <= 1), rescaled once at the end;
+            // with planes the derivative sum_k k b_k u^(k-1) alongside.
             const FxSeriesScaled* sc = p.series_scaled;
             const int scale = __ldg(&sc->scale);
             const float ur = ldexpf_fast(p.view_width.x * xf, p.view_width.e - scale);
@@ -293,16 +376,33 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             const int terms = __ldg(&sc->terms);
             float vr = __ldg(&sc->b[terms - 1][0]);
             float vi = __ldg(&sc->b[terms - 1][1]);
+            float wr = 0.0f, wi = 0.0f;  // derivative of the inner polynomial
             for (int k = terms - 1; k > 1; --k) {
+                if constexpr (Planes) {
+                    const float nwr = fmaf(wr, ur, fmaf(-wi, ui, vr));
+                    const float nwi = fmaf(wr, ui, fmaf(wi, ur, vi));
+                    wr = nwr;
+                    wi = nwi;
+                }
                 const float nr = fmaf(vr, ur, fmaf(-vi, ui, __ldg(&sc->b[k - 1][0])));
                 const float ni = fmaf(vr, ui, fmaf(vi, ur, __ldg(&sc->b[k - 1][1])));
                 vr = nr;
                 vi = ni;
             }
-            delta = norm(vr * ur - vi * ui, vr * ui + vi * ur, __ldg(&sc->shift));
+            const int shift = __ldg(&sc->shift);
+            delta = norm(vr * ur - vi * ui, vr * ui + vi * ur, shift);
+            if constexpr (Planes) {
+                // d/dc [v(u) u] 2^shift = (v + u v'(u)) 2^(shift - scale)
+                derivative = norm(vr + (wr * ur - wi * ui), vi + (wr * ui + wi * ur), shift - scale);
+            }
         } else {
             F2e value = ld_f2e(&p.series[p.series_terms - 1]);
-            for (int k = p.series_terms - 1; k > 1; --k) value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
+            F2e poly = zero();
+            for (int k = p.series_terms - 1; k > 1; --k) {
+                if constexpr (Planes) poly = add(mul(poly, dc), value);
+                value = add(mul(value, dc), ld_f2e(&p.series[k - 1]));
+            }
+            if constexpr (Planes) derivative = add(mul(poly, dc), value);
             delta = mul(value, dc);
         }
         ref = p.series_iteration;
@@ -310,7 +410,7 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
     }
     const N1e limit = bailout(p.escape_mode);
     const N1e three = N1e{0.75f, 2};
-    PixelOut result{static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter)};
+    PixelOut result = out_of(static_cast<float>(p.max_iter) - p.output_bias, static_cast<std::uint32_t>(p.max_iter));
     bool have_total = false;
     F2e total = zero();
     N1e total_norm = n_norm(0.0f, 0);
@@ -318,7 +418,7 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
     int rebases = 0;
     while (iteration < p.max_iter) {
         if (ref < 0 || ref >= p.orbit_size) {
-            result = PixelOut{static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration)};
+            result = out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
             break;
         }
         const F2e z = ld_f2e(&p.orbit[ref].z);
@@ -337,19 +437,19 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
                     ref = 0;
                     continue;
                 }
-                result = PixelOut{nan32(), 0u};
+                result = out_of(nan32(), 0u);
                 break;
             }
         }
         if (n_cmp(total_norm, limit) > 0) {
-            result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
-                              static_cast<std::uint32_t>(iteration)};
+            result = escaped<Planes>(smooth_from_norm(iteration, total_norm, p.output_bias),
+                                     static_cast<std::uint32_t>(iteration), total, derivative, p);
             break;
         }
         const N1e dn = norm2(delta);
         if (n_cmp(total_norm, dn) < 0) {
             if (++rebases > 64) {
-                result = continue_direct(p, total, iteration, dc);
+                result = continue_direct<Planes>(p, total, iteration, dc, derivative);
                 break;
             }
             delta = total;
@@ -357,7 +457,7 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             continue;
         }
         if (p.map_end > 1 && ref >= p.map_end) {
-            result = continue_direct(p, total, iteration, dc);
+            result = continue_direct<Planes>(p, total, iteration, dc, derivative);
             break;
         }
         const int remaining = p.max_iter - iteration;
@@ -374,11 +474,12 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
         }
         const int length = lin ? __ldg(&lin->len) : (cub ? __ldg(&cub->len) : 0);
         if (bla && (length <= 0 || ref + length > p.max_iter) && dn.e > -90) {
-            result = float_tail(p, iteration, ref, delta, dc);
+            result = float_tail<Planes>(p, iteration, ref, delta, dc, derivative);
             break;
         }
         if (length > 0 && ref + length <= p.max_iter) {
             const F2e previous = delta;
+            const F2e previous_derivative = derivative;
             delta = lin ? add(mul(ld_f2e(&lin->a), previous), mul(ld_f2e(&lin->b), dc))
                         : apply_cubic(cub, previous, dc, order);
             const F2e z_end = ld_f2e(&p.orbit[ref + length].z);
@@ -392,24 +493,29 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             if (n_cmp(end_norm, three) >= 0) {
                 // Replay the block exactly near escape.
                 delta = previous;
-                bool escaped = false;
+                bool escaped_here = false;
                 for (int k = 0; k < length && iteration < p.max_iter; ++k) {
                     const F2e zk = ld_f2e(&p.orbit[ref].z);
+                    if constexpr (Planes) derivative = derivative_step(add(zk, delta), derivative);
                     delta = add(twice(mul(zk, delta)), add(mul(delta, delta), dc));
                     ++ref;
                     ++iteration;
                     total = add(ld_f2e(&p.orbit[ref].z), delta);
                     total_norm = reference_norm(norm2(total), p.escape_mode);
                     if (n_cmp(total_norm, limit) > 0) {
-                        result = PixelOut{smooth_from_norm(iteration, total_norm, p.output_bias),
-                                          static_cast<std::uint32_t>(iteration)};
-                        escaped = true;
+                        result = escaped<Planes>(smooth_from_norm(iteration, total_norm, p.output_bias),
+                                                 static_cast<std::uint32_t>(iteration), total, derivative, p);
+                        escaped_here = true;
                         break;
                     }
                 }
-                if (escaped) break;
+                if (escaped_here) break;
                 have_total = true;
             } else {
+                if constexpr (Planes) {
+                    derivative = lin ? add(mul(ld_f2e(&lin->a), previous_derivative), ld_f2e(&lin->b))
+                                     : apply_cubic_derivative(cub, previous, dc, previous_derivative, order);
+                }
                 ref += length;
                 iteration += length;
                 total = end;
@@ -418,6 +524,7 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             }
             continue;
         }
+        if constexpr (Planes) derivative = derivative_step(total, derivative);
         delta = add(twice(mul(z, delta)), add(mul(delta, delta), dc));
         ++ref;
         ++iteration;

@@ -45,6 +45,7 @@ enum ScratchSlot {
     kScratchPoints,
     kScratchPlanesIn,
     kScratchPlanesOut,
+    kScratchDiscard,  // planes a batch's plain kernels write but no caller asked for
     kScratchCount
 };
 

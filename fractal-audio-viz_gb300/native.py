@@ -377,11 +377,29 @@ class Keyframe(ctypes.Structure):
     ]
 
 
+class Field(ctypes.Structure):
+    """FractalGb300Field: one field of a general batched device render."""
+
+    _fields_ = [
+        ("field", ctypes.c_void_p),
+        ("counts", ctypes.c_void_p),
+        ("de_x", ctypes.c_void_p),
+        ("de_y", ctypes.c_void_p),
+        ("zoom_text", ctypes.c_char_p),
+        ("reference", ctypes.c_void_p),
+        ("width", ctypes.c_int),
+        ("height", ctypes.c_int),
+        ("max_iter", ctypes.c_int),
+        ("flags", ctypes.c_int),
+    ]
+
+
 BATCH_GRAPH = 1
 BATCH_AUTOTUNE = 2
 BATCH_TILES = 4
 BATCH_LEARNED = 8
 BATCH_PROBE = 16
+BATCH_FP32_ALTERNATES = 32
 KEYFRAME_SHALLOW = 1
 
 _GB300_ABI = (
@@ -432,7 +450,11 @@ _GB300_ABI = (
      (ctypes.POINTER(Keyframe), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
       ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RenderOptions), ctypes.c_int,
       ctypes.c_uint, ctypes.c_void_p)),
+    ("fractal_gb300_render_fields_device", ctypes.c_int,
+     (ctypes.POINTER(Field), ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+      ctypes.POINTER(RenderOptions), ctypes.c_int, ctypes.c_uint, ctypes.c_void_p)),
     ("fractal_gb300_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
+    ("fractal_gb300_set_direct_fault_injection", ctypes.c_int, (ctypes.c_int, ctypes.c_int)),
     ("fractal_gb300_set_queue_shapes", ctypes.c_int, (ctypes.POINTER(ctypes.c_int), ctypes.c_int)),
     ("fractal_gb300_set_cost_network", ctypes.c_int, (ctypes.c_void_p,)),
     ("fractal_gb300_last_direct_steps", ctypes.c_int, (ctypes.POINTER(ctypes.c_ulonglong),)),

@@ -593,6 +593,12 @@ typedef struct FractalGb300Keyframe {
 /* With _TILES: compute the probe and the network features without using them
  * (training data: fractal_gb300_last_tiles returns features and costs). */
 #define FRACTAL_GB300_BATCH_PROBE 16u
+/* Form 1: render julia / burning-ship / tricorn fields (from 1e6) in the
+ * FP32 queue too.  Without it they stay in the FP64 plain form: their deep
+ * views hold long post-linear orbits that FP32 deltas do not follow (on the
+ * test views 0-31 % of counts differ from FP64, whose counts a direct mpmath
+ * iteration confirms), so this trades accuracy for about 10x speed. */
+#define FRACTAL_GB300_BATCH_FP32_ALTERNATES 32u
 
 /* Render many keyframes in a few launches: all direct frames in one
  * persistent lane-refill FP64 queue on a second stream, all floatexp frames
@@ -609,6 +615,41 @@ int fractal_gb300_render_keyframes_device(const FractalGb300Keyframe *frames, in
                                           int series_order, int series_block,
                                           const FractalRenderOptions *options, int form,
                                           unsigned flags, void *stream);
+
+/* One field of a general batch (no counterpart in the reference): device
+ * outputs (`counts` and the derivative planes may be NULL; de_x / de_y both
+ * or neither: the analytic distance estimate of render_plane_de,
+ * renderer.cpp:7844-7990, as in FractalRenderPlanes), its zoom, the reference
+ * handle it renders from (its formula, centre and, for Julia, c; NULL: the
+ * direct FP64 Mandelbrot path at the batch centre), its own size and cap,
+ * and flags (0 or FRACTAL_GB300_KEYFRAME_SHALLOW). */
+typedef struct FractalGb300Field {
+    float *field;
+    uint32_t *counts;
+    double *de_x;
+    double *de_y;
+    const char *zoom_text;
+    void *reference;
+    int width;
+    int height;
+    int max_iter;
+    int flags;
+} FractalGb300Field;
+
+/* fractal_gb300_render_keyframes_device for fields of uneven size and of
+ * every formula, with optional derivative planes.  Form 1 renders the
+ * floatexp-covered fields (strict, no cycle detection, no time budget:
+ * Mandelbrot from any zoom; the other formulas from 1e6 with
+ * FRACTAL_GB300_BATCH_FP32_ALTERNATES) in one persistent FP32 queue; the
+ * direct fields run in the FP64 lane-refill queue (one launch per formula
+ * and plane set) and the plain-form fields one launch each, on a second
+ * stream beside it.  Form 0 is the plain FP64 form, whose
+ * pixels and planes equal the per-field entry points'.  At most 64 floatexp
+ * fields with the tile flags; no limit otherwise. */
+int fractal_gb300_render_fields_device(const FractalGb300Field *fields, int count, const char *x_center,
+                                       const char *y_center, int series_order, int series_block,
+                                       const FractalRenderOptions *options, int form, unsigned flags,
+                                       void *stream);
 
 /* Pin the launch shapes of the calling thread's next batches (same order as
  * fractal_gb300_queue_shapes; a 0 chunk keeps the default, a 0 blocks/SM
@@ -636,6 +677,16 @@ int fractal_gb300_last_tiles(int *tiles, float *cost, uint16_t *features, int ca
  * fails too, after the count is copied, when the launch's spill queue
  * reported an unpublished entry (the render is then incomplete). */
 int fractal_gb300_last_direct_steps(unsigned long long *steps);
+
+/* Test hook (no counterpart in the reference): the calling thread's next
+ * direct launches wait at most `spin_limit` polls (1 .. 1 << 22; 0 = the
+ * default 1 << 22) for a spilled pixel's publish mark, and with
+ * withhold_publish = 1 write spilled pixels without publishing them, so a
+ * test can drive the wait to its bound: the kernel then drops those pixels,
+ * ends normally and fractal_gb300_last_direct_steps reports the queue error.
+ * (0, 0) restores normal operation.  The failure is made on the device by
+ * data only; no fault, trap or unbounded wait is involved. */
+int fractal_gb300_set_direct_fault_injection(int spin_limit, int withhold_publish);
 
 /* Launch shapes the calling thread's last batch used: direct chunk, direct
  * blocks per SM, floatexp chunk, floatexp blocks per SM (0 = as many as fit). */

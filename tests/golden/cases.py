@@ -153,6 +153,7 @@ def alternate_cases() -> list[dict]:
         for log_zoom, size in ((7.0, (96, 54)), (12.0, (64, 36))):
             cases.append(_m(f"{formula}_e{int(log_zoom)}_{size[0]}x{size[1]}", kind="reference", formula=formula,
                             centre=c[key], log10_zoom=log_zoom, width=size[0], height=size[1], max_iter=10_000))
+    cases.extend(deep_alternate_cases())
     # Non-strict (cycle detection) and linear-block-free variants.
     jf = c["julia_fixed_1"]
     cases.append(_m("julia_fixed_1_nonstrict_64x36", kind="reference", formula="julia",
@@ -161,6 +162,29 @@ def alternate_cases() -> list[dict]:
     cases.append(_m("burning-ship_nobla_48x27", kind="reference", formula="burning-ship",
                     centre=c["burning_ship_boundary"], log10_zoom=7.0, width=48, height=27, max_iter=10_000,
                     options=dict(disable_bla=1)))
+    return cases
+
+
+# Depths and caps of the deep alternate-formula fixtures: the batch
+# workload's range (zoom 1e10-1e100, caps 1e4-1e6) on small fields.
+DEEP_ALTERNATE_LEVELS = ((30.0, 100_000), (60.0, 300_000), (100.0, 1_000_000))
+
+
+def deep_alternate_cases() -> list[dict]:
+    """Julia, burning-ship and tricorn fields at 1e30, 1e60 and 1e100 with
+    caps 1e5-1e6 (64x36): Julia on the repelling fixed point, the others on
+    130-digit seeded preperiodic parameters."""
+    c = centres()
+    cases = []
+    jf = c["julia_fixed_1"]
+    for log_zoom, cap in DEEP_ALTERNATE_LEVELS:
+        cases.append(_m(f"julia_fixed_1_deep_e{int(log_zoom)}_64x36", kind="reference", formula="julia",
+                        centre=dict(re=jf["re"], im=jf["im"]), julia=(jf["c_re"], jf["c_im"]), log10_zoom=log_zoom,
+                        width=64, height=36, max_iter=cap))
+    for formula, key in (("burning-ship", "burning_ship_deep"), ("tricorn", "tricorn_deep")):
+        for log_zoom, cap in DEEP_ALTERNATE_LEVELS:
+            cases.append(_m(f"{formula}_deep_e{int(log_zoom)}_64x36", kind="reference", formula=formula,
+                            centre=c[key], log10_zoom=log_zoom, width=64, height=36, max_iter=cap))
     return cases
 
 
@@ -183,3 +207,45 @@ def kfp_cases() -> list[dict]:
             cases.append(dict(name=f"kfp_{recipe}_{field}", field=field, recipe=recipe, max_iter=max_iter,
                               field_bias=bias))
     return cases
+
+
+# The batch workload (configs[2]): field sizes and its zoom and cap ranges.
+BATCH_SIZES = ((720, 480), (1280, 720), (1920, 1080), (3840, 2160))
+
+
+def batch_centres() -> dict:
+    """Centre pool per formula for the batch: seeded Misiurewicz points
+    (Mandelbrot), the repelling fixed points of two seeded boundary
+    constants (Julia), seeded preperiodic parameters (burning ship, tricorn);
+    all with at least 120 digits, enough for 1e100."""
+    c = centres()
+    return {
+        "mandelbrot": [dict(re=c[k]["re"], im=c[k]["im"]) for k in ("field_e100", "fhd_stack_e50",
+                                                                   "field_640x360_e30")],
+        "julia": [dict(re=c[k]["re"], im=c[k]["im"], julia=(c[k]["c_re"], c[k]["c_im"]))
+                  for k in ("julia_fixed_1", "julia_fixed_2")],
+        "burning-ship": [dict(re=c["burning_ship_deep"]["re"], im=c["burning_ship_deep"]["im"])],
+        "tricorn": [dict(re=c["tricorn_deep"]["re"], im=c["tricorn_deep"]["im"])],
+    }
+
+
+def batch_mix(seed: int = 2024, count: int = 64, sizes=BATCH_SIZES, log_zoom=(10.0, 100.0),
+              log_cap=(4.0, 6.0)) -> list[dict]:
+    """A seeded mix of uneven fields: formula uniform over the four, centre
+    from its pool, size from `sizes`, log10 zoom and log10 cap uniform over
+    the given ranges."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    pool = batch_centres()
+    formulas = ("mandelbrot", "julia", "burning-ship", "tricorn")
+    mix = []
+    for i in range(count):
+        formula = formulas[int(rng.integers(0, 4))]
+        centre = pool[formula][int(rng.integers(0, len(pool[formula])))]
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        mix.append(dict(name=f"batch{i:02d}_{formula}", formula=formula, re=centre["re"], im=centre["im"],
+                        julia=centre.get("julia", ("0", "0")),
+                        log10_zoom=float(rng.uniform(*log_zoom)), width=w, height=h,
+                        max_iter=int(round(10.0 ** rng.uniform(*log_cap)))))
+    return mix

@@ -296,13 +296,84 @@ def julia_boundary_constant(seed: int):
     raise RuntimeError("no Julia boundary constant found")
 
 
+def _alt_orbit_jacobian(formula: str, cr, ci, steps: int):
+    """Orbit of 0 under the burning-ship or tricorn map with the real
+    Jacobian d(x, y)/d(cr, ci) carried along; stops early on escape."""
+    x = y = xa = ya = xb = yb = mpmath.mpf(0)
+    out = []
+    for _ in range(steps):
+        if formula == "burning-ship":
+            sx, sy = (1 if x >= 0 else -1), (1 if y >= 0 else -1)
+            ax, ay = abs(x), abs(y)
+            x, y, xa, ya, xb, yb = (x * x - y * y + cr, 2 * ax * ay + ci,
+                                    2 * x * xa - 2 * y * ya + 1, 2 * (sx * xa * ay + ax * sy * ya),
+                                    2 * x * xb - 2 * y * yb, 2 * (sx * xb * ay + ax * sy * yb) + 1)
+        else:
+            x, y, xa, ya, xb, yb = (x * x - y * y + cr, -2 * x * y + ci,
+                                    2 * x * xa - 2 * y * ya + 1, -2 * (xa * y + x * ya),
+                                    2 * x * xb - 2 * y * yb, -2 * (xb * y + x * yb) + 1)
+        out.append((x, y, xa, ya, xb, yb))
+        if x * x + y * y > 1e6:
+            break
+    return out
+
+
+def alternate_preperiodic(formula: str, seed: int, digits: int = 130):
+    """A preperiodic (Misiurewicz-like) parameter of the burning-ship or
+    tricorn map: z_{k+p} = z_k for seeded k ~ U{3..9}, p ~ U{1..4}, found by
+    real 2x2 Newton from seeded starts, first at 60 digits, then polished at
+    `digits`.  Views centred there show structure at every depth."""
+    rng = np.random.default_rng(seed)
+
+    def solve(c0, k, p, dps):
+        with mpmath.workdps(dps + 20):
+            cr, ci = mpmath.mpf(c0[0]), mpmath.mpf(c0[1])
+            for it in range(120):
+                o = _alt_orbit_jacobian(formula, cr, ci, k + p)
+                if len(o) < k + p:
+                    return None
+                x1, y1, xa1, ya1, xb1, yb1 = o[k + p - 1]
+                x0, y0, xa0, ya0, xb0, yb0 = o[k - 1]
+                fx, fy = x1 - x0, y1 - y0
+                j00, j01, j10, j11 = xa1 - xa0, xb1 - xb0, ya1 - ya0, yb1 - yb0
+                det = j00 * j11 - j01 * j10
+                if det == 0:
+                    return None
+                dr = (fx * j11 - fy * j01) / det
+                di = (j00 * fy - j10 * fx) / det
+                cr -= dr
+                ci -= di
+                if abs(dr) + abs(di) < mpmath.mpf(10) ** (-(dps + 5)):
+                    return cr, ci, it
+            return None
+
+    for _ in range(2000):
+        c0 = (rng.uniform(-1.9, 0.6), rng.uniform(-1.6, 0.6))
+        k, p = int(rng.integers(3, 10)), int(rng.integers(1, 5))
+        rough = solve(c0, k, p, 60)
+        if rough is None or rough[2] >= 100 or abs(rough[0]) + abs(rough[1]) < 1e-3:
+            continue
+        if abs(abs(rough[0]) - 1) < 1e-9 or abs(abs(rough[1]) - 1) < 1e-9:
+            continue  # rational corner points
+        fine = solve((rough[0], rough[1]), k, p, digits)
+        if fine is None:
+            continue
+        with mpmath.workdps(digits + 20):
+            re = mpmath.nstr(fine[0], digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+            im = mpmath.nstr(fine[1], digits, strip_zeros=False, min_fixed=-mpmath.inf, max_fixed=mpmath.inf)
+        return {"seed": seed, "preperiod": k, "period": p, "re": re, "im": im}
+    raise RuntimeError("no preperiodic point found")
+
+
 def add_deep_alternates(path: str) -> None:
-    """Add 130-digit burning-ship and tricorn boundary points (views to 1e100
-    need more than 100 digits) to an existing centres.json."""
+    """Add 130-digit preperiodic burning-ship and tricorn parameters (views
+    to 1e100 need more than 100 digits) to an existing centres.json."""
     with open(path, encoding="ascii") as handle:
         centres = json.load(handle)
-    centres["burning_ship_boundary_deep"] = alternate_boundary("burning-ship", seed=8201, digits=130)
-    centres["tricorn_boundary_deep"] = alternate_boundary("tricorn", seed=8202, digits=130)
+    centres.pop("burning_ship_boundary_deep", None)
+    centres.pop("tricorn_boundary_deep", None)
+    centres["burning_ship_deep"] = alternate_preperiodic("burning-ship", seed=8301)
+    centres["tricorn_deep"] = alternate_preperiodic("tricorn", seed=8302)
     with open(path, "w", encoding="ascii") as handle:
         json.dump(centres, handle, indent=1)
         handle.write("\n")

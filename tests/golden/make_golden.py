@@ -49,9 +49,36 @@ def _package_kfp():
 PLANE_LIMIT = 64 * 36  # store the f64 planes only for cases this small
 
 
+def write_cases(library, cases, index) -> None:
+    """Run `cases` through the reference build; store their fixtures and
+    index entries."""
+    for case in cases:
+        result = run_case(library, case)
+        info = summary(result)
+        index["cases"][case["name"]] = info
+        if case.get("store") != "hash":
+            arrays = {"field": result["field"], "counts": result["counts"]}
+            if case["width"] * case["height"] <= PLANE_LIMIT:
+                for key in ("orbit_iteration", "phase", "de_x", "de_y", "test1", "test2"):
+                    arrays[key] = result[key]
+            np.savez_compressed(os.path.join(FIXTURES, case["name"] + ".npz"), **arrays)
+        print(f"{case['name']:28s} sum={info['count_sum']:>12d} nan={info['nan_pixels']:>5d} "
+              f"range=[{info['count_min']},{info['count_max']}]")
+
+
 def main() -> int:
     native = _native()
     library = native.load(REFERENCE_LIBRARY)
+    if "--deep-alternates" in sys.argv:
+        # Only the deep alternate-formula fixtures, added to the index.
+        path = os.path.join(FIXTURES, "index.json")
+        with open(path, encoding="ascii") as handle:
+            index = json.load(handle)
+        write_cases(library, case_defs.deep_alternate_cases(), index)
+        with open(path, "w", encoding="ascii") as handle:
+            json.dump(index, handle, indent=1, sort_keys=True)
+            handle.write("\n")
+        return 0
     os.makedirs(FIXTURES, exist_ok=True)
     index = {"library": "oracle/_ref/mandelbrot.so (reference release build)", "cases": {}}
     all_cases = case_defs.parity_cases() + case_defs.alternate_cases()
