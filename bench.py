@@ -378,6 +378,23 @@ class StackBench:
         self.stack.close()
 
 
+def run_dry(args) -> int:
+    """The replica launch without rendering (tests of --gpus N on CPU hosts):
+    ranks rendezvous over gloo at MASTER_ADDR / MASTER_PORT and each prints
+    its rank and the max over ranks of rank + 1."""
+    import torch.distributed as dist
+
+    rank, world, local_rank = dist_env()
+    if world > 1:
+        dist.init_process_group("gloo")
+    print(json.dumps({"rank": rank, "world": world, "local_rank": local_rank,
+                      "max_over_ranks": max_over_ranks(float(rank + 1)),
+                      "master": os.environ.get("MASTER_ADDR")}), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def measure_batch_mix(package, library, stream, steps: int, local_rank: int) -> dict:
     """configs[2]: 64 seeded fields mixing the four formulas and the four
     sizes 720x480 .. 3840x2160, zooms log-uniform 1e10-1e100, caps
@@ -1145,6 +1162,9 @@ def main() -> int:
     parser.add_argument("--headline-only", action="store_true",
                         help="skip the 55-keyframe stack measured beside the 1e100 atlas")
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--dry-run", action="store_true",
+                        help="replica bookkeeping only: each rank joins the group (gloo), prints its rank and "
+                             "the max over ranks, and exits")
     parser.add_argument("--frame-passes", action="store_true",
                         help="time the per-frame 4K passes (atlas compositor, colour) and exit")
     parser.add_argument("--song", action="store_true",
@@ -1160,6 +1180,8 @@ def main() -> int:
     args = parser.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ and not (args.case or args.frame_passes or args.song):
         return launch_replicas(sys.argv[1:], args.gpus)
+    if args.dry_run:
+        return run_dry(args)
     if args.case:
         return run_case(args.case)
     if args.frame_passes:

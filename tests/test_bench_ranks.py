@@ -61,3 +61,19 @@ def test_single_process_value_is_unchanged():
     import bench
 
     assert bench.max_over_ranks(3.5) == 3.5
+
+
+def test_gpus_flag_starts_one_replica_per_gpu():
+    """bench.py --gpus N without a launcher starts N processes itself
+    (RANK / LOCAL_RANK / WORLD_SIZE, a 127.0.0.1 rendezvous); here the
+    replicas only rendezvous over gloo and reduce, with no GPU work."""
+    import json
+    import subprocess
+
+    result = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--dry-run"],
+                            capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert result.returncode == 0, result.stderr[-2000:]
+    lines = [json.loads(line) for line in result.stdout.splitlines() if line.startswith("{")]
+    assert sorted(line["rank"] for line in lines) == [0, 1]
+    assert all(line["world"] == 2 and line["local_rank"] == line["rank"] for line in lines)
+    assert all(line["max_over_ranks"] == 2.0 and line["master"] == "127.0.0.1" for line in lines)

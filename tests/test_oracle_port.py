@@ -7,6 +7,8 @@ fixtures, which are the reference release build's own output.
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import pytest
 
@@ -40,3 +42,34 @@ def test_port_aurora_matches_reference(oracle_port, reference_library, package):
         a = native.colourise(oracle_port, field, 160, 90, 50_000, *controls)
         b = native.colourise(reference_library, field, 160, 90, 50_000, *controls)
         np.testing.assert_array_equal(a, b)
+
+
+def test_port_runs_at_reference_speed(oracle_port, reference_library, package):
+    """The CPU baseline on the GPU host is the port (the reference sources are
+    not there), so it must run at least at 0.9x the reference build's speed:
+    both render the same deep levels of the FHD stack at 240x135 through the
+    same ABI, interleaved, best of five each, on the same thread count."""
+    import time
+
+    from .golden import cases as case_defs
+
+    native, atlas = package.native, package.atlas
+    e50 = case_defs.centres()["fhd_stack_e50"]
+    levels = [lv for lv in case_defs.fhd_stack_levels() if lv[0] in (30, 40, 54)]
+    stacks = {name: atlas.KeyframeStack(lib, e50["re"], e50["im"], levels, step=math.log10(8.0))
+              for name, lib in (("port", oracle_port), ("reference", reference_library))}
+    best = {name: 0.0 for name in stacks}
+    try:
+        for _ in range(5):
+            for name, stack in stacks.items():
+                t0 = time.perf_counter()
+                work = 0
+                for keyframe in stack.keyframes:
+                    field, planes = stack.render_host(keyframe, 240, 135, threads=2, planes=True)
+                    work += int(native.iteration_counts(field, planes["orbit_iteration"], keyframe.max_iter)
+                                .astype(np.uint64).sum())
+                best[name] = max(best[name], work / (time.perf_counter() - t0))
+    finally:
+        for stack in stacks.values():
+            stack.close()
+    assert best["port"] >= 0.9 * best["reference"], best
