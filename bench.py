@@ -798,7 +798,7 @@ def run_case(name: str) -> int:
         print("ok", name)
         return 0
     width, height = (960, 540) if name.endswith("960x540") else (WIDTH, HEIGHT)
-    levels, step = workload_levels()
+    levels, step = workload_levels("fhd_atlas_e100" if name.startswith("atlas_e100") else "fhd_keyframe_stack")
     x, y = centre()
     stack = package.atlas.KeyframeStack(library, x, y, levels, step=step)
     n = len(stack.keyframes)
@@ -807,12 +807,15 @@ def run_case(name: str) -> int:
     targets = [(fields[i].data_ptr(), counts[i].data_ptr()) for i in range(n)]
     direct = [i for i, k in enumerate(stack.keyframes) if k.reference is None]
     deep = [i for i, k in enumerate(stack.keyframes) if k.reference is not None][::-1]
+    shallow = [i for i, k in enumerate(stack.keyframes) if k.shallow_reference is not None]
     subsets = {"direct_levels_4_13_960x540": direct[4:], "direct_levels_0_3_960x540": direct[:4],
-               "deep_levels_12_960x540": deep[:12], "stack_step_fhd": direct + deep}
-    repeats = 2 if name == "stack_step_fhd" else 1
-    for _ in range(repeats):
+               "deep_levels_12_960x540": deep[:12], "stack_step_fhd": direct + deep,
+               "atlas_e100_step_fhd": direct + deep, "atlas_e100_deep_24_960x540": deep[:24],
+               "atlas_e100_shallow_960x540": shallow}
+    full = name in ("stack_step_fhd", "atlas_e100_step_fhd")
+    for _ in range(2 if full else 1):
         stack.render_batch_device(targets, width, height, form=1, stream=stream.cuda_stream, order=subsets[name],
-                                  graph=name == "stack_step_fhd")
+                                  graph=full)
     torch.cuda.synchronize()
     stack.close()
     print("ok", name)
@@ -1174,7 +1177,8 @@ def main() -> int:
                         help="parent zoom of the timed atlas frame (child fraction = zoom / 4)")
     parser.add_argument("--case", default=None,
                         choices=["direct_levels_4_13_960x540", "direct_levels_0_3_960x540", "deep_levels_12_960x540",
-                                 "stack_step_fhd", "costnet_predict_20992", "kfp_colour_3840x2160",
+                                 "stack_step_fhd", "atlas_e100_step_fhd", "atlas_e100_deep_24_960x540",
+                                 "atlas_e100_shallow_960x540", "costnet_predict_20992", "kfp_colour_3840x2160",
                                  "aurora_colour_3840x2160", "atlas_colour_3840x2160"],
                         help="run one fixed piece of the workload for a profiler capture and exit")
     args = parser.parse_args()

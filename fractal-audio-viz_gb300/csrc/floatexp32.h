@@ -130,6 +130,7 @@ F32_HD F2e mul(const F2e& a, const F2e& b) {
 
 F32_HD F2e twice(const F2e& a) { return is_zero(a) ? a : make(a.x, a.y, a.e + 1); }
 
+
 F32_HD N1e n_norm(float m, int e) {
     if (m == 0.0f) {
         N1e r;

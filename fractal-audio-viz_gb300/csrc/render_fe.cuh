@@ -107,8 +107,9 @@ __device__ __forceinline__ const FxLinear* find_linear(const FxParams& p, int st
     return find_block(p.linear, p.linear_index, start, dn, max_length);
 }
 
-// Cubic bivariate map in Horner form (renderer.cpp:8686-8730).
-__device__ F2e apply_cubic(const FxCubic* s, const F2e& d, const F2e& c, int order) {
+// Cubic bivariate map in Horner form (renderer.cpp:8686-8730).  Not inlined:
+// the pixel loop's hot code stays small enough for the instruction cache.
+__device__ __noinline__ F2e apply_cubic(const FxCubic* s, const F2e& d, const F2e& c, int order) {
     const F2e k0 = ld_f2e(&s->c[0]);
     const F2e k1 = ld_f2e(&s->c[1]);
     if (order <= 1) return add(mul(k0, d), mul(k1, c));
@@ -178,7 +179,7 @@ __device__ __forceinline__ PixelOut escaped(float value, std::uint32_t count, co
 
 // apply_bla_series_derivative (renderer.cpp:8732-8795): the derivative with
 // respect to c through a cubic block, given dd = dd/dc on entry.
-__device__ F2e apply_cubic_derivative(const FxCubic* s, const F2e& d, const F2e& c, const F2e& dd, int order) {
+__device__ __noinline__ F2e apply_cubic_derivative(const FxCubic* s, const F2e& d, const F2e& c, const F2e& dd, int order) {
     const F2e k0 = ld_f2e(&s->c[0]);
     const F2e k1 = ld_f2e(&s->c[1]);
     if (order <= 1) return add(mul(k0, dd), k1);
@@ -202,7 +203,7 @@ __device__ F2e apply_cubic_derivative(const FxCubic* s, const F2e& d, const F2e&
 
 // Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).
 template <bool Planes>
-__device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc,
+__device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc,
                                F2e derivative) {
     const float dcr = to_float_x(dc), dci = to_float_y(dc);
     float dr = to_float_x(delta), di = to_float_y(delta);
@@ -261,7 +262,7 @@ __device__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const 
 
 // Direct recurrence from the total once the pixel has left the reference.
 template <bool Planes>
-__device__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc, F2e derivative) {
+__device__ __noinline__ PixelOut continue_direct(const FxParams& p, F2e total, int iteration, const F2e& dc, F2e derivative) {
     const F2e parameter = add(ld_f2e(&p.orbit[1].z), dc);
     const N1e limit = bailout(p.escape_mode);
     while (iteration < p.max_iter) {
