@@ -1039,11 +1039,10 @@ def song_levels():
     return levels, step
 
 
-def song_frame(t: int, frames: int, step: float, last_level: int):
-    """Atlas parameters of frame t on a constant-rate path 1e0 -> 1e100:
-    (parent level, parent zoom, child fraction); child zoom is the
-    overscan (visualizer.py:11959-11975, 666-696)."""
-    log_zoom = SONG_MAX_LOG * t / max(1, frames - 1)
+def song_frame(log_zoom: float, step: float, last_level: int):
+    """Atlas parameters of a frame at log10 zoom `log_zoom`: (parent level,
+    parent zoom, child fraction); child zoom is the overscan
+    (visualizer.py:11959-11975, 666-696)."""
     level = max(0, min(int(math.floor(log_zoom / step + 1.0e-9)), last_level))
     parent_zoom = max(1.0, SONG_OVERSCAN * 10.0 ** (log_zoom - level * step))
     fraction = min(1.0, max(0.0, parent_zoom / (SONG_FACTOR * SONG_OVERSCAN))) if level < last_level else 0.0
@@ -1056,10 +1055,13 @@ def run_song(args) -> int:
     rendered once (batched keyframe call, chosen form), then every frame is
     one raw KFP atlas frame (parent + child composed into a 4K surface, one
     KFP pass: 16 seeded stops, ColorMethod 7, Differences 3, slopes, dither)
-    into device RGB8.  The zoom path is a constant rate (the audio-driven
-    zoom plan is outside the path).  Reports fps and the iteration / colour
-    time shares; the reference creation (MPFR orbit, host) is reported
-    apart."""
+    into device RGB8.  The camera follows the song: a seeded synthetic track
+    (sines 110-880 Hz, pink noise, a 120-BPM onset train, a slow envelope;
+    song.synthesize) gives per-frame loudness and onsets (song.frame_controls)
+    that drive the reference's zoom plan from 1e0 to 1e100 (song.zoom_plan,
+    visualizer.py:6982; punch 3, quiet speed -0.04, the CLI defaults).
+    Reports fps and the iteration / colour time shares; the reference
+    creation (MPFR orbit, host) and the audio side are reported apart."""
     import torch
 
     package = __graft_entry__._package()
@@ -1069,7 +1071,12 @@ def run_song(args) -> int:
     stream = torch.cuda.Stream()
     width, height = 3840, 2160
     pixels = width * height
-    frames = int(round(args.song_seconds * 60))
+    t0 = time.perf_counter()
+    audio = package.song.synthesize(seconds=args.song_seconds)
+    loudness, onset = package.song.frame_controls(audio, fps=60.0)
+    plan = package.song.zoom_plan(loudness, 0.0, SONG_MAX_LOG, 3.0, -0.04, onset, 0.0)
+    audio_s = time.perf_counter() - t0
+    frames = len(plan)
     levels, step = song_levels()
     last = len(levels) - 1
     x, y = centre()
@@ -1098,7 +1105,7 @@ def run_song(args) -> int:
     rgb = torch.empty((2, pixels * 3), dtype=torch.uint8, device="cuda")
 
     def frame(t):
-        level, parent_zoom, fraction = song_frame(t, frames, step, last)
+        level, parent_zoom, fraction = song_frame(float(plan[t]), step, last)
         child = level + 1 if fraction > 0.0 else None
         status = library.fractal_gb300_atlas_colourise_kfp_raw_device(
             fields[level].data_ptr(), width, height, caps[level],
@@ -1141,6 +1148,10 @@ def run_song(args) -> int:
     stack.close()
     print(json.dumps({
         "workload": f"song 4K60: {frames} frames, {len(levels)} atlas tiles (factor 4, to 1e100), KFP raw atlas frames",
+        "camera": "zoom plan of the synthetic song (loudness punch 3, quiet speed -0.04)",
+        "plan_backward_frames": int(np.sum(np.diff(plan) < 0)),
+        "plan_levels_visited": int(len({song_frame(float(z), step, last)[0] for z in plan})),
+        "audio_side_s": round(audio_s, 2),
         "fps": round(frames / (total_ms / 1e3), 1),
         "fields_ms": round(fields_ms, 2), "frames_ms": round(frames_ms, 2),
         "frames_wall_ms": round(frames_wall_ms, 2),

@@ -32,6 +32,7 @@ kfp = _load("kfp")
 costnet = _load("costnet")
 frames = _load("frames")
 fields = _load("fields")
+song = _load("song")
 _builder = _load("build")
 LIBRARY_PATH = _builder.LIBRARY
 
