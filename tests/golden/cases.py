@@ -110,6 +110,7 @@ def parity_cases() -> list[dict]:
         _m("odd_37x23", kind="reference", centre=e30, log10_zoom=20.0, width=37, height=23,
            max_iter=20_000),
     ]
+    cases += deep_mandelbrot_cases()
     # FHD keyframe stack: a reduced-size sample of its levels.  Levels below
     # 1e12 take the direct path exactly as the atlas does
     # (visualizer.py:6152); deeper levels use the reference path with the
@@ -168,6 +169,20 @@ def alternate_cases() -> list[dict]:
 # Depths and caps of the deep alternate-formula fixtures: the batch
 # workload's range (zoom 1e10-1e100, caps 1e4-1e6) on small fields.
 DEEP_ALTERNATE_LEVELS = ((30.0, 100_000), (60.0, 300_000), (100.0, 1_000_000))
+
+
+def deep_mandelbrot_cases() -> list[dict]:
+    """Mandelbrot views deeper than 1e100: 1e300 (deltas near the bottom of
+    the double exponent range) on the 360-digit e100 centre and 1e1000
+    (beyond it: only the extended-exponent arithmetic represents them) on a
+    1060-digit centre; cap 50,000, 64x36."""
+    c = centres()
+    return [
+        _m("e300_64x36", kind="reference", centre=c["field_e100"], log10_zoom=300.0, width=64, height=36,
+           max_iter=50_000),
+        _m("e1000_64x36", kind="reference", centre=c["field_e1000"], log10_zoom=1000.0, width=64, height=36,
+           max_iter=50_000),
+    ]
 
 
 def deep_alternate_cases() -> list[dict]:

@@ -379,9 +379,23 @@ def add_deep_alternates(path: str) -> None:
         handle.write("\n")
 
 
+def add_deep_mandelbrot(path: str) -> None:
+    """Add a 1060-digit Misiurewicz centre (3600-bit Newton) for views beyond
+    the double exponent range (1e1000) to an existing centres.json."""
+    with open(path, encoding="ascii") as handle:
+        centres = json.load(handle)
+    centres["field_e1000"] = misiurewicz_centre(seed=20243, bits=3600, digits=1060)
+    with open(path, "w", encoding="ascii") as handle:
+        json.dump(centres, handle, indent=1)
+        handle.write("\n")
+
+
 def main() -> int:
     if "--deep-alternates" in sys.argv:
         add_deep_alternates(os.path.join(HERE, "centres.json"))
+        return 0
+    if "--deep-mandelbrot" in sys.argv:
+        add_deep_mandelbrot(os.path.join(HERE, "centres.json"))
         return 0
     centres = {
         # 640x360 at 1e30: 400-bit Newton, 120-digit strings.

@@ -69,12 +69,15 @@ def write_cases(library, cases, index) -> None:
 def main() -> int:
     native = _native()
     library = native.load(REFERENCE_LIBRARY)
-    if "--deep-alternates" in sys.argv:
-        # Only the deep alternate-formula fixtures, added to the index.
+    if "--deep-alternates" in sys.argv or "--deep-mandelbrot" in sys.argv:
+        # Only the deep alternate-formula (or beyond-1e100 Mandelbrot)
+        # fixtures, added to the index.
         path = os.path.join(FIXTURES, "index.json")
         with open(path, encoding="ascii") as handle:
             index = json.load(handle)
-        write_cases(library, case_defs.deep_alternate_cases(), index)
+        cases = (case_defs.deep_alternate_cases() if "--deep-alternates" in sys.argv
+                 else case_defs.deep_mandelbrot_cases())
+        write_cases(library, cases, index)
         with open(path, "w", encoding="ascii") as handle:
             json.dump(index, handle, indent=1, sort_keys=True)
             handle.write("\n")
