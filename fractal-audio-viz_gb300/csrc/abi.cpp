@@ -60,6 +60,10 @@ ThreadRuntime::~ThreadRuntime() {
     for (auto& entry : graphs) cudaGraphExecDestroy(entry.second);
     if (fork) cudaEventDestroy(fork);
     if (join) cudaEventDestroy(join);
+    for (int l = 0; l < kPlainLanes; ++l) {
+        if (lane_join[l]) cudaEventDestroy(lane_join[l]);
+        if (lanes[l]) cudaStreamDestroy(lanes[l]);
+    }
     if (side) cudaStreamDestroy(side);
     if (capture) cudaStreamDestroy(capture);
     if (stream) cudaStreamDestroy(stream);
@@ -88,6 +92,10 @@ ThreadRuntime& thread_runtime() {
         check_cuda(cudaStreamCreateWithFlags(&rt.capture, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaEventCreateWithFlags(&rt.fork, cudaEventDisableTiming), "cudaEventCreate");
         check_cuda(cudaEventCreateWithFlags(&rt.join, cudaEventDisableTiming), "cudaEventCreate");
+        for (int l = 0; l < ThreadRuntime::kPlainLanes; ++l) {
+            check_cuda(cudaStreamCreateWithFlags(&rt.lanes[l], cudaStreamNonBlocking), "cudaStreamCreate");
+            check_cuda(cudaEventCreateWithFlags(&rt.lane_join[l], cudaEventDisableTiming), "cudaEventCreate");
+        }
     }
     return rt;
 }
@@ -1520,6 +1528,9 @@ struct BatchPlan {
     int tiles = 0;
     int feature_rows = 0;
     std::vector<std::function<void(cudaStream_t)>> plain;
+    // A time budget stamps its origin per launch in one per-thread word, so
+    // budgeted plain launches stay one after another on one stream.
+    bool serial_plain = false;
     std::vector<std::shared_ptr<ReferenceContext>> contexts;
     std::string key;
     std::size_t direct_bytes = 0;
@@ -1565,15 +1576,22 @@ TileBuffers tile_buffers(char* base, int tiles, int rows) {
 void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime& rt, cudaStream_t main,
                    void* direct_scratch, unsigned long long* counter) {
     // The direct queue runs on the second stream beside the other launches;
-    // with an FP32 queue in the batch the plain-form (FP64) launches join it
-    // there, so the FP64 and FP32 pipes work at once.
+    // with an FP32 queue in the batch a single plain-form (FP64) launch joins
+    // it there, so the FP64 and FP32 pipes work at once.  Two or more
+    // plain-form launches are dealt over the lane streams instead (all forked
+    // from and joined back to the caller's stream), so their tails overlap.
+    // Fields that asked for derivative planes only share one discard region
+    // for the planes nobody reads; concurrent lanes may write it in any order.
+    const int lanes = plan.plain.size() > 1 && !plan.serial_plain
+        ? static_cast<int>(std::min<std::size_t>(ThreadRuntime::kPlainLanes, plan.plain.size())) : 0;
     const bool fork = (!plan.direct.empty() && (!plan.floatexp.empty() || !plan.plain.empty()))
         || (!plan.plain.empty() && !plan.floatexp.empty());
     cudaStream_t plain_stream = fork && !plan.floatexp.empty() ? rt.side : main;
     cudaStream_t direct_stream = fork ? rt.side : main;
-    if (fork) {
-        check_cuda(cudaEventRecord(rt.fork, main), "cudaEventRecord (fork)");
-        check_cuda(cudaStreamWaitEvent(rt.side, rt.fork, 0), "cudaStreamWaitEvent (fork)");
+    if (fork || lanes > 0) check_cuda(cudaEventRecord(rt.fork, main), "cudaEventRecord (fork)");
+    if (fork) check_cuda(cudaStreamWaitEvent(rt.side, rt.fork, 0), "cudaStreamWaitEvent (fork)");
+    for (int l = 0; l < lanes; ++l) {
+        check_cuda(cudaStreamWaitEvent(rt.lanes[l], rt.fork, 0), "cudaStreamWaitEvent (lane fork)");
     }
     for (const auto& group : plan.direct) {
         const std::vector<DirectParams>& fields = group.second;
@@ -1624,7 +1642,15 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
                        "floatexp batch launch");
         }
     }
-    for (const auto& launch : plan.plain) launch(plain_stream);
+    if (lanes > 0) {
+        for (std::size_t i = 0; i < plan.plain.size(); ++i) plan.plain[i](rt.lanes[i % lanes]);
+        for (int l = 0; l < lanes; ++l) {
+            check_cuda(cudaEventRecord(rt.lane_join[l], rt.lanes[l]), "cudaEventRecord (lane join)");
+            check_cuda(cudaStreamWaitEvent(main, rt.lane_join[l], 0), "cudaStreamWaitEvent (lane join)");
+        }
+    } else {
+        for (const auto& launch : plan.plain) launch(plain_stream);
+    }
     if (fork) {
         check_cuda(cudaEventRecord(rt.join, rt.side), "cudaEventRecord (join)");
         check_cuda(cudaStreamWaitEvent(main, rt.join, 0), "cudaStreamWaitEvent (join)");
@@ -1830,6 +1856,7 @@ void render_field_batch(const std::vector<FieldRequest>& fields, const char* x_c
     cudaStream_t stream = stream_handle ? static_cast<cudaStream_t>(stream_handle) : rt.stream;
     BatchPlan plan;
     plan.fast_smooth = form == 1;
+    plan.serial_plain = o.time_budget_ms > 0;
     append_bytes(plan.key, form);
     std::size_t direct_doubles = 0;
     bool centre_parsed = false;

@@ -214,7 +214,19 @@ __device__ const AltStep* alt_lookup(const AltParams& p, int start, const Fe& dn
     if (offset < 0 || offset >= p.alt_index.count[0]) return nullptr;
     int top = 31 - __clz(max_length);
     top = top < p.alt_index.levels - 1 ? top : p.alt_index.levels - 1;
-    for (int level = top; level >= 0; --level) {
+    // Only blocks of two or more steps are taken, and they start at even
+    // offsets.  At one start the radii never grow with the level (a merge
+    // keeps at most its first half's radius, times 1 - 2^-40; an unpaired
+    // entry is copied), so a delta outside the two-step block's finite
+    // radius is outside every longer block's too: one load settles the
+    // common case of a delta too large for any block, with the same result
+    // as the full top-down search.
+    if (top < 1 || (offset & 1) != 0) return nullptr;
+    if ((offset >> 1) < p.alt_index.count[1]) {
+        const Fe r2 = ld_fe(&p.alt[p.alt_index.offset[1] + (offset >> 1)].r2);
+        if (fe_finite(r2) && fe_cmp(dn, r2) >= 0) return nullptr;
+    }
+    for (int level = top; level >= 1; --level) {
         if ((offset & ((1 << level) - 1)) != 0) continue;
         const int index = offset >> level;
         if (index >= p.alt_index.count[level]) continue;

@@ -98,7 +98,15 @@ __device__ const FxAltStep* alt_lookup(const FxParams& p, int start, const N1e& 
     if (offset < 0 || offset >= __ldg(&index->count[0])) return nullptr;
     int top = 31 - __clz(max_length);
     top = top < levels - 1 ? top : levels - 1;
-    for (int level = top; level >= 0; --level) {
+    // One load settles a delta too large for any block: radii never grow
+    // with the level at one start (see the FP64 lookup), and the FP32 radii
+    // are the FP64 ones rounded to nearest, which keeps their order.
+    if (top < 1 || (offset & 1) != 0) return nullptr;
+    if ((offset >> 1) < __ldg(&index->count[1])) {
+        const N1e r2 = ld_n1e(&p.alt[__ldg(&index->offset[1]) + (offset >> 1)].r2);
+        if (r2.e != 0x3fffffff && n_cmp(dn, r2) >= 0) return nullptr;
+    }
+    for (int level = top; level >= 1; --level) {
         if ((offset & ((1 << level) - 1)) != 0) continue;
         const int at = offset >> level;
         if (at >= __ldg(&index->count[level])) continue;

@@ -71,6 +71,12 @@ struct ThreadRuntime {
     cudaEvent_t fork = nullptr;
     cudaEvent_t join = nullptr;
     std::map<std::string, cudaGraphExec_t> graphs;
+    // Plain-form (FP64) fields of a batch are dealt over these streams, so a
+    // field's long-orbit tail overlaps the next fields' launches instead of
+    // holding the GPU mostly idle until it ends.
+    static constexpr int kPlainLanes = 8;
+    cudaStream_t lanes[kPlainLanes] = {};
+    cudaEvent_t lane_join[kPlainLanes] = {};
     int last_shapes[4] = {};
     int pinned_shapes[4] = {};  // set by fractal_gb300_set_queue_shapes
     void* costnet = nullptr;    // attached tile-cost network (not owned)
