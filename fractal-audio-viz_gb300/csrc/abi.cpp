@@ -327,9 +327,22 @@ void launch_deep_mandelbrot(ReferenceContext& ctx, DeviceTables& dev, const Outp
                "plain Mandelbrot kernel launch");
 }
 
+// Claim counters of the alternate-formula queue: one 256-byte slot per lane
+// stream of a batch, and one (the last) for single renders.
+constexpr int kAltQueueSlots = ThreadRuntime::kPlainLanes + 1;
+constexpr std::size_t kAltQueueStride = 256 / sizeof(unsigned long long);
+
+unsigned long long* alt_queue_counters(ThreadRuntime& rt) {
+    return static_cast<unsigned long long*>(scratch(rt, kScratchAltQueue, kAltQueueSlots * 256));
+}
+
+// `queue_counter`: the claim counter of the lane-refill queue (a batch
+// passes its lane's slot); NULL takes the single-render slot, and point
+// lists always run one thread per point.
 void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outputs& out, int width, int height,
                            const fx::Fe& zoom, int max_iter, const FractalRenderOptions& o, bool collect_stats,
-                           ThreadRuntime& rt, cudaStream_t stream, const PointInput* points = nullptr) {
+                           ThreadRuntime& rt, cudaStream_t stream, const PointInput* points = nullptr,
+                           unsigned long long* queue_counter = nullptr) {
     const DeepGeometry g = deep_geometry(zoom, width, height, o.coordinate_mode);
     AltParams p{};
     p.orbit = dev.orbit;
@@ -382,7 +395,11 @@ void launch_deep_alternate(ReferenceContext& ctx, DeviceTables& dev, const Outpu
         p.budget_ns = static_cast<unsigned long long>(o.time_budget_ms) * 1000000ull;
     }
     p.stats = collect_stats ? rt.stats : nullptr;
-    check_cuda(launch_plain_alternate(p, out.p_iter != nullptr, collect_stats, stream),
+    if (points == nullptr && queue_counter == nullptr) {
+        queue_counter = alt_queue_counters(rt) + (kAltQueueSlots - 1) * kAltQueueStride;
+    }
+    check_cuda(launch_plain_alternate(p, out.p_iter != nullptr, collect_stats, points ? nullptr : queue_counter,
+                                      stream),
                "plain alternate-formula kernel launch");
 }
 
@@ -1527,7 +1544,9 @@ struct BatchPlan {
     mlp::CostNet* net = nullptr;
     int tiles = 0;
     int feature_rows = 0;
-    std::vector<std::function<void(cudaStream_t)>> plain;
+    // Plain-form launches: (stream, the alternate queue's claim counter for
+    // that stream).
+    std::vector<std::function<void(cudaStream_t, unsigned long long*)>> plain;
     // A time budget stamps its origin per launch in one per-thread word, so
     // budgeted plain launches stay one after another on one stream.
     bool serial_plain = false;
@@ -1574,7 +1593,7 @@ TileBuffers tile_buffers(char* base, int tiles, int rows) {
 }
 
 void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime& rt, cudaStream_t main,
-                   void* direct_scratch, unsigned long long* counter) {
+                   void* direct_scratch, unsigned long long* counter, unsigned long long* alt_counters) {
     // The direct queue runs on the second stream beside the other launches;
     // with an FP32 queue in the batch a single plain-form (FP64) launch joins
     // it there, so the FP64 and FP32 pipes work at once.  Two or more
@@ -1643,13 +1662,15 @@ void enqueue_batch(const BatchPlan& plan, const BatchShapes& shapes, ThreadRunti
         }
     }
     if (lanes > 0) {
-        for (std::size_t i = 0; i < plan.plain.size(); ++i) plan.plain[i](rt.lanes[i % lanes]);
+        for (std::size_t i = 0; i < plan.plain.size(); ++i) {
+            plan.plain[i](rt.lanes[i % lanes], alt_counters + (i % lanes) * kAltQueueStride);
+        }
         for (int l = 0; l < lanes; ++l) {
             check_cuda(cudaEventRecord(rt.lane_join[l], rt.lanes[l]), "cudaEventRecord (lane join)");
             check_cuda(cudaStreamWaitEvent(main, rt.lane_join[l], 0), "cudaStreamWaitEvent (lane join)");
         }
     } else {
-        for (const auto& launch : plan.plain) launch(plain_stream);
+        for (const auto& launch : plan.plain) launch(plain_stream, alt_counters);
     }
     if (fork) {
         check_cuda(cudaEventRecord(rt.join, rt.side), "cudaEventRecord (join)");
@@ -1661,14 +1682,16 @@ void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime
                  bool graph) {
     void* direct_scratch = plan.direct.empty() ? nullptr : scratch(rt, kScratchDirect, plan.direct_bytes);
     auto* counter = static_cast<unsigned long long*>(scratch(rt, kScratchQueue, 256));
+    unsigned long long* alt_counters = plan.plain.empty() ? nullptr : alt_queue_counters(rt);
     if (!graph) {
-        enqueue_batch(plan, shapes, rt, stream, direct_scratch, counter);
+        enqueue_batch(plan, shapes, rt, stream, direct_scratch, counter, alt_counters);
         return;
     }
     std::string key = plan.key;
     append_bytes(key, shapes);
     append_bytes(key, direct_scratch);
     append_bytes(key, counter);
+    append_bytes(key, alt_counters);
     auto found = rt.graphs.find(key);
     if (found == rt.graphs.end()) {
         if (rt.graphs.size() >= 16) {
@@ -1678,7 +1701,7 @@ void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime
         }
         check_cuda(cudaStreamBeginCapture(rt.capture, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
         try {
-            enqueue_batch(plan, shapes, rt, rt.capture, direct_scratch, counter);
+            enqueue_batch(plan, shapes, rt, rt.capture, direct_scratch, counter, alt_counters);
         } catch (...) {
             cudaGraph_t broken = nullptr;
             cudaStreamEndCapture(rt.capture, &broken);
@@ -1952,9 +1975,10 @@ void render_field_batch(const std::vector<FieldRequest>& fields, const char* x_c
         ReferenceContext* raw = ctx.get();
         const int max_iter = frame.max_iter;
         plan.plain.push_back([raw, dev, out, width, height, zoom, max_iter, series_order, series_block, o,
-                              &rt](cudaStream_t s) {
+                              &rt](cudaStream_t s, unsigned long long* queue_counter) {
             if (raw->formula != kFormulaMandelbrot) {
-                launch_deep_alternate(*raw, *dev, out, width, height, zoom, max_iter, o, false, rt, s);
+                launch_deep_alternate(*raw, *dev, out, width, height, zoom, max_iter, o, false, rt, s, nullptr,
+                                      queue_counter);
             } else {
                 launch_deep_mandelbrot(*raw, *dev, out, width, height, zoom, max_iter, series_order,
                                        series_block, o, false, rt, s);

@@ -442,8 +442,12 @@ void render_floatexp_from_reference(ReferenceContext& ctx, const Outputs& out, i
                                     cudaStream_t stream);
 
 cudaError_t launch_plain_mandelbrot(const PlainParams& params, bool planes, bool stats, cudaStream_t stream);
+// With `queue_counter` (8 bytes of device memory no other launch uses at
+// the same time) a Julia field renders through the persistent lane-refill
+// queue; other formulas, point lists and calls without a counter run one
+// thread per pixel.
 cudaError_t launch_plain_alternate(const AltParams& params, bool planes, bool stats,
-                                   cudaStream_t stream);
+                                   unsigned long long* queue_counter, cudaStream_t stream);
 // A batch of direct fields (one kernel over all of them); the batch struct
 // travels as a __grid_constant__ kernel parameter.
 constexpr int kMaxDirectFields = 64;

@@ -46,6 +46,7 @@ enum ScratchSlot {
     kScratchPlanesIn,
     kScratchPlanesOut,
     kScratchDiscard,  // planes a batch's plain kernels write but no caller asked for
+    kScratchAltQueue, // claim counters of the alternate-formula queue (one per lane stream + one)
     kScratchCount
 };
 
