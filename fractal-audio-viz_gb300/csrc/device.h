@@ -310,7 +310,7 @@ constexpr int kStatsSlots = 39;
 // (k >= 1) with u = dc * 2^-scale, |u| <= 1 over the view, so every pixel
 // evaluates it in plain float (kernel-side prologue, render_fe.cu).
 constexpr int kMaxSeriesTerms = 33;
-struct FxSeriesScaled {
+struct alignas(8) FxSeriesScaled {
     float b[kMaxSeriesTerms][2];
     int terms;
     int shift;

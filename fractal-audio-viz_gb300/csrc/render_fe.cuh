@@ -68,6 +68,12 @@ __device__ __forceinline__ float smooth_from_norm(int iteration, const N1e& n, f
 // Near a periodic reference (|Z| close to 0) that zero flags a glitch the
 // exact norm would not.  This applies the same quantisation to the FP32 norm
 // where it is coarser than the FP32 mantissa.
+// The plain-float orbit value Z_i in one 8-byte load (records are 32 bytes
+// from a cudaMalloc base, so zr / zi sit 8-byte aligned).
+__device__ __forceinline__ float2 orbit_float(const FxOrbitRec* orbit, int i) {
+    return __ldg(reinterpret_cast<const float2*>(&orbit[i].zr));
+}
+
 __device__ __forceinline__ N1e reference_norm(const N1e& n, int mode) {
     const int place = mode == 1 ? -26 : -51;
     if (n.m == 0.0f || n.e >= place + 24) return n;
@@ -212,46 +218,64 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
     int steps = 0, rebases = 0;
     const bool strict = p.strict != 0;
     const PixelOut unresolved_out = out_of(nan32(), 0u);
-    float zr = __ldg(&p.orbit[ref].zr), zi = __ldg(&p.orbit[ref].zi);
-    while (iteration < p.max_iter && ref + 1 < p.orbit_size) {
-        if constexpr (Planes) derivative = derivative_step(norm(zr + dr, zi + di, 0), derivative);
-        const float lr = 2.0f * (zr * dr - zi * di);
-        const float li = 2.0f * (zr * di + zi * dr);
-        const float sr = dr * dr - di * di;
-        const float si = 2.0f * dr * di;
-        dr = lr + sr + dcr;
-        di = li + si + dci;
-        ++ref;
-        ++iteration;
-        if (++steps > 65536) {
-            return strict ? unresolved_out
-                          : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
-        }
-        zr = __ldg(&p.orbit[ref].zr);
-        zi = __ldg(&p.orbit[ref].zi);
-        const float tr = zr + dr, ti = zi + di;
-        const float m2 = tr * tr + ti * ti;
-        if (!isfinite(m2)) {
-            return strict ? unresolved_out
-                          : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
-        }
-        if (m2 > escape2) {
-            const float mag = sqrtf(fmaxf(m2, safe2));
-            return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
-                                   static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
-        }
-        if (m2 < dr * dr + di * di) {
-            dr = tr;
-            di = ti;
-            ref = 0;
-            zr = __ldg(&p.orbit[0].zr);
-            zi = __ldg(&p.orbit[0].zi);
-            if (++rebases > 64) {
+    float2 z = orbit_float(p.orbit, ref);
+    // The loop runs while iteration < max_iter and ref + 1 < orbit_size and
+    // gives up on its 65537th step.  Between rebases ref and iteration
+    // advance together, so the number of steps to the first of those bounds
+    // is known up front and each step tests one count instead of three.
+    while (true) {
+        const int room = min(p.max_iter - iteration, p.orbit_size - 1 - ref);
+        if (room <= 0) break;
+        const int to_limit = 65537 - steps;
+        const bool limited = room >= to_limit;
+        const int run = limited ? to_limit : room;
+        bool rebased = false;
+        for (int left = run; left > 0; --left) {
+            if constexpr (Planes) derivative = derivative_step(norm(z.x + dr, z.y + di, 0), derivative);
+            // d' = (2Z + d) d + dc, in FMA form as the shallow mode has it.
+            const float ar = fmaf(2.0f, z.x, dr), ai = fmaf(2.0f, z.y, di);
+            const float nr = fmaf(dr, ar, fmaf(-di, ai, dcr));
+            const float ni = fmaf(2.0f, fmaf(z.x, di, dr * (z.y + di)), dci);
+            dr = nr;
+            di = ni;
+            ++ref;
+            ++iteration;
+            if (limited && left == 1) {
                 return strict ? unresolved_out
                               : out_of(static_cast<float>(iteration) - p.output_bias,
                                        static_cast<std::uint32_t>(iteration));
             }
+            z = orbit_float(p.orbit, ref);
+            const float tr = z.x + dr, ti = z.y + di;
+            const float m2 = fmaf(tr, tr, ti * ti);
+            // One test for escape and overflow: a NaN or infinite norm fails
+            // m2 <= escape2 as an escaping one does.
+            if (!(m2 <= escape2)) {
+                if (!isfinite(m2)) {
+                    return strict ? unresolved_out
+                                  : out_of(static_cast<float>(iteration) - p.output_bias,
+                                           static_cast<std::uint32_t>(iteration));
+                }
+                const float mag = sqrtf(fmaxf(m2, safe2));
+                return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                                       static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
+            }
+            if (m2 < fmaf(dr, dr, di * di)) {
+                dr = tr;
+                di = ti;
+                ref = 0;
+                z = orbit_float(p.orbit, 0);
+                if (++rebases > 64) {
+                    return strict ? unresolved_out
+                                  : out_of(static_cast<float>(iteration) - p.output_bias,
+                                           static_cast<std::uint32_t>(iteration));
+                }
+                steps += run - left + 1;
+                rebased = true;
+                break;
+            }
         }
+        if (!rebased) break;
     }
     if (iteration < p.max_iter) {
         return strict ? unresolved_out
@@ -375,8 +399,12 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             const float ur = ldexpf_fast(p.view_width.x * xf, p.view_width.e - scale);
             const float ui = ldexpf_fast(p.view_height.x * yf, p.view_height.e - scale);
             const int terms = __ldg(&sc->terms);
-            float vr = __ldg(&sc->b[terms - 1][0]);
-            float vi = __ldg(&sc->b[terms - 1][1]);
+            // Coefficient pairs in one 8-byte load each (the struct's pairs
+            // are 8-byte aligned).
+            const float2* b = reinterpret_cast<const float2*>(sc->b);
+            const float2 top = __ldg(b + terms - 1);
+            float vr = top.x;
+            float vi = top.y;
             float wr = 0.0f, wi = 0.0f;  // derivative of the inner polynomial
             for (int k = terms - 1; k > 1; --k) {
                 if constexpr (Planes) {
@@ -385,8 +413,9 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
                     wr = nwr;
                     wi = nwi;
                 }
-                const float nr = fmaf(vr, ur, fmaf(-vi, ui, __ldg(&sc->b[k - 1][0])));
-                const float ni = fmaf(vr, ui, fmaf(vi, ur, __ldg(&sc->b[k - 1][1])));
+                const float2 bk = __ldg(b + k - 1);
+                const float nr = fmaf(vr, ur, fmaf(-vi, ui, bk.x));
+                const float ni = fmaf(vr, ui, fmaf(vi, ur, bk.y));
                 vr = nr;
                 vi = ni;
             }
