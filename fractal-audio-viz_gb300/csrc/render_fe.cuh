@@ -221,16 +221,19 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
     float2 z = orbit_float(p.orbit, ref);
     // The loop runs while iteration < max_iter and ref + 1 < orbit_size and
     // gives up on its 65537th step.  Between rebases ref and iteration
-    // advance together, so the number of steps to the first of those bounds
-    // is known up front and each step tests one count instead of three.
+    // advance together, so the steps to the first of those bounds are known
+    // up front: a run takes them with one counter, and the step that would
+    // exceed the limit is not computed (its output needs only the count).
     while (true) {
         const int room = min(p.max_iter - iteration, p.orbit_size - 1 - ref);
         if (room <= 0) break;
         const int to_limit = 65537 - steps;
         const bool limited = room >= to_limit;
-        const int run = limited ? to_limit : room;
+        const int run = limited ? to_limit - 1 : room;
+        const float2* next = reinterpret_cast<const float2*>(p.orbit + ref + 1);
+        constexpr int kStride = sizeof(FxOrbitRec) / sizeof(float2);
         bool rebased = false;
-        for (int left = run; left > 0; --left) {
+        for (int k = 0; k < run; ++k) {
             if constexpr (Planes) derivative = derivative_step(norm(z.x + dr, z.y + di, 0), derivative);
             // d' = (2Z + d) d + dc, in FMA form as the shallow mode has it.
             const float ar = fmaf(2.0f, z.x, dr), ai = fmaf(2.0f, z.y, di);
@@ -238,19 +241,13 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
             const float ni = fmaf(2.0f, fmaf(z.x, di, dr * (z.y + di)), dci);
             dr = nr;
             di = ni;
-            ++ref;
-            ++iteration;
-            if (limited && left == 1) {
-                return strict ? unresolved_out
-                              : out_of(static_cast<float>(iteration) - p.output_bias,
-                                       static_cast<std::uint32_t>(iteration));
-            }
-            z = orbit_float(p.orbit, ref);
+            z = __ldg(next + k * kStride);
             const float tr = z.x + dr, ti = z.y + di;
             const float m2 = fmaf(tr, tr, ti * ti);
             // One test for escape and overflow: a NaN or infinite norm fails
             // m2 <= escape2 as an escaping one does.
             if (!(m2 <= escape2)) {
+                iteration += k + 1;
                 if (!isfinite(m2)) {
                     return strict ? unresolved_out
                                   : out_of(static_cast<float>(iteration) - p.output_bias,
@@ -261,6 +258,7 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
                                        static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
             }
             if (m2 < fmaf(dr, dr, di * di)) {
+                iteration += k + 1;
                 dr = tr;
                 di = ti;
                 ref = 0;
@@ -270,12 +268,19 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
                                   : out_of(static_cast<float>(iteration) - p.output_bias,
                                            static_cast<std::uint32_t>(iteration));
                 }
-                steps += run - left + 1;
+                steps += k + 1;
                 rebased = true;
                 break;
             }
         }
-        if (!rebased) break;
+        if (rebased) continue;
+        iteration += run;
+        if (limited) {
+            ++iteration;
+            return strict ? unresolved_out
+                          : out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
+        }
+        break;
     }
     if (iteration < p.max_iter) {
         return strict ? unresolved_out
