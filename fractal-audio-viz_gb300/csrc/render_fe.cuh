@@ -93,6 +93,19 @@ __device__ const Step* find_block(const Step* table, const LevelIndex* index, in
     int top = 31 - __clz(max_length);
     top = top < levels - 1 ? top : levels - 1;
     const int offset = start - 1;
+    // Blocks of two or more steps start at even offsets.  At one start a
+    // level's squared radius is at most the level below's, up to rounding
+    // (each merge keeps at most its first half's radius; a compacted zero
+    // radius is not used here), so a delta outside the two-step block's
+    // radius by more than that rounding (2^-20 relative) fits no block: one
+    // load replaces the failing top-down search.
+    if (top < 1 || (offset & 1) != 0) return nullptr;
+    if ((offset >> 1) < __ldg(&index->count[1])) {
+        const N1e r2 = ld_n1e(&table[__ldg(&index->offset[1]) + (offset >> 1)].r2);
+        if (r2.m > 0.0f && r2.e != 0x3fffffff && n_cmp(dn, n_norm(r2.m * 1.00000095367431640625f, r2.e)) >= 0) {
+            return nullptr;
+        }
+    }
     for (int level = top; level >= 1; --level) {
         if ((offset & ((1 << level) - 1)) != 0) continue;
         const int at = offset >> level;
@@ -349,32 +362,42 @@ __device__ __noinline__ PixelOut shallow_pixel(const FxParams& p, int px, int py
     float dr = 0.0f, di = 0.0f;
     float zr = 0.0f, zi = 0.0f;  // Z_0
     F2e derivative = zero();
-    int ref = 0;
-    for (int iteration = 1; iteration <= p.max_iter; ++iteration) {
-        if constexpr (Planes) derivative = derivative_step(norm(zr + dr, zi + di, 0), derivative);
-        const float ar = fmaf(2.0f, zr, dr), ai = fmaf(2.0f, zi, di);
-        const float nr = fmaf(dr, ar, fmaf(-di, ai, dcr));
-        const float ni = fmaf(2.0f, fmaf(zr, di, dr * (zi + di)), dci);
-        dr = nr;
-        di = ni;
-        ++ref;
-        const float2 z = __ldg(orbit + static_cast<long long>(ref) * kStride);
-        zr = z.x;
-        zi = z.y;
-        const float tr = zr + dr, ti = zi + di;
-        const float m2 = fmaf(tr, tr, ti * ti);
-        if (m2 > escape2) {
-            const float mag = sqrtf(fmaxf(m2, safe2));
-            return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
-                                   static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
+    // Runs from Z_0: each takes up to `valid` steps (the orbit's last usable
+    // entry) or the iterations left, with one counter; a rebase (|Z + d| <
+    // |d|, or the run reaching `valid`) starts the next run from Z_0.
+    int done = 0;  // iterations completed
+    while (done < p.max_iter) {
+        const int run = min(valid, p.max_iter - done);
+        int k = 1;
+        bool rebase = false;
+        for (; k <= run; ++k) {
+            if constexpr (Planes) derivative = derivative_step(norm(zr + dr, zi + di, 0), derivative);
+            const float ar = fmaf(2.0f, zr, dr), ai = fmaf(2.0f, zi, di);
+            const float nr = fmaf(dr, ar, fmaf(-di, ai, dcr));
+            const float ni = fmaf(2.0f, fmaf(zr, di, dr * (zi + di)), dci);
+            dr = nr;
+            di = ni;
+            const float2 z = __ldg(orbit + static_cast<long long>(k) * kStride);
+            zr = z.x;
+            zi = z.y;
+            const float tr = zr + dr, ti = zi + di;
+            const float m2 = fmaf(tr, tr, ti * ti);
+            if (m2 > escape2) {
+                const int iteration = done + k;
+                const float mag = sqrtf(fmaxf(m2, safe2));
+                return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
+                                       static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
+            }
+            if (m2 < fmaf(dr, dr, di * di) || k == valid) {
+                dr = tr;
+                di = ti;
+                zr = 0.0f;
+                zi = 0.0f;
+                rebase = true;
+                break;
+            }
         }
-        if (m2 < fmaf(dr, dr, di * di) || ref >= valid) {
-            dr = tr;
-            di = ti;
-            zr = 0.0f;
-            zi = 0.0f;
-            ref = 0;
-        }
+        done += rebase ? k : run;
     }
     return inside;
 }
@@ -411,6 +434,7 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             float vr = top.x;
             float vi = top.y;
             float wr = 0.0f, wi = 0.0f;  // derivative of the inner polynomial
+#pragma unroll 4
             for (int k = terms - 1; k > 1; --k) {
                 if constexpr (Planes) {
                     const float nwr = fmaf(wr, ur, fmaf(-wi, ui, vr));
