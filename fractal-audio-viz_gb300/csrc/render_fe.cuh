@@ -93,19 +93,6 @@ __device__ const Step* find_block(const Step* table, const LevelIndex* index, in
     int top = 31 - __clz(max_length);
     top = top < levels - 1 ? top : levels - 1;
     const int offset = start - 1;
-    // Blocks of two or more steps start at even offsets.  At one start a
-    // level's squared radius is at most the level below's, up to rounding
-    // (each merge keeps at most its first half's radius; a compacted zero
-    // radius is not used here), so a delta outside the two-step block's
-    // radius by more than that rounding (2^-20 relative) fits no block: one
-    // load replaces the failing top-down search.
-    if (top < 1 || (offset & 1) != 0) return nullptr;
-    if ((offset >> 1) < __ldg(&index->count[1])) {
-        const N1e r2 = ld_n1e(&table[__ldg(&index->offset[1]) + (offset >> 1)].r2);
-        if (r2.m > 0.0f && r2.e != 0x3fffffff && n_cmp(dn, n_norm(r2.m * 1.00000095367431640625f, r2.e)) >= 0) {
-            return nullptr;
-        }
-    }
     for (int level = top; level >= 1; --level) {
         if ((offset & ((1 << level) - 1)) != 0) continue;
         const int at = offset >> level;
