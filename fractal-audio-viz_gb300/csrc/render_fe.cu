@@ -72,14 +72,21 @@ __global__ void series_prologue_kernel(const __grid_constant__ FxBatch b) {
     if (shift == -0x3fffffff) shift = 0;
     out->b[0][0] = 0.0f;
     out->b[0][1] = 0.0f;
+    // Trailing terms below 2^-48 of the largest are dropped from the pixels'
+    // Horner loop: with |u| <= 1 each is smaller than that largest term
+    // times u^k by more than float rounding can see.  (Terms inside the kept
+    // range stay, however small: a small low-order coefficient still
+    // dominates near the view's centre.)
+    int used = 2;
     for (int k = 1; k < terms; ++k) {
         const f32x::F2e c = p.series[k];
         const long long d = static_cast<long long>(c.e) + static_cast<long long>(k) * scale - shift;
         const bool keep = d > -200 && !(c.x == 0.0f && c.y == 0.0f);
         out->b[k][0] = keep ? f32x::ldexpf_fast(c.x, static_cast<int>(d)) : 0.0f;
         out->b[k][1] = keep ? f32x::ldexpf_fast(c.y, static_cast<int>(d)) : 0.0f;
+        if (keep && d > -48 && k + 1 > used) used = k + 1;
     }
-    out->terms = terms;
+    out->terms = used < terms ? used : terms;
     out->shift = shift;
     out->scale = scale;
 }

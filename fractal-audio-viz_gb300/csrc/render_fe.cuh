@@ -77,7 +77,7 @@ __device__ __forceinline__ float2 orbit_float(const FxOrbitRec* orbit, int i) {
 __device__ __forceinline__ N1e reference_norm(const N1e& n, int mode) {
     const int place = mode == 1 ? -26 : -51;
     if (n.m == 0.0f || n.e >= place + 24) return n;
-    const float units = rintf(ldexpf(n.m, n.e - place));
+    const float units = rintf(ldexpf_fast(n.m, n.e - place));
     return n_norm(units, place);
 }
 
@@ -232,8 +232,14 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
         const int run = limited ? to_limit - 1 : room;
         const float2* next = reinterpret_cast<const float2*>(p.orbit + ref + 1);
         constexpr int kStride = sizeof(FxOrbitRec) / sizeof(float2);
-        bool rebased = false;
-        for (int k = 0; k < run; ++k) {
+        // A step leaves the run on escape or overflow (a NaN or infinite
+        // norm fails m2 <= escape2 as an escaping one does) or to rebase
+        // (|Z + d| < |d|): one branch per step, sorted out after the loop.
+        int k = 0;
+        float tr = 0.0f, ti = 0.0f, m2 = 0.0f;
+        bool left_run = false;
+#pragma unroll 2
+        for (; k < run; ++k) {
             if constexpr (Planes) derivative = derivative_step(norm(z.x + dr, z.y + di, 0), derivative);
             // d' = (2Z + d) d + dc, in FMA form as the shallow mode has it.
             const float ar = fmaf(2.0f, z.x, dr), ai = fmaf(2.0f, z.y, di);
@@ -242,12 +248,17 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
             dr = nr;
             di = ni;
             z = __ldg(next + k * kStride);
-            const float tr = z.x + dr, ti = z.y + di;
-            const float m2 = fmaf(tr, tr, ti * ti);
-            // One test for escape and overflow: a NaN or infinite norm fails
-            // m2 <= escape2 as an escaping one does.
+            tr = z.x + dr;
+            ti = z.y + di;
+            m2 = fmaf(tr, tr, ti * ti);
+            if (!(m2 <= escape2) | (m2 < fmaf(dr, dr, di * di))) {
+                left_run = true;
+                break;
+            }
+        }
+        if (left_run) {
+            iteration += k + 1;
             if (!(m2 <= escape2)) {
-                iteration += k + 1;
                 if (!isfinite(m2)) {
                     return strict ? unresolved_out
                                   : out_of(static_cast<float>(iteration) - p.output_bias,
@@ -257,23 +268,18 @@ __device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, in
                 return escaped<Planes>((static_cast<float>(iteration) - __logf(__logf(mag)) * kInvLn2) - p.output_bias,
                                        static_cast<std::uint32_t>(iteration), norm(tr, ti, 0), derivative, p);
             }
-            if (m2 < fmaf(dr, dr, di * di)) {
-                iteration += k + 1;
-                dr = tr;
-                di = ti;
-                ref = 0;
-                z = orbit_float(p.orbit, 0);
-                if (++rebases > 64) {
-                    return strict ? unresolved_out
-                                  : out_of(static_cast<float>(iteration) - p.output_bias,
-                                           static_cast<std::uint32_t>(iteration));
-                }
-                steps += k + 1;
-                rebased = true;
-                break;
+            dr = tr;
+            di = ti;
+            ref = 0;
+            z = orbit_float(p.orbit, 0);
+            if (++rebases > 64) {
+                return strict ? unresolved_out
+                              : out_of(static_cast<float>(iteration) - p.output_bias,
+                                       static_cast<std::uint32_t>(iteration));
             }
+            steps += k + 1;
+            continue;
         }
-        if (rebased) continue;
         iteration += run;
         if (limited) {
             ++iteration;
