@@ -28,8 +28,9 @@ struct LevelIndex {
     int count[kMaxLevels] = {};
 };
 
-// FP32-mantissa / int32-exponent mirrors used by the floatexp form.
-struct FxOrbitRec {
+// FP32-mantissa / int32-exponent mirrors used by the floatexp form.  The
+// records are 16-byte aligned so that kernels read them in 16-byte loads.
+struct alignas(16) FxOrbitRec {
     float zr, zi;  // Z_i as plain float (0 below the float range)
     f32x::F2e z;   // Z_i as floatexp
     // Mandelbrot references: |Z_i|^2.  Other formulas: the signed escape
@@ -47,20 +48,25 @@ struct FxAltStep {
     int pad;
 };
 
-struct FxLinear {
+// BLA blocks start with a 16-byte head (squared radius, length), so the
+// lookup reads a level's candidate with one load.
+struct alignas(16) FxLinear {
+    f32x::N1e r2;
+    int len;
+    int pad;
     f32x::F2e a;
     f32x::F2e b;
-    f32x::N1e r2;
-    int len;
-    int pad;
 };
 
-struct FxCubic {
-    f32x::F2e c[9];
+struct alignas(16) FxCubic {
     f32x::N1e r2;
     int len;
     int pad;
+    f32x::F2e c[9];
 };
+
+static_assert(sizeof(FxOrbitRec) == 32, "FxOrbitRec is two 16-byte halves");
+static_assert(sizeof(FxLinear) % 16 == 0 && sizeof(FxCubic) % 16 == 0, "16-byte block records");
 
 struct DeviceTables {
     int device = -1;

@@ -68,6 +68,24 @@ __device__ __forceinline__ float smooth_from_norm(int iteration, const N1e& n, f
 // Near a periodic reference (|Z| close to 0) that zero flags a glitch the
 // exact norm would not.  This applies the same quantisation to the FP32 norm
 // where it is coarser than the FP32 mantissa.
+// Z_i (floatexp) and the record's norm / margin word in two 16-byte loads.
+__device__ __forceinline__ void orbit_record(const FxOrbitRec* orbit, int i, F2e& z, N1e& z2) {
+    const float4 lo = __ldg(reinterpret_cast<const float4*>(orbit + i));
+    const int4 hi = __ldg(reinterpret_cast<const int4*>(orbit + i) + 1);
+    z = make(lo.z, lo.w, hi.x);
+    z2.m = __int_as_float(hi.y);
+    z2.e = hi.z;
+}
+
+// A block's head (squared radius, length) in one 16-byte load.
+template <typename Step>
+__device__ __forceinline__ void block_head(const Step* s, N1e& r2, int& len) {
+    const int4 h = __ldg(reinterpret_cast<const int4*>(s));
+    r2.m = __int_as_float(h.x);
+    r2.e = h.y;
+    len = h.z;
+}
+
 // The plain-float orbit value Z_i in one 8-byte load (records are 32 bytes
 // from a cudaMalloc base, so zr / zi sit 8-byte aligned).
 __device__ __forceinline__ float2 orbit_float(const FxOrbitRec* orbit, int i) {
@@ -98,8 +116,10 @@ __device__ const Step* find_block(const Step* table, const LevelIndex* index, in
         const int at = offset >> level;
         if (at >= __ldg(&index->count[level])) continue;
         const Step* c = table + __ldg(&index->offset[level]) + at;
-        const N1e r2 = ld_n1e(&c->r2);
-        if (__ldg(&c->len) > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
+        N1e r2;
+        int len;
+        block_head(c, r2, len);
+        if (len > 1 && r2.e != 0x3fffffff && n_cmp(dn, r2) < 0) return c;
     }
     return nullptr;
 }
@@ -473,13 +493,14 @@ __device__ __noinline__ PixelOut floatexp_pixel(const FxParams& p, int px, int p
             result = out_of(static_cast<float>(iteration) - p.output_bias, static_cast<std::uint32_t>(iteration));
             break;
         }
-        const F2e z = ld_f2e(&p.orbit[ref].z);
+        F2e z;
+        N1e z2;
+        orbit_record(p.orbit, ref, z, z2);
         if (!have_total) {
             total = add(z, delta);
             total_norm = reference_norm(norm2(total), p.escape_mode);
         }
         have_total = false;
-        const N1e z2 = ld_n1e(&p.orbit[ref].z2);
         if (z2.m != 0.0f && z2.e != 0x3fffffff) {
             // Glitch when |Z + d|^2 < 1e-7 |Z|^2.
             const N1e bound = n_norm(z2.m * 1.0e-7f, z2.e);
