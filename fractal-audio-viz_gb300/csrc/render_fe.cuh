@@ -227,9 +227,11 @@ __device__ __noinline__ F2e apply_cubic_derivative(const FxCubic* s, const F2e& 
     return add(mul(pd, dd), pc);
 }
 
-// Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).
+// Plain-float tail (the FP32 counterpart of renderer.cpp:12451-12669).  It is
+// the deep pixels' hot loop, so it is inlined into the pixel function: as a
+// call it cost a stack frame's worth of register saves per pixel.
 template <bool Planes>
-__device__ __noinline__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc,
+__device__ __forceinline__ PixelOut float_tail(const FxParams& p, int iteration, int ref, const F2e& delta, const F2e& dc,
                                F2e derivative) {
     const float dcr = to_float_x(dc), dci = to_float_y(dc);
     float dr = to_float_x(delta), di = to_float_y(delta);
