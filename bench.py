@@ -714,9 +714,11 @@ def run_gpu_arm(args) -> int:
                     "path": f"fractal_render_reference_ex (backend {4 if chosen else 0}) / render_fractal_ex "
                             f"into host memory, {E2E_THREADS} host threads"},
             # Per step: direct coordinates + direct queue (when the step has
-            # FP64 direct levels), series prologue + floatexp queue; the plain
-            # form launches the direct pair plus one kernel per deep field.
-            "gpu_launches": args.steps * ((2 if run.fp64_direct else 0) + 2 if chosen else 2 + len(run.deep)),
+            # FP64 direct levels), and a series prologue + floatexp queue per
+            # 64 FP32-queue fields; the plain form launches the direct pair
+            # plus one kernel per deep field.
+            "gpu_launches": args.steps * ((2 if run.fp64_direct else 0) + 2 * ((len(run.floatexp) + 63) // 64)
+                                          if chosen else 2 + len(run.deep)),
             "roofline": roofline,
             "cpu_baseline": cpu,
         }
