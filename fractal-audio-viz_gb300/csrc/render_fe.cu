@@ -14,7 +14,7 @@
 namespace fgb {
 namespace {
 
-__global__ void __launch_bounds__(128) floatexp_kernel(const FxParams p) {
+__global__ void __launch_bounds__(128, 8) floatexp_kernel(const FxParams p) {
     const long long pixels = static_cast<long long>(p.width) * p.height;
     const long long index = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (index >= pixels) return;
