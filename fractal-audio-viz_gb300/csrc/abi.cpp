@@ -1729,13 +1729,41 @@ void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime
 // resident at once (the FP64 direct queue and the FP32 floatexp queue then
 // share every SM instead of waiting on each other).  Shapes change only the
 // schedule, never a pixel.
+// FP32-queue blocks that stay resident on an SM beside `direct_blocks`
+// blocks of the FP64 direct queue: the registers (allocated per warp in
+// units of 256) and shared memory (plus the 1 KB each block reserves) left
+// over, within the FP32 queue's own occupancy and the SM's thread limit.
+int floatexp_blocks_beside(int direct_blocks, bool tiles) {
+    const int alone = floatexp_queue_occupancy(tiles);
+    cudaFuncAttributes fd{}, ff{};
+    int device = 0, sm_regs = 0, sm_smem = 0, sm_threads = 0;
+    if (direct_queue_attributes(&fd) != cudaSuccess || floatexp_queue_attributes(tiles, &ff) != cudaSuccess
+        || cudaGetDevice(&device) != cudaSuccess
+        || cudaDeviceGetAttribute(&sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, device) != cudaSuccess
+        || cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess
+        || cudaDeviceGetAttribute(&sm_threads, cudaDevAttrMaxThreadsPerMultiProcessor, device) != cudaSuccess) {
+        cudaGetLastError();
+        return std::max(1, std::min(direct_queue_occupancy(), alone) - direct_blocks);
+    }
+    auto block_regs = [](const cudaFuncAttributes& a) {
+        return 4 * ((a.numRegs * 32 + 255) / 256 * 256);  // four warps of 128-thread blocks
+    };
+    const int regs_left = sm_regs - direct_blocks * block_regs(fd);
+    const int smem_left = sm_smem - direct_blocks * (static_cast<int>(fd.sharedSizeBytes) + 1024);
+    int blocks = std::min(alone, regs_left / std::max(1, block_regs(ff)));
+    blocks = std::min(blocks, smem_left / (static_cast<int>(ff.sharedSizeBytes) + 1024));
+    blocks = std::min(blocks, (sm_threads - 128 * direct_blocks) / 128);
+    return std::max(1, blocks);
+}
+
 BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stream, bool graph) {
     BatchShapes best;
     const bool both = !plan.direct.empty() && !plan.floatexp.empty();
-    const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
+    const bool tiles = plan.tile_flags != 0;
+    const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(tiles));
     if (both) {
         best.direct.blocks_per_sm = std::max(1, capacity / 2);
-        best.floatexp.blocks_per_sm = std::max(1, capacity - best.direct.blocks_per_sm);
+        best.floatexp.blocks_per_sm = floatexp_blocks_beside(best.direct.blocks_per_sm, tiles);
     }
     cudaEvent_t a = nullptr, b = nullptr;
     check_cuda(cudaEventCreate(&a), "cudaEventCreate");
@@ -1786,7 +1814,7 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
                     if (d == best.direct.blocks_per_sm) continue;
                     BatchShapes s = best;
                     s.direct.blocks_per_sm = d;
-                    s.floatexp.blocks_per_sm = capacity - d;
+                    s.floatexp.blocks_per_sm = floatexp_blocks_beside(d, tiles);
                     c.push_back(s);
                 }
             } else if (!plan.direct.empty()) {
@@ -2050,10 +2078,10 @@ void render_field_batch(const std::vector<FieldRequest>& fields, const char* x_c
         }
     }
     if (!tuned && !plan.direct.empty() && !plan.floatexp.empty()) {
-        // Both queues resident at once: split the SM's blocks between them.
+        // Both queues resident at once: split the SM between them.
         const int capacity = std::min(direct_queue_occupancy(), floatexp_queue_occupancy(plan.tile_flags != 0));
         shapes.direct.blocks_per_sm = std::max(1, capacity / 2);
-        shapes.floatexp.blocks_per_sm = std::max(1, capacity - shapes.direct.blocks_per_sm);
+        shapes.floatexp.blocks_per_sm = floatexp_blocks_beside(shapes.direct.blocks_per_sm, plan.tile_flags != 0);
     }
     if (rt.shapes_pinned) {
         if (rt.pinned_shapes[0] > 0) shapes.direct.chunk = rt.pinned_shapes[0];

@@ -427,9 +427,12 @@ struct TileSchedule {
 int batch_tiles(const FxParams* fields, int count);
 // Fill each field's series_scaled slot (before any launch that renders it).
 cudaError_t launch_series_prologue(const FxParams* fields, int count, cudaStream_t stream);
-// Resident 128-thread blocks per SM of the persistent queue kernels.
+// Resident 128-thread blocks per SM of the persistent queue kernels, and
+// their register / shared-memory use (for sharing an SM between the two).
 int floatexp_queue_occupancy(bool tiles);
 int direct_queue_occupancy();
+cudaError_t floatexp_queue_attributes(bool tiles, cudaFuncAttributes* attributes);
+cudaError_t direct_queue_attributes(cudaFuncAttributes* attributes);
 cudaError_t launch_floatexp_tiles(const FxParams* fields, const float* log_zoom, int count,
                                   unsigned long long* counter, const QueueShape& shape, const TileSchedule& schedule,
                                   cudaStream_t stream);

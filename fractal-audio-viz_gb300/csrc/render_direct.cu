@@ -805,6 +805,10 @@ cudaError_t launch_stamp_time(unsigned long long* slot, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+cudaError_t direct_queue_attributes(cudaFuncAttributes* attributes) {
+    return cudaFuncGetAttributes(attributes, direct_queue_kernel<kFormulaMandelbrot, false>);
+}
+
 int direct_queue_occupancy() {
     int blocks = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, direct_queue_kernel<kFormulaMandelbrot, false>, 128, 0);

@@ -271,6 +271,11 @@ cudaError_t launch_series_prologue(const FxParams* fields, int count, cudaStream
     return cudaGetLastError();
 }
 
+cudaError_t floatexp_queue_attributes(bool tiles, cudaFuncAttributes* attributes) {
+    return tiles ? cudaFuncGetAttributes(attributes, floatexp_tile_kernel)
+                 : cudaFuncGetAttributes(attributes, floatexp_queue_kernel);
+}
+
 int floatexp_queue_occupancy(bool tiles) {
     int blocks = 0;
     if (tiles) {
