@@ -406,8 +406,11 @@ __device__ void finish_parked(const DirectBatch& b, const ParkSlot& e) {
 // never waits on a finished lane: each warp claims chunks of pixels from a
 // device counter over all fields of the batch and refills idle lanes every
 // step from its start stack; escapes are parked and finished 32 at a time.
+// Capped at 64 registers (a few spills): beside the FP32 queue on one SM, a
+// block then takes as many registers as an FP32-queue block, so two of each
+// kind fit where 80-register blocks left room for fewer.
 template <int Formula, bool Planes>
-__global__ void __launch_bounds__(128) direct_queue_kernel(const __grid_constant__ DirectBatch b) {
+__global__ void __launch_bounds__(128, 8) direct_queue_kernel(const __grid_constant__ DirectBatch b) {
     constexpr unsigned kFull = 0xffffffffu;
     __shared__ WarpStage stages[4];
     WarpStage& st = stages[threadIdx.x >> 5];
