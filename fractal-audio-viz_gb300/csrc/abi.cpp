@@ -88,7 +88,13 @@ ThreadRuntime& thread_runtime() {
         check_cuda(cudaEventCreate(&rt.start), "cudaEventCreate");
         check_cuda(cudaEventCreate(&rt.stop), "cudaEventCreate");
         check_cuda(cudaEventCreateWithFlags(&rt.scratch_done, cudaEventDisableTiming), "cudaEventCreate");
-        check_cuda(cudaStreamCreateWithFlags(&rt.side, cudaStreamNonBlocking), "cudaStreamCreate");
+        // The FP64 direct queue's stream has the highest priority: when both
+        // persistent queues are launched, its blocks are placed first, and
+        // FP32-queue blocks beyond what fits beside them start as its blocks
+        // finish (see the autotuner's over-subscribed candidates).
+        int least = 0, greatest = 0;
+        check_cuda(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
+        check_cuda(cudaStreamCreateWithPriority(&rt.side, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
         check_cuda(cudaStreamCreateWithFlags(&rt.capture, cudaStreamNonBlocking), "cudaStreamCreate");
         check_cuda(cudaEventCreateWithFlags(&rt.fork, cudaEventDisableTiming), "cudaEventCreate");
         check_cuda(cudaEventCreateWithFlags(&rt.join, cudaEventDisableTiming), "cudaEventCreate");
@@ -1810,12 +1816,21 @@ BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stre
                 }
             }
             if (both) {
+                // Co-resident splits, and the FP32 queue at its full
+                // occupancy: the blocks that do not fit beside the direct
+                // queue's start when its blocks finish.
+                const int full = floatexp_queue_occupancy(tiles);
                 for (int d = 1; d < capacity; ++d) {
-                    if (d == best.direct.blocks_per_sm) continue;
-                    BatchShapes s = best;
-                    s.direct.blocks_per_sm = d;
-                    s.floatexp.blocks_per_sm = floatexp_blocks_beside(d, tiles);
-                    c.push_back(s);
+                    // Full occupancy is tried with every direct share, or for
+                    // batches of a second or more with the best one so far.
+                    const bool try_full = repeats > 1 || d == best.direct.blocks_per_sm;
+                    for (int f : {floatexp_blocks_beside(d, tiles), try_full ? full : 0}) {
+                        if (f == 0 || (d == best.direct.blocks_per_sm && f == best.floatexp.blocks_per_sm)) continue;
+                        BatchShapes s = best;
+                        s.direct.blocks_per_sm = d;
+                        s.floatexp.blocks_per_sm = f;
+                        c.push_back(s);
+                    }
                 }
             } else if (!plan.direct.empty()) {
                 for (int d : {2, 4, 6, 0}) {
