@@ -9,7 +9,7 @@ max_iterations(min(100, (i+1)*log10(8)), 2000, 3000, 200000)
 point (tests/golden/centres.json "fhd_stack_e50", 1200-bit Newton, 360
 digits).  Levels below 1e12 are direct-path levels, deeper ones render from
 the shared MPFR reference and its BLA tiers, as the reference pipeline does.
-configs[1]'s 55-keyframe stack (levels 0..54, to 1e48.8, caps up to 151k,
+The 55-keyframe FHD stack (levels 0..54, to 1e48.8, caps up to 151k,
 `fhd_keyframe_stack`) is measured beside it.  Work unit: a pixel-iteration,
 i.e. the sum of uint32 iteration counts (escape index, or the cap for
 interior pixels); iterations skipped by the image series or BLA count as
@@ -401,7 +401,7 @@ def run_dry(args) -> int:
 
 
 def measure_batch_mix(package, library, stream, steps: int, local_rank: int) -> dict:
-    """configs[2]: 64 seeded fields mixing the four formulas and the four
+    """The mixed batch: 64 seeded fields mixing the four formulas and the four
     sizes 720x480 .. 3840x2160, zooms log-uniform 1e10-1e100, caps
     log-uniform 1e4-1e6, counts + smooth field + derivative planes, all in
     one fractal_gb300_render_fields_device call (graph replay, launch
@@ -620,7 +620,7 @@ def run_gpu_arm(args) -> int:
         e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * work * e2e_steps / e2e_s / 1e9
 
-    # configs[1]'s 55-keyframe stack beside the headline (N=1 replica 0 only).
+    # The 55-keyframe FHD stack beside the headline (N=1 replica 0 only).
     second = None
     if rank == 0 and args.workload == HEADLINE and not args.headline_only:
         del run.fields, run.counts

@@ -224,7 +224,7 @@ def kfp_cases() -> list[dict]:
     return cases
 
 
-# The batch workload (configs[2]): field sizes and its zoom and cap ranges.
+# The mixed batch workload: field sizes and its zoom and cap ranges.
 BATCH_SIZES = ((720, 480), (1280, 720), (1920, 1080), (3840, 2160))
 
 
