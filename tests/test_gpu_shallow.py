@@ -5,7 +5,7 @@ Below 1e12 the reference pipeline renders a field by direct FP64 iteration
 those fields by plain FP32 perturbation against the stack's root reference
 orbit, from iteration 0 with unlimited rebasing (FxParams::shallow).  Its
 counts may differ from the FP64 form only where rounding decides an escape
-iteration; the benchmark spec's budget for the chosen form is 1e-4 of pixels,
+iteration; the floatexp form's budget is 1e-4 of pixels,
 the tolerance used here (plus two pixels of slack per field set).
 """
 
