@@ -48,6 +48,26 @@ def test_zoom_plan_matches_reference(song):
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)
 
 
+def test_zoom_plan_edge_cases_match_reference(song):
+    """A single frame, no zoom range, silence (no net motion: the crawl
+    forward) and two silent frames, against the reference's own plan."""
+    if not os.path.isfile(os.path.join(REFERENCE_SOURCES, "visualizer.py")):
+        pytest.skip("reference sources are not present on this machine")
+    sys.path.insert(0, REFERENCE_SOURCES)
+    try:
+        import visualizer  # noqa: PLC0415  (reference pipeline, read-only)
+    finally:
+        sys.path.remove(REFERENCE_SOURCES)
+    cases = ((np.array([0.5]), 10.0), (np.array([0.2, 0.4, 0.9]), 0.0), (np.zeros(5), 5.0),
+             (np.zeros(2), 3.0), (np.full(7, 0.01), 40.0))
+    for loud, top in cases:
+        want = visualizer._zoom_plan(loud, 1.0, 10.0 ** top, 3.0, -0.04, None, 0.0)
+        got = song.zoom_plan(loud, 0.0, top, 3.0, -0.04, None, 0.0)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)
+    with pytest.raises(ValueError):
+        song.zoom_plan(np.zeros(0), 0.0, 10.0)
+
+
 def test_synthetic_song_and_controls(song):
     audio = song.synthesize(seconds=6.0)
     assert audio.shape == (6 * 44_100, 2) and audio.dtype == np.float32
