@@ -1725,16 +1725,6 @@ void launch_plan(const BatchPlan& plan, const BatchShapes& shapes, ThreadRuntime
     check_cuda(cudaGraphLaunch(found->second, stream), "cudaGraphLaunch");
 }
 
-// Coordinate descent over the launch shapes, each candidate timed once with
-// CUDA events on the batch itself.  Shapes change only the schedule, never a
-// pixel: every candidate renders the same values.
-// Coordinate descent over the launch shapes, each candidate timed (median of
-// three, CUDA events) on the batch itself and through the same launch path
-// (graph replay or direct enqueue) the batch will use.  When the batch has
-// both queues, their blocks per SM are chosen together so both stay
-// resident at once (the FP64 direct queue and the FP32 floatexp queue then
-// share every SM instead of waiting on each other).  Shapes change only the
-// schedule, never a pixel.
 // FP32-queue blocks that stay resident on an SM beside `direct_blocks`
 // blocks of the FP64 direct queue: the registers (allocated per warp in
 // units of 256) and shared memory (plus the 1 KB each block reserves) left
@@ -1762,6 +1752,15 @@ int floatexp_blocks_beside(int direct_blocks, bool tiles) {
     return std::max(1, blocks);
 }
 
+// Coordinate descent over the launch shapes, each candidate timed (median of
+// three, or one run for batches of a second or more; CUDA events) on the
+// batch itself and through the same launch path (graph replay or direct
+// enqueue) the batch will use.  When the batch has both queues, their
+// blocks per SM are chosen together: splits where both stay resident (the
+// FP64 direct queue and the FP32 queue then share every SM instead of
+// waiting on each other), and the FP32 queue at its full occupancy, whose
+// extra blocks start as the direct queue's (placed first: its stream has the
+// highest priority) finish.  Shapes change only the schedule, never a pixel.
 BatchShapes autotune(const BatchPlan& plan, ThreadRuntime& rt, cudaStream_t stream, bool graph) {
     BatchShapes best;
     const bool both = !plan.direct.empty() && !plan.floatexp.empty();
